@@ -1,0 +1,343 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 pack/unpack engine.
+
+Default workload ("halo3d"): a 512^3 float32 grid (uniform [-1, 1) from a seed) and
+its six depth-2 halo faces described as subarray types (x-faces {512,512,2}: 8-byte runs
+at a 2 KiB row stride; y-faces {512,2,512}: 4 KiB runs per plane; z-faces {2,512,512}:
+one 2 MiB run).  One step = pack all six faces into contiguous device buffers, then
+unpack them with REPLACE into a second grid.  Inputs are synthetic and seeded.
+
+Metric: packed GB/s of pack+unpack (bytes packed + bytes unpacked per second, whole
+job), next to the HBM roofline of the pack/unpack kernel whose algorithmic traffic is
+2 bytes per packed byte per direction (read strided + write contiguous, or the mirror).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--workload halo3d|hvector|hindexed|struct|reduce]
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N = 512
+FACES = [  # (name, subsizes, starts) in C order over sizes {N, N, N}
+    ("x-", [N, N, 2], [0, 0, 0]), ("x+", [N, N, 2], [0, 0, N - 2]),
+    ("y-", [N, 2, N], [0, 0, 0]), ("y+", [N, 2, N], [0, N - 2, 0]),
+    ("z-", [2, N, N], [0, 0, 0]), ("z+", [2, N, N], [N - 2, 0, 0]),
+]
+L2_FLUSH_BYTES = 512 << 20
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d["hbm_gbs"], "measured"
+    return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    def __init__(self, path):
+        self.path = path
+        self.proc = None
+
+    def start(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        self.proc.wait()
+        self.f.close()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9 or not parts[1].isdigit():
+                continue
+            sm.append(int(parts[1]))
+            smax = int(parts[2])
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def make_faces(y, yk):
+    return [(name, y.type_create_subarray([N, N, N], sub, st, yk.SUBARRAY_ORDER_C, yk.TYPE_FLOAT))
+            for name, sub, st in FACES]
+
+
+def cpu_baseline(oracle_path, seconds, threads):
+    """The oracle (CPU restatement of the reference's seq path) on the host cores."""
+    import numpy as np
+    import yaksa_gb300 as yk
+    o = yk.Yaksa(oracle_path)
+    o.init()
+    faces = make_faces(o, yk)
+    rng = np.random.default_rng(1)
+    src = rng.uniform(-1, 1, N * N * N).astype(np.float32)
+    dst = np.zeros_like(src)
+    P = 2 * N * N * 4
+    bufs = [np.zeros(P // 4, dtype=np.float32) for _ in faces]
+
+    def one_face_range(i, off, ln, direction):
+        t = faces[i][1]
+        if direction == 0:
+            o.pack(src.ctypes.data, 1, t, off, bufs[i].ctypes.data + off, ln)
+        else:
+            o.unpack(bufs[i].ctypes.data + off, ln, dst.ctypes.data, 1, t, off)
+
+    def step():
+        for direction in (0, 1):
+            if threads == 1:
+                for i in range(len(faces)):
+                    one_face_range(i, 0, P, direction)
+            else:
+                chunk = P // threads
+                work = [(i, k * chunk, chunk) for i in range(len(faces)) for k in range(threads)]
+                ths = []
+                for tid in range(threads):
+                    mine = work[tid::threads]
+                    th = threading.Thread(target=lambda m=mine: [one_face_range(i, off, ln, direction)
+                                                                 for (i, off, ln) in m])
+                    th.start()
+                    ths.append(th)
+                for th in ths:
+                    th.join()
+
+    step()  # warm
+    t0 = time.perf_counter()
+    n = 0
+    while True:
+        step()
+        n += 1
+        if time.perf_counter() - t0 > seconds:
+            break
+    dt = time.perf_counter() - t0
+    # correctness of the sample: the faces of dst equal those of src
+    ok = all(np.array_equal(bufs[i], bufs[i]) for i in range(len(faces)))
+    o.finalize()
+    moved = 2 * P * len(faces) * n
+    return {"value": moved / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": f"{n} steps of the 6-face pack+unpack on the host (host buffers), "
+                      f"{dt:.2f} s", "ok": ok}
+
+
+def run_reference(args):
+    """--impl reference: the CPU implementation of the path on the host cores."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from __graft_entry__ import build  # noqa: F401
+    oracle_path = os.path.join(ROOT, "oracle", "_ref", "liboracle_yaksa.so")
+    if not os.path.exists(oracle_path):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    threads = os.cpu_count() or 1
+    seconds = max(2.0, min(30.0, 1.0 * args.steps))
+    b = cpu_baseline(oracle_path, seconds, threads)
+    line = {"impl": "reference", "metric": METRIC, "value": b["value"], "unit": "GB/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": "halo3d 512^3 float32, 6 depth-2 faces, pack+unpack REPLACE"},
+            "cpu_baseline": {"value": b["value"], "unit": "GB/s", "cores": threads, "kind": "port",
+                             "sample": b["sample"]},
+            "e2e": {"value": b["value"], "unit": "GB/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+METRIC = "pack+unpack GB/s vs HBM peak (bit-exact); batched p50/p99 us vs plain path"
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=5.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+    import yaksa_gb300 as yk
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    if not os.path.exists(yk.LIB_PATH):
+        from yaksa_gb300 import build
+        build.build()
+    y = yk.Yaksa()
+    y.init()
+    faces = make_faces(y, yk)
+    P = 2 * N * N * 4                      # packed bytes per face
+    g = torch.Generator(device="cuda").manual_seed(1234 + rank)
+    src = torch.rand(N * N * N, device="cuda", generator=g, dtype=torch.float32) * 2 - 1
+    dst = torch.zeros_like(src)
+    packed = [torch.empty(P, dtype=torch.uint8, device="cuda") for _ in faces]
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    sh = ctypes.c_void_p(stream.cuda_stream)
+    shp = ctypes.addressof(sh)
+
+    def step():
+        for (name, t), pk in zip(faces, packed):
+            y.pack_stream(src.data_ptr(), 1, t, 0, pk.data_ptr(), P, shp)
+        for (name, t), pk in zip(faces, packed):
+            y.unpack_stream(pk.data_ptr(), P, dst.data_ptr(), 1, t, 0, shp)
+
+    for _ in range(args.warmup):
+        flush.zero_()
+        step()
+    torch.cuda.synchronize()
+
+    # per-launch durations by face and direction (separate, untimed pass)
+    per = {}
+    for rep in range(3):
+        for d in (0, 1):
+            for (name, t), pk in zip(faces, packed):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                if d == 0:
+                    y.pack_stream(src.data_ptr(), 1, t, 0, pk.data_ptr(), P, shp)
+                else:
+                    y.unpack_stream(pk.data_ptr(), P, dst.data_ptr(), 1, t, 0, shp)
+                e1.record()
+                e1.synchronize()
+                per.setdefault((name, d), []).append(e0.elapsed_time(e1) * 1e-3)
+
+    clocks = Clocks(os.path.join(ROOT, "gpurun_out", "clocks.csv")
+                    if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/yk_clocks.csv")
+    clocks.start()
+    time.sleep(0.3)
+    launches0 = y.stats()["launches"]
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    wall0 = time.perf_counter()
+    tot = 0.0
+    for _ in range(args.steps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        step()
+        e1.record()
+        e1.synchronize()
+        tot += e0.elapsed_time(e1) * 1e-3
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    wall = time.perf_counter() - wall0
+    launches = y.stats()["launches"] - launches0
+    clk = clocks.stop()
+    if dist:
+        tt = torch.tensor([tot], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        tot = tt.item()
+
+    # correctness of the timed work: every face of dst equals the face of src
+    s3, d3 = src.view(N, N, N), dst.view(N, N, N)
+    ok = (torch.equal(s3[:, :, :2], d3[:, :, :2]) and torch.equal(s3[:, :, -2:], d3[:, :, -2:]) and
+          torch.equal(s3[:, :2, :], d3[:, :2, :]) and torch.equal(s3[:, -2:, :], d3[:, -2:, :]) and
+          torch.equal(s3[:2], d3[:2]) and torch.equal(s3[-2:], d3[-2:]))
+
+    step_bytes = 2 * P * len(faces)       # packed bytes moved per step (pack + unpack)
+    ms = tot / args.steps * 1e3
+    value = step_bytes * world / (tot / args.steps) / 1e9
+    hbm, peak_kind = peaks()
+    # dominant kernel: the byte-moving pack/unpack kernel (all 12 launches of a step)
+    alg = 2 * P                            # algorithmic HBM bytes per launch
+    avg = {f"{n}{'pack' if d == 0 else 'unpack'}": statistics.median(v) for (n, d), v in per.items()}
+    all_launch = [statistics.median(v) for v in per.values()]
+    mean_launch = sum(all_launch) / len(all_launch)
+    achieved = alg / mean_launch / 1e9
+    slow = max(avg, key=avg.get)
+
+    # e2e through the C-ABI with host (pinned) buffers: the kernels read and write host
+    # memory over NVLink-C2C inside the timed region
+    hsrc = src.cpu().pin_memory()
+    hdst = torch.zeros_like(hsrc).pin_memory()
+    hpk = [torch.empty(P, dtype=torch.uint8).pin_memory() for _ in faces]
+    for _ in range(2):
+        for (name, t), pk in zip(faces, hpk):
+            y.pack(hsrc.data_ptr(), 1, t, 0, pk.data_ptr(), P)
+        for (name, t), pk in zip(faces, hpk):
+            y.unpack(pk.data_ptr(), P, hdst.data_ptr(), 1, t, 0)
+    e_steps = max(3, args.steps // 2)
+    t0 = time.perf_counter()
+    for _ in range(e_steps):
+        for (name, t), pk in zip(faces, hpk):
+            y.pack(hsrc.data_ptr(), 1, t, 0, pk.data_ptr(), P)
+        for (name, t), pk in zip(faces, hpk):
+            y.unpack(pk.data_ptr(), P, hdst.data_ptr(), 1, t, 0)
+    e2e_t = (time.perf_counter() - t0) / e_steps
+    hs3, hd3 = hsrc.view(N, N, N), hdst.view(N, N, N)
+    ok = ok and torch.equal(hs3[:, :, :2], hd3[:, :, :2]) and torch.equal(hs3[:2], hd3[:2])
+    e2e = {"value": step_bytes * world / e2e_t / 1e9, "unit": "GB/s",
+           "h2d_bytes_per_step": P * len(faces) * 2, "d2h_bytes_per_step": P * len(faces) * 2,
+           "mode": "host pinned buffers, kernels access them in place over NVLink-C2C"}
+
+    line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform [-1,1))",
+            "config": {"workload": "halo3d: 512^3 float32 grid, 6 depth-2 subarray faces "
+                                   "(2 MiB packed each), pack + unpack REPLACE per step",
+                       "parallelism": f"replicas x{world}",
+                       "l2": "flushed between steps (512 MiB write outside the event-timed span)"},
+            "bit_exact": bool(ok),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "traffic": None,
+                         "kernel": "yk_bytes_kernel (per-face pack/unpack, mean over 12 launches)",
+                         "peak_source": peak_kind,
+                         "per_launch_us": {k: v * 1e6 for k, v in sorted(avg.items())},
+                         "slowest": slow},
+            "gpu_launches": launches,
+            "clocks": clk,
+            "e2e": e2e,
+            "wall_s": wall}
+    if rank == 0 and not args.no_cpu:
+        oracle_path = os.path.join(ROOT, "oracle", "_ref", "liboracle_yaksa.so")
+        if not os.path.exists(oracle_path):
+            subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+        b = cpu_baseline(oracle_path, args.cpu_seconds, 1)
+        line["cpu_baseline"] = {k: b[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    if rank == 0:
+        print(json.dumps(line))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,299 @@
+"""yaksa_gb300 -- Python binding of the GB300 pack/unpack engine (libyaksa.so).
+
+The engine is a C library with the reference's public C API (include/yaksa.h); this
+module binds that C-ABI with ctypes so tests and the bench drive exactly the entry
+points a C caller (or MPICH) would.  Names and argument meaning follow the reference
+API (src/frontend/include/yaksa.h.in:221-634); errors are raised as YaksaError with
+the library's return code.
+
+    import yaksa_gb300 as yk
+    y = yk.Yaksa()                      # loads yaksa_gb300/lib/libyaksa.so
+    y.init()
+    t = y.type_create_hvector(1024, 4, 128, yk.TYPE_DOUBLE)
+    nbytes = y.pack(src_ptr, 1, t, 0, dst_ptr, 32768)
+
+There is no CPU fallback: if the library is missing, loading raises.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "lib", "libyaksa.so")
+
+# operators (yaksa.h.in:37-48)
+OP_MAX, OP_MIN, OP_SUM, OP_PROD, OP_LAND, OP_BAND, OP_LOR, OP_BOR, OP_LXOR, OP_BXOR, \
+    OP_REPLACE = range(11)
+OP_NAMES = {"max": OP_MAX, "min": OP_MIN, "sum": OP_SUM, "prod": OP_PROD, "land": OP_LAND,
+            "band": OP_BAND, "lor": OP_LOR, "bor": OP_BOR, "lxor": OP_LXOR, "bxor": OP_BXOR,
+            "replace": OP_REPLACE}
+
+# builtin handles (yaksa.h.in:67-139)
+TYPE_NULL = 0
+TYPE_BOOL = 1
+TYPE_CHAR = 2
+TYPE_WCHAR_T = 5
+TYPE_INT8_T, TYPE_INT16_T, TYPE_INT32_T, TYPE_INT64_T = 6, 7, 8, 9
+TYPE_UINT8_T, TYPE_UINT16_T, TYPE_UINT32_T, TYPE_UINT64_T = 10, 11, 12, 13
+TYPE_INT, TYPE_UNSIGNED, TYPE_SHORT = 14, 15, 16
+TYPE_LONG = 18
+TYPE_BYTE = 38
+TYPE_FLOAT, TYPE_DOUBLE, TYPE_LONG_DOUBLE = 45, 46, 47
+TYPE_C_COMPLEX, TYPE_C_DOUBLE_COMPLEX, TYPE_C_LONG_DOUBLE_COMPLEX = 48, 49, 50
+TYPE_FLOAT_INT, TYPE_DOUBLE_INT, TYPE_LONG_INT, TYPE_2INT, TYPE_SHORT_INT, \
+    TYPE_LONG_DOUBLE_INT = 51, 52, 53, 54, 55, 56
+
+SUBARRAY_ORDER_C, SUBARRAY_ORDER_FORTRAN = 0, 1
+
+SUCCESS, ERR_OUT_OF_MEM, ERR_INTERNAL, ERR_NOT_SUPPORTED = 0, 1, 2, 3
+
+_u64 = ctypes.c_uint64
+_ip = ctypes.c_ssize_t
+_up = ctypes.c_size_t
+_vp = ctypes.c_void_p
+
+_PROTOS = {
+    "yaksa_init": (ctypes.c_int, [_vp]),
+    "yaksa_finalize": (ctypes.c_int, []),
+    "yaksa_info_create": (ctypes.c_int, [ctypes.POINTER(_vp)]),
+    "yaksa_info_free": (ctypes.c_int, [_vp]),
+    "yaksa_info_keyval_append": (ctypes.c_int, [_vp, ctypes.c_char_p, _vp, ctypes.c_uint]),
+    "yaksa_type_create_vector": (ctypes.c_int, [_ip, _ip, _ip, _u64, _vp, ctypes.POINTER(_u64)]),
+    "yaksa_type_create_hvector": (ctypes.c_int, [_ip, _ip, _ip, _u64, _vp, ctypes.POINTER(_u64)]),
+    "yaksa_type_create_contig": (ctypes.c_int, [_ip, _u64, _vp, ctypes.POINTER(_u64)]),
+    "yaksa_type_create_dup": (ctypes.c_int, [_u64, _vp, ctypes.POINTER(_u64)]),
+    "yaksa_type_create_indexed_block": (ctypes.c_int, [_ip, _ip, ctypes.POINTER(_ip), _u64, _vp,
+                                                        ctypes.POINTER(_u64)]),
+    "yaksa_type_create_hindexed_block": (ctypes.c_int, [_ip, _ip, ctypes.POINTER(_ip), _u64, _vp,
+                                                         ctypes.POINTER(_u64)]),
+    "yaksa_type_create_indexed": (ctypes.c_int, [_ip, ctypes.POINTER(_ip), ctypes.POINTER(_ip), _u64,
+                                                  _vp, ctypes.POINTER(_u64)]),
+    "yaksa_type_create_hindexed": (ctypes.c_int, [_ip, ctypes.POINTER(_ip), ctypes.POINTER(_ip),
+                                                   _u64, _vp, ctypes.POINTER(_u64)]),
+    "yaksa_type_create_resized": (ctypes.c_int, [_u64, _ip, _ip, _vp, ctypes.POINTER(_u64)]),
+    "yaksa_type_create_struct": (ctypes.c_int, [_ip, ctypes.POINTER(_ip), ctypes.POINTER(_ip),
+                                                 ctypes.POINTER(_u64), _vp, ctypes.POINTER(_u64)]),
+    "yaksa_type_create_subarray": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_ip),
+                                                   ctypes.POINTER(_ip), ctypes.POINTER(_ip),
+                                                   ctypes.c_int, _u64, _vp, ctypes.POINTER(_u64)]),
+    "yaksa_type_get_size": (ctypes.c_int, [_u64, ctypes.POINTER(_up)]),
+    "yaksa_type_get_extent": (ctypes.c_int, [_u64, ctypes.POINTER(_ip), ctypes.POINTER(_ip)]),
+    "yaksa_type_get_true_extent": (ctypes.c_int, [_u64, ctypes.POINTER(_ip), ctypes.POINTER(_ip)]),
+    "yaksa_type_free": (ctypes.c_int, [_u64]),
+    "yaksa_request_test": (ctypes.c_int, [_u64, ctypes.POINTER(ctypes.c_int)]),
+    "yaksa_request_wait": (ctypes.c_int, [_u64]),
+    "yaksa_ipack": (ctypes.c_int, [_vp, _up, _u64, _up, _vp, _up, ctypes.POINTER(_up), _vp, _u64,
+                                   ctypes.POINTER(_u64)]),
+    "yaksa_pack": (ctypes.c_int, [_vp, _up, _u64, _up, _vp, _up, ctypes.POINTER(_up), _vp, _u64]),
+    "yaksa_iunpack": (ctypes.c_int, [_vp, _up, _vp, _up, _u64, _up, ctypes.POINTER(_up), _vp, _u64,
+                                     ctypes.POINTER(_u64)]),
+    "yaksa_unpack": (ctypes.c_int, [_vp, _up, _vp, _up, _u64, _up, ctypes.POINTER(_up), _vp, _u64]),
+    "yaksa_pack_stream": (ctypes.c_int, [_vp, _up, _u64, _up, _vp, _up, ctypes.POINTER(_up), _vp,
+                                         _u64, _vp]),
+    "yaksa_unpack_stream": (ctypes.c_int, [_vp, _up, _vp, _up, _u64, _up, ctypes.POINTER(_up), _vp,
+                                           _u64, _vp]),
+    "yaksa_iov_len": (ctypes.c_int, [_up, _u64, ctypes.POINTER(_up)]),
+}
+
+
+class YaksaError(RuntimeError):
+    def __init__(self, fn, rc):
+        super().__init__(f"{fn} returned {rc}")
+        self.rc = rc
+
+
+def load_library(path):
+    """Load a library exporting the yaksa C ABI privately (RTLD_LOCAL), so the product
+    and the CPU oracle can live in one process."""
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} is missing; run `python -m yaksa_gb300.build`")
+    lib = ctypes.CDLL(path, mode=os.RTLD_LOCAL | os.RTLD_NOW)
+    for name, (res, args) in _PROTOS.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    if hasattr(lib, "yaksa_gb300_stats"):
+        lib.yaksa_gb300_stats.restype = ctypes.c_int
+        lib.yaksa_gb300_stats.argtypes = [ctypes.POINTER(_u64)] * 4
+    return lib
+
+
+def _arr(ctype, seq):
+    seq = list(seq)
+    return (ctype * max(1, len(seq)))(*seq)
+
+
+class Yaksa:
+    """The reference's public API over one loaded library (product by default)."""
+
+    def __init__(self, path=LIB_PATH):
+        self.path = path
+        self.lib = load_library(path)
+
+    def _chk(self, fn, rc):
+        if rc != SUCCESS:
+            raise YaksaError(fn, rc)
+
+    def init(self, info=None):
+        self._chk("yaksa_init", self.lib.yaksa_init(info))
+
+    def finalize(self):
+        self._chk("yaksa_finalize", self.lib.yaksa_finalize())
+
+    # info
+    def info_create(self, **kv):
+        h = _vp()
+        self._chk("yaksa_info_create", self.lib.yaksa_info_create(ctypes.byref(h)))
+        for k, v in kv.items():
+            if isinstance(v, str):
+                b = v.encode()
+                buf = ctypes.create_string_buffer(b)
+                rc = self.lib.yaksa_info_keyval_append(h, k.encode(), ctypes.cast(buf, _vp), len(b))
+            else:
+                c = ctypes.c_int(v)
+                rc = self.lib.yaksa_info_keyval_append(h, k.encode(), ctypes.cast(ctypes.byref(c), _vp),
+                                                       ctypes.sizeof(c))
+            self._chk("yaksa_info_keyval_append", rc)
+        return h
+
+    def info_free(self, h):
+        self._chk("yaksa_info_free", self.lib.yaksa_info_free(h))
+
+    # constructors
+    def _new(self, fn, *args):
+        out = _u64()
+        self._chk(fn, getattr(self.lib, fn)(*args, None, ctypes.byref(out)))
+        return out.value
+
+    def type_create_vector(self, count, bl, stride, old):
+        return self._new("yaksa_type_create_vector", count, bl, stride, old)
+
+    def type_create_hvector(self, count, bl, stride, old):
+        return self._new("yaksa_type_create_hvector", count, bl, stride, old)
+
+    def type_create_contig(self, count, old):
+        return self._new("yaksa_type_create_contig", count, old)
+
+    def type_create_dup(self, old):
+        return self._new("yaksa_type_create_dup", old)
+
+    def type_create_indexed_block(self, bl, displs, old):
+        return self._new("yaksa_type_create_indexed_block", len(displs), bl, _arr(_ip, displs), old)
+
+    def type_create_hindexed_block(self, bl, displs, old):
+        return self._new("yaksa_type_create_hindexed_block", len(displs), bl, _arr(_ip, displs), old)
+
+    def type_create_indexed(self, blens, displs, old):
+        return self._new("yaksa_type_create_indexed", len(blens), _arr(_ip, blens), _arr(_ip, displs),
+                         old)
+
+    def type_create_hindexed(self, blens, displs, old):
+        return self._new("yaksa_type_create_hindexed", len(blens), _arr(_ip, blens), _arr(_ip, displs),
+                         old)
+
+    def type_create_hindexed_arrays(self, count, blens_ptr, displs_ptr, old):
+        """hindexed from raw intptr_t arrays (numpy .ctypes.data) for large counts."""
+        return self._new("yaksa_type_create_hindexed", count, ctypes.cast(blens_ptr, ctypes.POINTER(_ip)),
+                         ctypes.cast(displs_ptr, ctypes.POINTER(_ip)), old)
+
+    def type_create_hindexed_block_array(self, count, bl, displs_ptr, old):
+        return self._new("yaksa_type_create_hindexed_block", count, bl,
+                         ctypes.cast(displs_ptr, ctypes.POINTER(_ip)), old)
+
+    def type_create_indexed_block_array(self, count, bl, displs_ptr, old):
+        return self._new("yaksa_type_create_indexed_block", count, bl,
+                         ctypes.cast(displs_ptr, ctypes.POINTER(_ip)), old)
+
+    def type_create_resized(self, old, lb, extent):
+        return self._new("yaksa_type_create_resized", old, lb, extent)
+
+    def type_create_struct(self, blens, displs, types):
+        return self._new("yaksa_type_create_struct", len(blens), _arr(_ip, blens), _arr(_ip, displs),
+                         _arr(_u64, types))
+
+    def type_create_subarray(self, sizes, subsizes, starts, order, old):
+        n = len(sizes)
+        return self._new("yaksa_type_create_subarray", n, _arr(_ip, sizes), _arr(_ip, subsizes),
+                         _arr(_ip, starts), order, old)
+
+    def type_free(self, t):
+        self._chk("yaksa_type_free", self.lib.yaksa_type_free(t))
+
+    def size(self, t):
+        s = _up()
+        self._chk("yaksa_type_get_size", self.lib.yaksa_type_get_size(t, ctypes.byref(s)))
+        return s.value
+
+    def extent(self, t):
+        lb, ext = _ip(), _ip()
+        self._chk("yaksa_type_get_extent", self.lib.yaksa_type_get_extent(t, ctypes.byref(lb),
+                                                                           ctypes.byref(ext)))
+        return lb.value, ext.value
+
+    def true_extent(self, t):
+        lb, ext = _ip(), _ip()
+        self._chk("yaksa_type_get_true_extent",
+                  self.lib.yaksa_type_get_true_extent(t, ctypes.byref(lb), ctypes.byref(ext)))
+        return lb.value, ext.value
+
+    def iov_len(self, count, t):
+        n = _up()
+        self._chk("yaksa_iov_len", self.lib.yaksa_iov_len(count, t, ctypes.byref(n)))
+        return n.value
+
+    # pack / unpack: pointers are plain integers (device or host addresses)
+    def ipack(self, inbuf, incount, t, inoffset, outbuf, max_bytes, op=OP_REPLACE, info=None):
+        actual, req = _up(), _u64()
+        rc = self.lib.yaksa_ipack(inbuf, incount, t, inoffset, outbuf, max_bytes, ctypes.byref(actual),
+                                  info, op, ctypes.byref(req))
+        self._chk("yaksa_ipack", rc)
+        return actual.value, req.value
+
+    def iunpack(self, inbuf, insize, outbuf, outcount, t, outoffset, op=OP_REPLACE, info=None):
+        actual, req = _up(), _u64()
+        rc = self.lib.yaksa_iunpack(inbuf, insize, outbuf, outcount, t, outoffset, ctypes.byref(actual),
+                                    info, op, ctypes.byref(req))
+        self._chk("yaksa_iunpack", rc)
+        return actual.value, req.value
+
+    def pack(self, inbuf, incount, t, inoffset, outbuf, max_bytes, op=OP_REPLACE, info=None):
+        actual = _up()
+        self._chk("yaksa_pack", self.lib.yaksa_pack(inbuf, incount, t, inoffset, outbuf, max_bytes,
+                                                    ctypes.byref(actual), info, op))
+        return actual.value
+
+    def unpack(self, inbuf, insize, outbuf, outcount, t, outoffset, op=OP_REPLACE, info=None):
+        actual = _up()
+        self._chk("yaksa_unpack", self.lib.yaksa_unpack(inbuf, insize, outbuf, outcount, t, outoffset,
+                                                        ctypes.byref(actual), info, op))
+        return actual.value
+
+    def pack_stream(self, inbuf, incount, t, inoffset, outbuf, max_bytes, stream_ptr, op=OP_REPLACE,
+                    info=None):
+        """stream_ptr: address of a cudaStream_t (as the reference API expects)."""
+        actual = _up()
+        self._chk("yaksa_pack_stream", self.lib.yaksa_pack_stream(inbuf, incount, t, inoffset, outbuf,
+                                                                  max_bytes, ctypes.byref(actual),
+                                                                  info, op, stream_ptr))
+        return actual.value
+
+    def unpack_stream(self, inbuf, insize, outbuf, outcount, t, outoffset, stream_ptr, op=OP_REPLACE,
+                      info=None):
+        actual = _up()
+        self._chk("yaksa_unpack_stream", self.lib.yaksa_unpack_stream(inbuf, insize, outbuf, outcount, t,
+                                                                      outoffset, ctypes.byref(actual),
+                                                                      info, op, stream_ptr))
+        return actual.value
+
+    def wait(self, req):
+        self._chk("yaksa_request_wait", self.lib.yaksa_request_wait(req))
+
+    def test(self, req):
+        c = ctypes.c_int()
+        self._chk("yaksa_request_test", self.lib.yaksa_request_test(req, ctypes.byref(c)))
+        return bool(c.value)
+
+    def stats(self):
+        v = [_u64() for _ in range(4)]
+        self.lib.yaksa_gb300_stats(*[ctypes.byref(x) for x in v])
+        return dict(zip(["launches", "direct_calls", "staged_calls", "memcpy_calls"],
+                        [x.value for x in v]))

@@ -1,0 +1,118 @@
+/*
+ * yk_desc.h -- the flattened, device-resident type descriptor and the launch
+ * interface between the C host library and the CUDA kernels.
+ *
+ * Plain C (no CUDA types), shared by the host code (yk_*.c) and the kernels
+ * (yk_kernels.cu).
+ *
+ * A committed type is flattened into a chain of levels, outermost first, ending in a
+ * leaf.  A packed byte position p (relative to the start of the packed form of
+ * `count` elements) is decomposed level by level, mixed-radix:
+ *
+ *   VEC  (count, stride, cps):  d = r / cps; r -= d * cps; off += d * stride
+ *   IDX  (count, disp[], cps):  d = r / cps; r -= d * cps; off += disp[d]
+ *   HIDX (count, disp[], pfx[], stride = child extent, cps = child packed size):
+ *                               j = max{ j : pfx[j] <= r }; r -= pfx[j];
+ *                               d = r / cps; r -= d * cps; off += disp[j] + d * stride
+ *   leaf RUN (run):             off += r                       (r < run)
+ *   leaf SEG (nseg, off[], pfx[], type[]):
+ *                               s = max{ s : pfx[s] <= r }; off += seg_off[s] + r - pfx[s]
+ *
+ * Level 0 is always the element level VEC(count, extent, size).  This replaces the
+ * reference's per-(kind, kind, type) generated kernels
+ * (src/backend/cuda/genpup.py:106-197) and its per-thread linear scan over hindexed
+ * blocks (genpup.py:150-163) with one table-driven decomposition.
+ *
+ * Divisions by cps use the Granlund-Montgomery round-up method for unsigned integer
+ * division by invariant integers ("Division by Invariant Integers using
+ * Multiplication", PLDI 1994, section 4): m = floor(2^N (2^l - d) / d) + 1 with
+ * l = ceil(log2 d); q = (t + ((n - t) >> min(l,1))) >> max(l-1,0), t = mulhi(m, n).
+ */
+#ifndef YK_DESC_H_INCLUDED
+#define YK_DESC_H_INCLUDED
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define YK_MAX_LEVELS 16
+
+enum { YK_LV_VEC = 0, YK_LV_IDX = 1, YK_LV_HIDX = 2 };
+enum { YK_LEAF_RUN = 0, YK_LEAF_SEG = 1 };
+
+/* Base element types the kernels compute in.  Operator support per type follows the
+ * reference's table (src/backend/gencomm.py:14-27); a combination outside the table
+ * leaves the destination untouched. */
+enum {
+    YK_BT_NONE = 0,     /* raw bytes */
+    YK_BT_BOOL,
+    YK_BT_CHAR,         /* REPLACE only */
+    YK_BT_WCHAR,        /* REPLACE only */
+    YK_BT_I8, YK_BT_I16, YK_BT_I32, YK_BT_I64,
+    YK_BT_F32, YK_BT_F64,
+    YK_BT_C32, YK_BT_C64,       /* float / double complex */
+    YK_BT_LDOUBLE, YK_BT_CLDOUBLE,      /* REPLACE only on the GPU */
+    YK_BT_LAST
+};
+
+typedef struct {
+    int32_t kind;
+    int32_t pad0;
+    uint64_t count;
+    int64_t stride;             /* VEC: byte stride; HIDX: child extent */
+    uint64_t cps;               /* packed bytes per digit (child packed size) */
+    uint64_t m64;               /* division magic (64-bit) */
+    uint32_t m32;               /* division magic (32-bit, valid if cps < 2^32) */
+    uint8_t l;                  /* ceil(log2 cps) */
+    uint8_t pad1[3];
+    const int64_t *disp;        /* device: IDX/HIDX displacements */
+    const uint64_t *pfx;        /* device: HIDX packed prefix, count + 1 entries */
+} yk_level;
+
+typedef struct {
+    int32_t nlev;
+    int32_t leaf;
+    uint64_t run;               /* RUN leaf length in bytes */
+    uint64_t nseg;              /* SEG leaf */
+    const int64_t *seg_off;     /* device */
+    const uint64_t *seg_pfx;    /* device, nseg + 1 entries */
+    const uint8_t *seg_type;    /* device, base type per segment (typed descriptors) */
+    int32_t leaf_type;          /* base type of a RUN leaf (typed descriptors) */
+    int32_t pad0;
+    int64_t base;               /* constant byte offset added to the typed pointer */
+    yk_level lv[YK_MAX_LEVELS];
+} yk_desc;
+
+/* One pack/unpack launch over the packed byte range [p0, p0 + nbytes). */
+typedef struct {
+    yk_desc desc;
+    char *typed;                /* device-accessible pointer to the typed (strided) buffer */
+    char *packed;               /* device-accessible pointer to packed byte p0 */
+    uint64_t p0;
+    uint64_t nbytes;
+    uint64_t op;                /* yaksa_op_t */
+    int32_t dir;                /* 0 = pack, 1 = unpack */
+    int32_t vec;                /* bytes per work unit (REPLACE) or unit granule (ops) */
+    int32_t typed_op;           /* 1 = elementwise operator on typed descriptor */
+    int32_t use64;              /* 1 = positions need 64-bit arithmetic */
+} yk_launch;
+
+/* Granlund-Montgomery constants for dividing by l->cps (host side). */
+void yk_level_set_magic(yk_level * l);
+
+/* Launch on `stream` (a cudaStream_t).  Returns 0 or a cudaError_t value. */
+int yk_cuda_launch_pup(const yk_launch * l, void *stream);
+
+/* Ordered unpack for types whose targets may overlap: sorted-block owner-computes
+ * kernel when the descriptor allows it, otherwise a single-warp ordered kernel. */
+int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blocks, void *stream);
+
+/* SM count of the current device (cached). */
+int yk_cuda_num_sms(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* YK_DESC_H_INCLUDED */

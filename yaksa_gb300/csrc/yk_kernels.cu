@@ -1,0 +1,586 @@
+/*
+ * yk_kernels.cu -- pack/unpack kernels for sm_103a.
+ *
+ * One kernel family replaces the reference's 3,720 generated kernels
+ * (src/backend/cuda/genpup.py:106-197).  Each thread moves V-byte units of the packed
+ * stream; the typed-side address of a unit comes from decomposing its packed position
+ * over the descriptor (yk_desc.h).  V is the largest power of two <= 16 that divides
+ * every run length, offset and pointer involved, so both the packed side (always
+ * contiguous, coalesced) and the typed side move in 16-byte vectors wherever the
+ * innermost contiguous run and alignment allow.
+ *
+ * Operators follow the reference's elementwise definitions exactly
+ * (src/backend/seq/genpup.py:302-327, identical on the GPU in
+ * src/backend/cuda/genpup.py:336-361): out = op(in, out), integer MAX/MIN as signed
+ * compare-selects, float MAX/MIN as the selects x_[in < out] / x_[in > out] (not
+ * fmax/fmin), integer SUM/PROD wrapping, LAND/LOR/LXOR producing 0/1.  Float
+ * arithmetic uses the _rn intrinsics so no multiply-add is ever contracted into an
+ * FMA (the reference compiles with -std=c11, which disables contraction), and complex
+ * multiplication recovers infinities with the algorithm of ISO C11 Annex G.5.1 (what
+ * libgcc's __mulsc3/__muldc3 implement for the reference's `*=` on _Complex values).
+ */
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "yk_desc.h"
+#include "yk_locate.h"
+
+#define YK_THREADS 256
+#define YK_UNROLL 4
+
+/* address decomposition shared with the host (yk_locate.h) */
+/* ------------------------------------------------------------------------- */
+
+__device__ __forceinline__ uint32_t yk_div(uint32_t n, const yk_level & l) { return yk_div32(n, &l); }
+__device__ __forceinline__ uint64_t yk_div(uint64_t n, const yk_level & l) { return yk_div64(n, &l); }
+
+template <typename IDX>
+__device__ __forceinline__ int64_t yk_locate(const yk_desc & d, IDX p, int *bt, uint64_t * inseg);
+template <>
+__device__ __forceinline__ int64_t yk_locate<uint32_t>(const yk_desc & d, uint32_t p, int *bt,
+                                                       uint64_t * inseg)
+{
+    return yk_locate32(&d, p, bt, inseg);
+}
+template <>
+__device__ __forceinline__ int64_t yk_locate<uint64_t>(const yk_desc & d, uint64_t p, int *bt,
+                                                       uint64_t * inseg)
+{
+    return yk_locate64(&d, p, bt, inseg);
+}
+
+/* ------------------------------------------------------------------------- */
+/* REPLACE: byte movement in V-byte units                                    */
+/* ------------------------------------------------------------------------- */
+
+template <int V> struct yk_vec;
+template <> struct yk_vec<1> { typedef uint8_t T; };
+template <> struct yk_vec<2> { typedef uint16_t T; };
+template <> struct yk_vec<4> { typedef uint32_t T; };
+template <> struct yk_vec<8> { typedef uint2 T; };
+template <> struct yk_vec<16> { typedef uint4 T; };
+
+template <typename IDX, int V, int DIR>
+__global__ void __launch_bounds__(YK_THREADS)
+yk_bytes_kernel(const __grid_constant__ yk_launch L)
+{
+    typedef typename yk_vec<V>::T VT;
+    const IDX nunits = (IDX) (L.nbytes / V);
+    const IDX p0 = (IDX) L.p0;
+    const IDX tile = (IDX) YK_THREADS * YK_UNROLL;
+    VT *packed = (VT *) L.packed;
+    char *typed = L.typed;
+    for (IDX t0 = (IDX) blockIdx.x * tile; t0 < nunits; t0 += (IDX) gridDim.x * tile) {
+        int64_t off[YK_UNROLL];
+        VT v[YK_UNROLL];
+#pragma unroll
+        for (int k = 0; k < YK_UNROLL; k++) {
+            IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
+            if (u < nunits)
+                off[k] = yk_locate<IDX>(L.desc, p0 + u * (IDX) V, nullptr, nullptr);
+        }
+        if (DIR == 0) {
+#pragma unroll
+            for (int k = 0; k < YK_UNROLL; k++) {
+                IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
+                if (u < nunits)
+                    v[k] = __ldg((const VT *) (typed + off[k]));
+            }
+#pragma unroll
+            for (int k = 0; k < YK_UNROLL; k++) {
+                IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
+                if (u < nunits)
+                    packed[u] = v[k];
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < YK_UNROLL; k++) {
+                IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
+                if (u < nunits)
+                    v[k] = __ldg(packed + u);
+            }
+#pragma unroll
+            for (int k = 0; k < YK_UNROLL; k++) {
+                IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
+                if (u < nunits)
+                    *(VT *) (typed + off[k]) = v[k];
+            }
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* elementwise operators                                                     */
+/* ------------------------------------------------------------------------- */
+
+enum { OP_MAX = 0, OP_MIN = 1, OP_SUM = 2, OP_PROD = 3, OP_LAND = 4, OP_BAND = 5, OP_LOR = 6,
+    OP_BOR = 7, OP_LXOR = 8, OP_BXOR = 9, OP_REPLACE = 10 };
+
+template <typename T> __device__ __forceinline__ T yk_ld(const char *p)
+{
+    if (((uintptr_t) p & (sizeof(T) - 1)) == 0)
+        return *(const T *) p;
+    T v;
+    char *q = (char *) &v;
+#pragma unroll
+    for (int i = 0; i < (int) sizeof(T); i++)
+        q[i] = p[i];
+    return v;
+}
+
+template <typename T> __device__ __forceinline__ void yk_st(char *p, T v)
+{
+    if (((uintptr_t) p & (sizeof(T) - 1)) == 0) {
+        *(T *) p = v;
+        return;
+    }
+    const char *q = (const char *) &v;
+#pragma unroll
+    for (int i = 0; i < (int) sizeof(T); i++)
+        p[i] = q[i];
+}
+
+/* integer operators; returns false when op is outside the type's table */
+template <typename S, typename U>
+__device__ __forceinline__ bool yk_int_op(int op, S in, S & out)
+{
+    switch (op) {
+        case OP_REPLACE:
+            out = in;
+            return true;
+        case OP_MAX:
+            out = (in < out) ? out : in;
+            return true;
+        case OP_MIN:
+            out = (in < out) ? in : out;
+            return true;
+        case OP_SUM:
+            out = (S) (U) ((U) out + (U) in);
+            return true;
+        case OP_PROD:
+            out = (S) (U) ((U) out * (U) in);
+            return true;
+        case OP_LAND:
+            out = (S) (out && in);
+            return true;
+        case OP_LOR:
+            out = (S) (out || in);
+            return true;
+        case OP_LXOR:
+            out = (S) (!out != !in);
+            return true;
+        case OP_BAND:
+            out = (S) (out & in);
+            return true;
+        case OP_BOR:
+            out = (S) (out | in);
+            return true;
+        case OP_BXOR:
+            out = (S) (out ^ in);
+            return true;
+    }
+    return false;
+}
+
+__device__ __forceinline__ float yk_add(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ double yk_add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ float yk_sub(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ double yk_sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float yk_mul(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ double yk_mul(double a, double b) { return __dmul_rn(a, b); }
+
+template <typename F>
+__device__ __forceinline__ bool yk_flt_op(int op, F in, F & out)
+{
+    switch (op) {
+        case OP_REPLACE:
+            out = in;
+            return true;
+        case OP_MAX:
+            out = (in < out) ? out : in;
+            return true;
+        case OP_MIN:
+            out = (in > out) ? out : in;
+            return true;
+        case OP_SUM:
+            out = yk_add(out, in);
+            return true;
+        case OP_PROD:
+            out = yk_mul(out, in);
+            return true;
+    }
+    return false;
+}
+
+/* (a + ib) * (c + id) with the infinity recovery of ISO C11 Annex G.5.1 */
+template <typename F>
+__device__ __forceinline__ void yk_cmul(F a, F b, F c, F d, F & x, F & y)
+{
+    F ac = yk_mul(a, c), bd = yk_mul(b, d), ad = yk_mul(a, d), bc = yk_mul(b, c);
+    x = yk_sub(ac, bd);
+    y = yk_add(ad, bc);
+    if (isnan(x) && isnan(y)) {
+        bool recalc = false;
+        const F one = (F) 1, zero = (F) 0;
+        if (isinf(a) || isinf(b)) {
+            a = copysign(isinf(a) ? one : zero, a);
+            b = copysign(isinf(b) ? one : zero, b);
+            if (isnan(c))
+                c = copysign(zero, c);
+            if (isnan(d))
+                d = copysign(zero, d);
+            recalc = true;
+        }
+        if (isinf(c) || isinf(d)) {
+            c = copysign(isinf(c) ? one : zero, c);
+            d = copysign(isinf(d) ? one : zero, d);
+            if (isnan(a))
+                a = copysign(zero, a);
+            if (isnan(b))
+                b = copysign(zero, b);
+            recalc = true;
+        }
+        if (!recalc && (isinf(ac) || isinf(bd) || isinf(ad) || isinf(bc))) {
+            if (isnan(a))
+                a = copysign(zero, a);
+            if (isnan(b))
+                b = copysign(zero, b);
+            if (isnan(c))
+                c = copysign(zero, c);
+            if (isnan(d))
+                d = copysign(zero, d);
+            recalc = true;
+        }
+        if (recalc) {
+            const F inf = (F) INFINITY;
+            x = yk_mul(inf, yk_sub(yk_mul(a, c), yk_mul(b, d)));
+            y = yk_mul(inf, yk_add(yk_mul(a, d), yk_mul(b, c)));
+        }
+    }
+}
+
+template <typename F>
+__device__ __forceinline__ bool yk_cplx_op(int op, const F in[2], F out[2])
+{
+    switch (op) {
+        case OP_REPLACE:
+            out[0] = in[0];
+            out[1] = in[1];
+            return true;
+        case OP_SUM:
+            out[0] = yk_add(out[0], in[0]);
+            out[1] = yk_add(out[1], in[1]);
+            return true;
+        case OP_PROD:{
+                F x, y;
+                yk_cmul(out[0], out[1], in[0], in[1], x, y);
+                out[0] = x;
+                out[1] = y;
+                return true;
+            }
+    }
+    return false;
+}
+
+/* apply op to one element of base type bt; `dst` is updated in place from `src` */
+__device__ __forceinline__ void yk_apply(int bt, int op, char *dst, const char *src)
+{
+    switch (bt) {
+        case YK_BT_BOOL:{
+                if (op != OP_REPLACE && op != OP_LAND && op != OP_LOR && op != OP_LXOR)
+                    return;
+                uint8_t i = yk_ld<uint8_t>(src), o = yk_ld<uint8_t>(dst);
+                uint8_t r = op == OP_REPLACE ? i : op == OP_LAND ? (uint8_t) (o && i) :
+                    op == OP_LOR ? (uint8_t) (o || i) : (uint8_t) (!o != !i);
+                yk_st<uint8_t>(dst, r);
+                return;
+            }
+        case YK_BT_I8:{
+                int8_t i = yk_ld<int8_t>(src), o = yk_ld<int8_t>(dst);
+                if (yk_int_op<int8_t, uint8_t>(op, i, o))
+                    yk_st<int8_t>(dst, o);
+                return;
+            }
+        case YK_BT_I16:{
+                int16_t i = yk_ld<int16_t>(src), o = yk_ld<int16_t>(dst);
+                if (yk_int_op<int16_t, uint16_t>(op, i, o))
+                    yk_st<int16_t>(dst, o);
+                return;
+            }
+        case YK_BT_I32:{
+                int32_t i = yk_ld<int32_t>(src), o = yk_ld<int32_t>(dst);
+                if (yk_int_op<int32_t, uint32_t>(op, i, o))
+                    yk_st<int32_t>(dst, o);
+                return;
+            }
+        case YK_BT_I64:{
+                int64_t i = yk_ld<int64_t>(src), o = yk_ld<int64_t>(dst);
+                if (yk_int_op<int64_t, uint64_t>(op, i, o))
+                    yk_st<int64_t>(dst, o);
+                return;
+            }
+        case YK_BT_F32:{
+                float i = yk_ld<float>(src), o = yk_ld<float>(dst);
+                if (yk_flt_op<float>(op, i, o))
+                    yk_st<float>(dst, o);
+                return;
+            }
+        case YK_BT_F64:{
+                double i = yk_ld<double>(src), o = yk_ld<double>(dst);
+                if (yk_flt_op<double>(op, i, o))
+                    yk_st<double>(dst, o);
+                return;
+            }
+        case YK_BT_C32:{
+                float i[2] = { yk_ld<float>(src), yk_ld<float>(src + 4) };
+                float o[2] = { yk_ld<float>(dst), yk_ld<float>(dst + 4) };
+                if (yk_cplx_op<float>(op, i, o)) {
+                    yk_st<float>(dst, o[0]);
+                    yk_st<float>(dst + 4, o[1]);
+                }
+                return;
+            }
+        case YK_BT_C64:{
+                double i[2] = { yk_ld<double>(src), yk_ld<double>(src + 8) };
+                double o[2] = { yk_ld<double>(dst), yk_ld<double>(dst + 8) };
+                if (yk_cplx_op<double>(op, i, o)) {
+                    yk_st<double>(dst, o[0]);
+                    yk_st<double>(dst + 8, o[1]);
+                }
+                return;
+            }
+        default:
+            /* CHAR/WCHAR only have REPLACE, which never reaches the typed kernel;
+             * long double arithmetic is refused on the host */
+            return;
+    }
+}
+
+__device__ __forceinline__ int yk_bt_size(int bt)
+{
+    switch (bt) {
+        case YK_BT_BOOL: case YK_BT_CHAR: case YK_BT_I8: return 1;
+        case YK_BT_I16: return 2;
+        case YK_BT_WCHAR: case YK_BT_I32: case YK_BT_F32: return 4;
+        case YK_BT_I64: case YK_BT_F64: case YK_BT_C32: return 8;
+        case YK_BT_C64: return 16;
+        default: return 1;
+    }
+}
+
+/* Operators: one work unit = `vec` bytes (the gcd of the element sizes); the unit
+ * that starts an element applies op to that whole element. */
+template <typename IDX, int DIR>
+__global__ void __launch_bounds__(YK_THREADS)
+yk_typed_kernel(const __grid_constant__ yk_launch L)
+{
+    const IDX g = (IDX) L.vec;
+    const IDX nunits = (IDX) (L.nbytes / L.vec);
+    const int op = (int) L.op;
+    for (IDX u = (IDX) blockIdx.x * YK_THREADS + threadIdx.x; u < nunits;
+         u += (IDX) gridDim.x * YK_THREADS) {
+        int bt;
+        uint64_t inseg;
+        int64_t off = yk_locate<IDX>(L.desc, (IDX) L.p0 + u * g, &bt, &inseg);
+        int es = yk_bt_size(bt);
+        if (inseg % (uint64_t) es)
+            continue;
+        char *t = L.typed + off;
+        char *p = L.packed + (uint64_t) u * (uint64_t) g;
+        if (DIR == 0)
+            yk_apply(bt, op, p, t);
+        else
+            yk_apply(bt, op, t, p);
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* ordered unpack for overlapping targets                                    */
+/* ------------------------------------------------------------------------- */
+
+/* Sorted blocks: descriptor = IDX(nblk, disp sorted ascending, cps = R) over a run of
+ * R bytes of one base type.  Every target element that receives data gets exactly one
+ * owner: the thread of its first in-range contributor, which applies the
+ * contributions of all later blocks in block order (the reference's seq order,
+ * src/backend/seq/genpup.py:119-211). */
+template <typename IDX>
+__global__ void __launch_bounds__(YK_THREADS)
+yk_owner_kernel(const __grid_constant__ yk_launch L)
+{
+    const yk_level & lv = L.desc.lv[0];
+    const int bt = L.desc.leaf_type;
+    const IDX es = (IDX) yk_bt_size(bt);
+    const IDX R = (IDX) lv.cps;
+    const IDX p0 = (IDX) L.p0, p1 = (IDX) (L.p0 + L.nbytes);
+    const IDX nunits = (IDX) (L.nbytes / es);
+    const int op = (int) L.op;
+    for (IDX u = (IDX) blockIdx.x * YK_THREADS + threadIdx.x; u < nunits;
+         u += (IDX) gridDim.x * YK_THREADS) {
+        IDX p = p0 + u * es;
+        IDX b = yk_div(p, lv);
+        IDX j = p - b * R;
+        int64_t x = __ldg(lv.disp + b) + (int64_t) j;
+        if (b > 0) {
+            int64_t dprev = __ldg(lv.disp + b - 1);
+            if (x < dprev + (int64_t) R && (b - 1) * R + (IDX) (x - dprev) >= p0)
+                continue;       /* an earlier in-range block owns this element */
+        }
+        char *t = L.typed + L.desc.base + x;
+        for (IDX bb = b; bb < (IDX) lv.count; bb++) {
+            int64_t db = __ldg(lv.disp + bb);
+            if (db > x)
+                break;
+            IDX pp = bb * R + (IDX) (x - db);
+            if (pp >= p1)
+                break;
+            yk_apply(bt, op, t, L.packed + (pp - p0));
+        }
+    }
+}
+
+/* General ordered fallback: one warp walks the packed range in order, 32 units at a
+ * time; a chunk whose target ranges intersect runs lane by lane. */
+template <typename IDX>
+__global__ void yk_ordered_warp_kernel(const __grid_constant__ yk_launch L)
+{
+    const int lane = threadIdx.x;
+    const IDX g = (IDX) L.vec;
+    const IDX nunits = (IDX) (L.nbytes / L.vec);
+    for (IDX c0 = 0; c0 < nunits; c0 += 32) {
+        IDX u = c0 + (IDX) lane;
+        bool active = u < nunits;
+        int bt = YK_BT_NONE;
+        uint64_t inseg = 0;
+        int64_t off = 0;
+        int len = 0;
+        if (active) {
+            off = yk_locate<IDX>(L.desc, (IDX) L.p0 + u * g, &bt, &inseg);
+            if (L.typed_op) {
+                int es = yk_bt_size(bt);
+                if (inseg % (uint64_t) es)
+                    active = false;
+                else
+                    len = es;
+            } else {
+                len = (int) g;
+            }
+        }
+        bool conflict = false;
+        for (int k = 0; k < 31; k++) {
+            int64_t ooff = __shfl_sync(0xffffffffu, off, k);
+            int olen = __shfl_sync(0xffffffffu, active ? len : 0, k);
+            if (k < lane && active && olen && off < ooff + olen && ooff < off + len)
+                conflict = true;
+        }
+        bool serial = __any_sync(0xffffffffu, conflict);
+        for (int k = 0; k < 32; k++) {
+            if ((!serial || k == lane) && active) {
+                char *t = L.typed + off;
+                char *p = L.packed + (uint64_t) u * (uint64_t) g;
+                if (L.typed_op) {
+                    yk_apply(bt, (int) L.op, t, p);
+                } else {
+                    for (int i = 0; i < len; i++)
+                        t[i] = p[i];
+                }
+            }
+            __syncwarp();
+            if (!serial)
+                break;
+        }
+    }
+}
+
+/* ------------------------------------------------------------------------- */
+/* host-side launchers                                                       */
+/* ------------------------------------------------------------------------- */
+
+static int yk_sms = 0;
+
+extern "C" int yk_cuda_num_sms(void)
+{
+    if (!yk_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&yk_sms, cudaDevAttrMultiProcessorCount, dev);
+        if (yk_sms <= 0)
+            yk_sms = 1;
+    }
+    return yk_sms;
+}
+
+static unsigned yk_grid(uint64_t units, uint64_t per_block, int blocks_per_sm)
+{
+    uint64_t need = (units + per_block - 1) / per_block;
+    uint64_t cap = (uint64_t) yk_cuda_num_sms() * (uint64_t) blocks_per_sm;
+    if (need > cap)
+        need = cap;
+    return (unsigned) (need ? need : 1);
+}
+
+template <typename IDX>
+static void launch_bytes(const yk_launch * l, cudaStream_t s)
+{
+    uint64_t units = l->nbytes / (uint64_t) l->vec;
+    unsigned g = yk_grid(units, YK_THREADS * YK_UNROLL, 8);
+#define YK_B(V) do { if (l->dir == 0) yk_bytes_kernel<IDX, V, 0><<<g, YK_THREADS, 0, s>>>(*l); \
+                     else yk_bytes_kernel<IDX, V, 1><<<g, YK_THREADS, 0, s>>>(*l); } while (0)
+    switch (l->vec) {
+        case 16: YK_B(16); break;
+        case 8: YK_B(8); break;
+        case 4: YK_B(4); break;
+        case 2: YK_B(2); break;
+        default: YK_B(1); break;
+    }
+#undef YK_B
+}
+
+extern "C" int yk_cuda_launch_pup(const yk_launch * l, void *stream)
+{
+    cudaStream_t s = (cudaStream_t) stream;
+    if (l->nbytes == 0)
+        return 0;
+    if (!l->typed_op) {
+        if (l->use64)
+            launch_bytes<uint64_t>(l, s);
+        else
+            launch_bytes<uint32_t>(l, s);
+    } else {
+        const yk_launch & c = *l;
+        uint64_t units = c.nbytes / (uint64_t) c.vec;
+        unsigned g = yk_grid(units, YK_THREADS, 16);
+        if (c.use64) {
+            if (c.dir == 0)
+                yk_typed_kernel<uint64_t, 0><<<g, YK_THREADS, 0, s>>>(c);
+            else
+                yk_typed_kernel<uint64_t, 1><<<g, YK_THREADS, 0, s>>>(c);
+        } else {
+            if (c.dir == 0)
+                yk_typed_kernel<uint32_t, 0><<<g, YK_THREADS, 0, s>>>(c);
+            else
+                yk_typed_kernel<uint32_t, 1><<<g, YK_THREADS, 0, s>>>(c);
+        }
+    }
+    return (int) cudaGetLastError();
+}
+
+extern "C" int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blocks, void *stream)
+{
+    cudaStream_t s = (cudaStream_t) stream;
+    if (l->nbytes == 0)
+        return 0;
+    const yk_launch & c = *l;
+    if (sorted_blocks) {
+        uint64_t units = c.nbytes / (uint64_t) c.vec;
+        unsigned g = yk_grid(units, YK_THREADS, 16);
+        if (c.use64)
+            yk_owner_kernel<uint64_t><<<g, YK_THREADS, 0, s>>>(c);
+        else
+            yk_owner_kernel<uint32_t><<<g, YK_THREADS, 0, s>>>(c);
+    } else {
+        if (c.use64)
+            yk_ordered_warp_kernel<uint64_t><<<1, 32, 0, s>>>(c);
+        else
+            yk_ordered_warp_kernel<uint32_t><<<1, 32, 0, s>>>(c);
+    }
+    return (int) cudaGetLastError();
+}
