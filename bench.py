@@ -27,12 +27,17 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-N = 512
-FACES = [  # (name, subsizes, starts) in C order over sizes {N, N, N}
-    ("x-", [N, N, 2], [0, 0, 0]), ("x+", [N, N, 2], [0, 0, N - 2]),
-    ("y-", [N, 2, N], [0, 0, 0]), ("y+", [N, 2, N], [0, N - 2, 0]),
-    ("z-", [2, N, N], [0, 0, 0]), ("z+", [2, N, N], [N - 2, 0, 0]),
-]
+N = int(os.environ.get("YK_BENCH_N", "512"))   # grid edge; smaller only for ncu captures
+
+
+def face_specs(n):
+    """(name, subsizes, starts) of the six depth-2 faces, C order over sizes {n, n, n}."""
+    return [("x-", [n, n, 2], [0, 0, 0]), ("x+", [n, n, 2], [0, 0, n - 2]),
+            ("y-", [n, 2, n], [0, 0, 0]), ("y+", [n, 2, n], [0, n - 2, 0]),
+            ("z-", [2, n, n], [0, 0, 0]), ("z+", [2, n, n], [n - 2, 0, 0])]
+
+
+FACES = face_specs(N)
 L2_FLUSH_BYTES = 512 << 20
 
 
@@ -211,32 +216,62 @@ def main():
     sh = ctypes.c_void_p(stream.cuda_stream)
     shp = ctypes.addressof(sh)
 
-    def step():
+    # the step through the batched C-ABI: one launch packs all six faces, one unpacks them
+    pack_batch = y.batch_array([yk.pack_op(src.data_ptr(), 1, t, 0, pk.data_ptr(), P)
+                                for (name, t), pk in zip(faces, packed)])
+    unpack_batch = y.batch_array([yk.unpack_op(pk.data_ptr(), P, dst.data_ptr(), 1, t, 0)
+                                  for (name, t), pk in zip(faces, packed)])
+
+    # the exchange repeats with the same buffers every step: capture it once
+    graph, _ = y.graph_create([[yk.pack_op(src.data_ptr(), 1, t, 0, pk.data_ptr(), P)
+                                for (name, t), pk in zip(faces, packed)],
+                               [yk.unpack_op(pk.data_ptr(), P, dst.data_ptr(), 1, t, 0)
+                                for (name, t), pk in zip(faces, packed)]])
+
+    def step_batched():
+        y.graph_launch(graph, shp)
+
+    def step_batched_uncaptured():
+        y.pup_batch_stream(pack_batch, shp)
+        y.pup_batch_stream(unpack_batch, shp)
+
+    # the same step through the reference's API: one stream-ordered call per face
+    def step_plain():
         for (name, t), pk in zip(faces, packed):
             y.pack_stream(src.data_ptr(), 1, t, 0, pk.data_ptr(), P, shp)
         for (name, t), pk in zip(faces, packed):
             y.unpack_stream(pk.data_ptr(), P, dst.data_ptr(), 1, t, 0, shp)
 
+    def timed(fn, steps):
+        tot = 0.0
+        for _ in range(steps):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            fn()
+            e1.record()
+            e1.synchronize()
+            tot += e0.elapsed_time(e1) * 1e-3
+        return tot
+
     for _ in range(args.warmup):
         flush.zero_()
-        step()
+        step_batched()
+        flush.zero_()
+        step_plain()
     torch.cuda.synchronize()
 
-    # per-launch durations by face and direction (separate, untimed pass)
-    per = {}
-    for rep in range(3):
-        for d in (0, 1):
-            for (name, t), pk in zip(faces, packed):
-                flush.zero_()
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record()
-                if d == 0:
-                    y.pack_stream(src.data_ptr(), 1, t, 0, pk.data_ptr(), P, shp)
-                else:
-                    y.unpack_stream(pk.data_ptr(), P, dst.data_ptr(), 1, t, 0, shp)
-                e1.record()
-                e1.synchronize()
-                per.setdefault((name, d), []).append(e0.elapsed_time(e1) * 1e-3)
+    # per-launch durations of the dominant kernel (one batched launch per direction)
+    per = {"pack": [], "unpack": []}
+    for rep in range(5):
+        for d, arr in (("pack", pack_batch), ("unpack", unpack_batch)):
+            flush.zero_()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            y.pup_batch_stream(arr, shp)
+            e1.record()
+            e1.synchronize()
+            per[d].append(e0.elapsed_time(e1) * 1e-3)
 
     clocks = Clocks(os.path.join(ROOT, "gpurun_out", "clocks.csv")
                     if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/yk_clocks.csv")
@@ -247,15 +282,7 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     wall0 = time.perf_counter()
-    tot = 0.0
-    for _ in range(args.steps):
-        flush.zero_()
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        step()
-        e1.record()
-        e1.synchronize()
-        tot += e0.elapsed_time(e1) * 1e-3
+    tot = timed(step_batched, args.steps)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
@@ -266,63 +293,78 @@ def main():
         tt = torch.tensor([tot], device="cuda", dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         tot = tt.item()
+    tot_plain = timed(step_plain, args.steps)
+    tot_uncap = timed(step_batched_uncaptured, args.steps)
 
     # correctness of the timed work: every face of dst equals the face of src
-    s3, d3 = src.view(N, N, N), dst.view(N, N, N)
-    ok = (torch.equal(s3[:, :, :2], d3[:, :, :2]) and torch.equal(s3[:, :, -2:], d3[:, :, -2:]) and
-          torch.equal(s3[:, :2, :], d3[:, :2, :]) and torch.equal(s3[:, -2:, :], d3[:, -2:, :]) and
-          torch.equal(s3[:2], d3[:2]) and torch.equal(s3[-2:], d3[-2:]))
+    def faces_equal(a, b):
+        s3, d3 = a.view(N, N, N), b.view(N, N, N)
+        return (torch.equal(s3[:, :, :2], d3[:, :, :2]) and torch.equal(s3[:, :, -2:], d3[:, :, -2:])
+                and torch.equal(s3[:, :2, :], d3[:, :2, :]) and torch.equal(s3[:, -2:, :], d3[:, -2:, :])
+                and torch.equal(s3[:2], d3[:2]) and torch.equal(s3[-2:], d3[-2:]))
+    ok = faces_equal(src, dst)
 
     step_bytes = 2 * P * len(faces)       # packed bytes moved per step (pack + unpack)
     ms = tot / args.steps * 1e3
     value = step_bytes * world / (tot / args.steps) / 1e9
+    plain_value = step_bytes * world / (tot_plain / args.steps) / 1e9
     hbm, peak_kind = peaks()
-    # dominant kernel: the byte-moving pack/unpack kernel (all 12 launches of a step)
-    alg = 2 * P                            # algorithmic HBM bytes per launch
-    avg = {f"{n}{'pack' if d == 0 else 'unpack'}": statistics.median(v) for (n, d), v in per.items()}
-    all_launch = [statistics.median(v) for v in per.values()]
-    mean_launch = sum(all_launch) / len(all_launch)
+    # dominant kernel: yk_batch_kernel; algorithmic bytes = 2 per packed byte per launch
+    alg = 2 * P * len(faces)
+    med = {d: statistics.median(v) for d, v in per.items()}
+    mean_launch = (med["pack"] + med["unpack"]) / 2
     achieved = alg / mean_launch / 1e9
-    slow = max(avg, key=avg.get)
 
-    # e2e through the C-ABI with host (pinned) buffers: the kernels read and write host
-    # memory over NVLink-C2C inside the timed region
+    # e2e through the reference's C-ABI (yaksa_ipack / yaksa_iunpack + wait) with host
+    # pinned buffers: the kernels read and write host memory over NVLink-C2C inside the
+    # timed region
     hsrc = src.cpu().pin_memory()
     hdst = torch.zeros_like(hsrc).pin_memory()
     hpk = [torch.empty(P, dtype=torch.uint8).pin_memory() for _ in faces]
+
+    def e2e_step():
+        reqs = [y.ipack(hsrc.data_ptr(), 1, t, 0, pk.data_ptr(), P)[1] for (name, t), pk in zip(faces, hpk)]
+        for r in reqs:
+            y.wait(r)
+        reqs = [y.iunpack(pk.data_ptr(), P, hdst.data_ptr(), 1, t, 0)[1] for (name, t), pk in zip(faces, hpk)]
+        for r in reqs:
+            y.wait(r)
     for _ in range(2):
-        for (name, t), pk in zip(faces, hpk):
-            y.pack(hsrc.data_ptr(), 1, t, 0, pk.data_ptr(), P)
-        for (name, t), pk in zip(faces, hpk):
-            y.unpack(pk.data_ptr(), P, hdst.data_ptr(), 1, t, 0)
+        e2e_step()
     e_steps = max(3, args.steps // 2)
     t0 = time.perf_counter()
     for _ in range(e_steps):
-        for (name, t), pk in zip(faces, hpk):
-            y.pack(hsrc.data_ptr(), 1, t, 0, pk.data_ptr(), P)
-        for (name, t), pk in zip(faces, hpk):
-            y.unpack(pk.data_ptr(), P, hdst.data_ptr(), 1, t, 0)
+        e2e_step()
     e2e_t = (time.perf_counter() - t0) / e_steps
-    hs3, hd3 = hsrc.view(N, N, N), hdst.view(N, N, N)
-    ok = ok and torch.equal(hs3[:, :, :2], hd3[:, :, :2]) and torch.equal(hs3[:2], hd3[:2])
+    ok = ok and faces_equal(hsrc, hdst)
     e2e = {"value": step_bytes * world / e2e_t / 1e9, "unit": "GB/s",
            "h2d_bytes_per_step": P * len(faces) * 2, "d2h_bytes_per_step": P * len(faces) * 2,
-           "mode": "host pinned buffers, kernels access them in place over NVLink-C2C"}
+           "mode": "yaksa_ipack/yaksa_iunpack + wait per face on host pinned buffers; the kernels "
+                   "access host memory in place over NVLink-C2C"}
 
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform [-1,1))",
             "config": {"workload": "halo3d: 512^3 float32 grid, 6 depth-2 subarray faces "
-                                   "(2 MiB packed each), pack + unpack REPLACE per step",
+                                   "(2 MiB packed each), pack + unpack REPLACE per step, batched "
+                                   "C-ABI (one launch per direction) captured once as a CUDA "
+                                   "graph and replayed per step",
                        "parallelism": f"replicas x{world}",
                        "l2": "flushed between steps (512 MiB write outside the event-timed span)"},
             "bit_exact": bool(ok),
+            "plain_path": {"value": plain_value, "unit": "GB/s",
+                           "ms_per_step": tot_plain / args.steps * 1e3,
+                           "note": "one yaksa_pack_stream/yaksa_unpack_stream launch per face"},
+            "batched_uncaptured": {"value": step_bytes * world / (tot_uncap / args.steps) / 1e9,
+                                   "unit": "GB/s", "ms_per_step": tot_uncap / args.steps * 1e3,
+                                   "note": "yaksa_gb300_pup_batch_stream per direction, host "
+                                           "planning inside the timed span"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": None,
-                         "kernel": "yk_bytes_kernel (per-face pack/unpack, mean over 12 launches)",
+                         "kernel": "yk_batch_kernel (6 faces per launch; mean of pack and unpack)",
                          "peak_source": peak_kind,
-                         "per_launch_us": {k: v * 1e6 for k, v in sorted(avg.items())},
-                         "slowest": slow},
+                         "launch_us": {d: v * 1e6 for d, v in med.items()},
+                         "algorithmic_bytes_per_launch": alg},
             "gpu_launches": launches,
             "clocks": clk,
             "e2e": e2e,

@@ -14,6 +14,48 @@
 extern "C" {
 #endif
 
+/* One pack (kind 0) or unpack (kind 1) request, with the arguments of yaksa_pack /
+ * yaksa_unpack: pack reads the typed buffer inbuf (count, type) and writes packed bytes
+ * [offset, offset + actual) to outbuf; unpack reads maxbytes packed bytes from inbuf
+ * into the typed buffer outbuf.  `actual` receives the bytes moved. */
+typedef struct {
+    int32_t kind;
+    int32_t pad;
+    const void *inbuf;
+    void *outbuf;
+    uintptr_t count;
+    yaksa_type_t type;
+    uintptr_t offset;
+    uintptr_t maxbytes;
+    yaksa_op_t op;
+    uintptr_t actual;
+} yaksa_gb300_pup_t;
+
+/* Batched requests (no counterpart in the reference, whose callers issue one
+ * yaksa_ipack/yaksa_iunpack per buffer).  The n requests must be independent (no
+ * request writes bytes another reads or writes); they may run concurrently.  All
+ * device-addressable REPLACE requests share a single kernel launch.
+ *   _stream: enqueued on *(cudaStream_t *) stream (NULL: the library stream);
+ *   blocking form: returns when every request completed;
+ *   i-form: returns a request for yaksa_request_test / yaksa_request_wait. */
+int yaksa_gb300_pup_batch_stream(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info, void *stream);
+int yaksa_gb300_pup_batch(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info);
+int yaksa_gb300_ipup_batch(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info,
+                           yaksa_request_t * request);
+
+/* Captured sequences (no counterpart in the reference).  A halo exchange repeats the
+ * same packs and unpacks on the same buffers every step; capturing them once into a
+ * CUDA graph removes all per-step host work.  ops[0 .. batch_ends[0]) is the first
+ * batch, ops[batch_ends[0] .. batch_ends[1]) the second, and so on; batches run in
+ * order, the requests of one batch concurrently.  Buffers and types are bound at
+ * creation (types stay referenced until yaksa_gb300_graph_free).  Requests whose
+ * buffers the GPU cannot address are refused with YAKSA_ERR__NOT_SUPPORTED. */
+typedef struct yaksa_gb300_graph_s *yaksa_gb300_graph_t;
+int yaksa_gb300_graph_create(yaksa_gb300_pup_t * ops, const int *batch_ends, int nbatches,
+                             yaksa_info_t info, yaksa_gb300_graph_t * graph);
+int yaksa_gb300_graph_launch(yaksa_gb300_graph_t graph, void *stream);
+int yaksa_gb300_graph_free(yaksa_gb300_graph_t graph);
+
 /* Runtime counters since load: kernel launches, calls served in place (device or
  * GPU-addressable host memory), calls that staged host data through device memory,
  * and contiguous calls served by one copy. */

@@ -95,6 +95,21 @@ _PROTOS = {
 }
 
 
+class PupOp(ctypes.Structure):
+    """yaksa_gb300_pup_t (include/yaksa_gb300.h): one request of a batch."""
+    _fields_ = [("kind", ctypes.c_int32), ("pad", ctypes.c_int32), ("inbuf", _vp), ("outbuf", _vp),
+                ("count", _up), ("type", _u64), ("offset", _up), ("maxbytes", _up), ("op", _u64),
+                ("actual", _up)]
+
+
+def pack_op(inbuf, count, t, offset, outbuf, maxbytes, op=10):
+    return PupOp(0, 0, inbuf, outbuf, count, t, offset, maxbytes, op, 0)
+
+
+def unpack_op(inbuf, insize, outbuf, count, t, offset, op=10):
+    return PupOp(1, 0, inbuf, outbuf, count, t, offset, insize, op, 0)
+
+
 class YaksaError(RuntimeError):
     def __init__(self, fn, rc):
         super().__init__(f"{fn} returned {rc}")
@@ -114,6 +129,18 @@ def load_library(path):
     if hasattr(lib, "yaksa_gb300_stats"):
         lib.yaksa_gb300_stats.restype = ctypes.c_int
         lib.yaksa_gb300_stats.argtypes = [ctypes.POINTER(_u64)] * 4
+        for name, extra in (("yaksa_gb300_pup_batch_stream", [_vp]), ("yaksa_gb300_pup_batch", []),
+                            ("yaksa_gb300_ipup_batch", [ctypes.POINTER(_u64)])):
+            f = getattr(lib, name)
+            f.restype = ctypes.c_int
+            f.argtypes = [ctypes.POINTER(PupOp), ctypes.c_int, _vp] + extra
+        lib.yaksa_gb300_graph_create.restype = ctypes.c_int
+        lib.yaksa_gb300_graph_create.argtypes = [ctypes.POINTER(PupOp), ctypes.POINTER(ctypes.c_int),
+                                                 ctypes.c_int, _vp, ctypes.POINTER(_vp)]
+        lib.yaksa_gb300_graph_launch.restype = ctypes.c_int
+        lib.yaksa_gb300_graph_launch.argtypes = [_vp, _vp]
+        lib.yaksa_gb300_graph_free.restype = ctypes.c_int
+        lib.yaksa_gb300_graph_free.argtypes = [_vp]
     return lib
 
 
@@ -291,6 +318,46 @@ class Yaksa:
         c = ctypes.c_int()
         self._chk("yaksa_request_test", self.lib.yaksa_request_test(req, ctypes.byref(c)))
         return bool(c.value)
+
+    # batches (include/yaksa_gb300.h)
+    @staticmethod
+    def batch_array(ops):
+        arr = (PupOp * len(ops))(*ops)
+        return arr
+
+    def pup_batch(self, arr, info=None):
+        self._chk("yaksa_gb300_pup_batch", self.lib.yaksa_gb300_pup_batch(arr, len(arr), info))
+        return [o.actual for o in arr]
+
+    def pup_batch_stream(self, arr, stream_ptr, info=None):
+        self._chk("yaksa_gb300_pup_batch_stream",
+                  self.lib.yaksa_gb300_pup_batch_stream(arr, len(arr), info, stream_ptr))
+
+    def ipup_batch(self, arr, info=None):
+        req = _u64()
+        self._chk("yaksa_gb300_ipup_batch",
+                  self.lib.yaksa_gb300_ipup_batch(arr, len(arr), info, ctypes.byref(req)))
+        return req.value
+
+    def graph_create(self, batches, info=None):
+        """batches: list of lists of PupOp; returns (graph handle, flat PupOp array)."""
+        flat = [o for b in batches for o in b]
+        arr = (PupOp * len(flat))(*flat)
+        ends, acc = [], 0
+        for b in batches:
+            acc += len(b)
+            ends.append(acc)
+        e = (ctypes.c_int * len(ends))(*ends)
+        g = _vp()
+        self._chk("yaksa_gb300_graph_create",
+                  self.lib.yaksa_gb300_graph_create(arr, e, len(ends), info, ctypes.byref(g)))
+        return g, arr
+
+    def graph_launch(self, g, stream_ptr=None):
+        self._chk("yaksa_gb300_graph_launch", self.lib.yaksa_gb300_graph_launch(g, stream_ptr))
+
+    def graph_free(self, g):
+        self._chk("yaksa_gb300_graph_free", self.lib.yaksa_gb300_graph_free(g))
 
     def stats(self):
         v = [_u64() for _ in range(4)]

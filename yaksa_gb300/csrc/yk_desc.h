@@ -97,7 +97,27 @@ typedef struct {
     int32_t vec;                /* bytes per work unit (REPLACE) or unit granule (ops) */
     int32_t typed_op;           /* 1 = elementwise operator on typed descriptor */
     int32_t use64;              /* 1 = positions need 64-bit arithmetic */
+    int32_t regular;            /* 0..YK_REGULAR_MAX: that many VEC levels over a RUN leaf
+                                 * with 32-bit positions; -1: any other shape */
+    int32_t pad1;
 } yk_launch;
+
+#define YK_REGULAR_MAX 3
+
+/* Up to YK_BATCH_MAX REPLACE requests with 32-bit positions in one launch; passed by
+ * value as the kernel parameter (about 19 KB, under the 32 KB parameter limit). */
+#define YK_BATCH_MAX 16
+typedef struct {
+    int32_t n;
+    int32_t pad;
+    uint64_t tile_start[YK_BATCH_MAX + 1];      /* first tile of each request */
+    yk_launch req[YK_BATCH_MAX];
+} yk_batch;
+
+/* Tiles of one batch request (units per tile depend on the batch's total size). */
+int yk_cuda_batch_units_per_thread(uint64_t total_units);
+uint64_t yk_cuda_tiles(uint64_t units, int units_per_thread);
+int yk_cuda_launch_batch(const yk_batch * b, int units_per_thread, int regular, void *stream);
 
 /* Granlund-Montgomery constants for dividing by l->cps (host side). */
 void yk_level_set_magic(yk_level * l);

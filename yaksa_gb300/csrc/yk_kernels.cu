@@ -59,52 +59,255 @@ template <> struct yk_vec<4> { typedef uint32_t T; };
 template <> struct yk_vec<8> { typedef uint2 T; };
 template <> struct yk_vec<16> { typedef uint4 T; };
 
-template <typename IDX, int V, int DIR>
+/* Loads cached in L2 only and with no L2 prefetch-size qualifier, so an isolated
+ * 8-byte run costs one 32-byte sector request instead of a 128-byte line. */
+__device__ __forceinline__ uint8_t yk_ldcg(const uint8_t * p)
+{
+    uint16_t v;
+    asm volatile ("ld.global.cg.u8 %0, [%1];" : "=h"(v) : "l"(p));
+    return (uint8_t) v;
+}
+
+__device__ __forceinline__ uint16_t yk_ldcg(const uint16_t * p)
+{
+    uint16_t v;
+    asm volatile ("ld.global.cg.u16 %0, [%1];" : "=h"(v) : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ uint32_t yk_ldcg(const uint32_t * p)
+{
+    uint32_t v;
+    asm volatile ("ld.global.cg.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ uint2 yk_ldcg(const uint2 * p)
+{
+    uint2 v;
+    asm volatile ("ld.global.cg.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
+    return v;
+}
+
+__device__ __forceinline__ uint4 yk_ldcg(const uint4 * p)
+{
+    uint4 v;
+    asm volatile ("ld.global.cg.v4.u32 {%0, %1, %2, %3}, [%4];"
+                  : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
+    return v;
+}
+
+/* One tile: units t0 + k * YK_THREADS + threadIdx.x, k < U, of a request with
+ * `nunits` V-byte units.  All U addresses are computed first and all U loads issued
+ * before any store, so every thread keeps U independent memory requests in flight.
+ * Loads use ld.global.cg (cache in L2 only): an L1-allocating load of an isolated
+ * 8-byte run fills a 128-byte line, which is 16x the useful DRAM traffic for runs
+ * at a large stride. */
+template <typename IDX, int V, int DIR, int U>
+__device__ __forceinline__ void yk_bytes_tile(const yk_launch & L, IDX t0, IDX nunits)
+{
+    typedef typename yk_vec<V>::T VT;
+    const IDX p0 = (IDX) L.p0;
+    VT *packed = (VT *) L.packed;
+    char *typed = L.typed;
+    int64_t off[U];
+    VT v[U];
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+        IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
+        if (u < nunits)
+            off[k] = yk_locate<IDX>(L.desc, p0 + u * (IDX) V, nullptr, nullptr);
+    }
+    if (DIR == 0) {
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
+            if (u < nunits)
+                v[k] = yk_ldcg((const VT *) (typed + off[k]));
+        }
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
+            if (u < nunits)
+                packed[u] = v[k];
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
+            if (u < nunits)
+                v[k] = yk_ldcg((const VT *) (packed + u));
+        }
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
+            if (u < nunits)
+                *(VT *) (typed + off[k]) = v[k];
+        }
+    }
+}
+
+/* Regular nests (NL strided levels over one contiguous run, 32-bit positions): the
+ * decomposition unrolls at compile time into NL multiply-high/shift/multiply-add steps
+ * with no table loads, which keeps the kernel near 32 registers and lets eight
+ * 256-thread CTAs share an SM (full occupancy, the most loads in flight). */
+/* the few fields of a regular request a tile needs, held in registers */
+struct yk_rt {
+    char *typed;                /* typed pointer + descriptor base */
+    char *packed;
+    uint32_t p0;
+    uint32_t m[YK_REGULAR_MAX];
+    uint32_t cps[YK_REGULAR_MAX];
+    uint32_t sh1[YK_REGULAR_MAX], sh2[YK_REGULAR_MAX];
+    int64_t stride[YK_REGULAR_MAX];
+};
+
+template <int NL>
+__device__ __forceinline__ void yk_rt_load(yk_rt & t, const yk_launch & L)
+{
+    t.typed = L.typed + L.desc.base;
+    t.packed = L.packed;
+    t.p0 = (uint32_t) L.p0;
+#pragma unroll
+    for (int i = 0; i < NL; i++) {
+        t.m[i] = L.desc.lv[i].m32;
+        t.cps[i] = (uint32_t) L.desc.lv[i].cps;
+        t.sh1[i] = L.desc.lv[i].l ? 1u : 0u;
+        t.sh2[i] = L.desc.lv[i].l ? (uint32_t) L.desc.lv[i].l - 1u : 0u;
+        t.stride[i] = L.desc.lv[i].stride;
+    }
+}
+
+template <int V, int DIR, int U, int NL>
+__device__ __forceinline__ void yk_regular_tile(const yk_launch & L, uint32_t t0, uint32_t nunits)
+{
+    typedef typename yk_vec<V>::T VT;
+    yk_rt rt;
+    yk_rt_load<NL>(rt, L);
+    VT *packed = (VT *) rt.packed;
+    char *typed = rt.typed;
+    int64_t off[U];
+    VT v[U];
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+        uint32_t u = t0 + (uint32_t) (k * YK_THREADS + threadIdx.x);
+        uint32_t r = rt.p0 + u * (uint32_t) V;
+        int64_t o = 0;
+#pragma unroll
+        for (int i = 0; i < NL; i++) {
+            uint32_t t = __umulhi(rt.m[i], r);
+            uint32_t q = (t + ((r - t) >> rt.sh1[i])) >> rt.sh2[i];
+            r -= q * rt.cps[i];
+            o += (int64_t) q * rt.stride[i];
+        }
+        off[k] = o + (int64_t) r;
+    }
+    if (DIR == 0) {
+#pragma unroll
+        for (int k = 0; k < U; k++)
+            if (t0 + (uint32_t) (k * YK_THREADS + threadIdx.x) < nunits)
+                v[k] = yk_ldcg((const VT *) (typed + off[k]));
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            uint32_t u = t0 + (uint32_t) (k * YK_THREADS + threadIdx.x);
+            if (u < nunits)
+                packed[u] = v[k];
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            uint32_t u = t0 + (uint32_t) (k * YK_THREADS + threadIdx.x);
+            if (u < nunits)
+                v[k] = yk_ldcg((const VT *) (packed + u));
+        }
+#pragma unroll
+        for (int k = 0; k < U; k++)
+            if (t0 + (uint32_t) (k * YK_THREADS + threadIdx.x) < nunits)
+                *(VT *) (typed + off[k]) = v[k];
+    }
+}
+
+template <int V, int DIR, int U>
+__device__ __forceinline__ void yk_regular_dispatch(const yk_launch & L, uint32_t t0,
+                                                    uint32_t nunits)
+{
+    switch (L.regular) {
+        case 0: yk_regular_tile<V, DIR, U, 0>(L, t0, nunits); break;
+        case 1: yk_regular_tile<V, DIR, U, 1>(L, t0, nunits); break;
+        case 2: yk_regular_tile<V, DIR, U, 2>(L, t0, nunits); break;
+        default: yk_regular_tile<V, DIR, U, 3>(L, t0, nunits); break;
+    }
+}
+
+template <int V, int DIR, int U>
+__global__ void __launch_bounds__(YK_THREADS, (U == 1 ? 8 : 4))
+yk_regular_kernel(const __grid_constant__ yk_launch L)
+{
+    const uint32_t nunits = (uint32_t) (L.nbytes / V);
+    const uint32_t tile = (uint32_t) YK_THREADS * U;
+    for (uint32_t t0 = blockIdx.x * tile; t0 < nunits; t0 += gridDim.x * tile)
+        yk_regular_dispatch<V, DIR, U>(L, t0, nunits);
+}
+
+/* A batch of regular REPLACE requests: tiles numbered consecutively over requests. */
+template <int U>
+__global__ void __launch_bounds__(YK_THREADS, (U == 1 ? 8 : 4))
+yk_batch_regular_kernel(const __grid_constant__ yk_batch B)
+{
+    for (uint64_t g = blockIdx.x; g < B.tile_start[B.n]; g += gridDim.x) {
+        int r = 0;
+        while (g >= B.tile_start[r + 1])
+            r++;
+        const yk_launch & L = B.req[r];
+        const uint32_t nunits = (uint32_t) (L.nbytes / (uint64_t) L.vec);
+        const uint32_t t0 = (uint32_t) (g - B.tile_start[r]) * (uint32_t) (YK_THREADS * U);
+#define YK_RB(V) do { if (L.dir == 0) yk_regular_dispatch<V, 0, U>(L, t0, nunits); \
+                      else yk_regular_dispatch<V, 1, U>(L, t0, nunits); } while (0)
+        switch (L.vec) {
+            case 16: YK_RB(16); break;
+            case 8: YK_RB(8); break;
+            case 4: YK_RB(4); break;
+            case 2: YK_RB(2); break;
+            default: YK_RB(1); break;
+        }
+#undef YK_RB
+    }
+}
+
+template <typename IDX, int V, int DIR, int U>
 __global__ void __launch_bounds__(YK_THREADS)
 yk_bytes_kernel(const __grid_constant__ yk_launch L)
 {
-    typedef typename yk_vec<V>::T VT;
     const IDX nunits = (IDX) (L.nbytes / V);
-    const IDX p0 = (IDX) L.p0;
-    const IDX tile = (IDX) YK_THREADS * YK_UNROLL;
-    VT *packed = (VT *) L.packed;
-    char *typed = L.typed;
-    for (IDX t0 = (IDX) blockIdx.x * tile; t0 < nunits; t0 += (IDX) gridDim.x * tile) {
-        int64_t off[YK_UNROLL];
-        VT v[YK_UNROLL];
-#pragma unroll
-        for (int k = 0; k < YK_UNROLL; k++) {
-            IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
-            if (u < nunits)
-                off[k] = yk_locate<IDX>(L.desc, p0 + u * (IDX) V, nullptr, nullptr);
+    const IDX tile = (IDX) YK_THREADS * U;
+    for (IDX t0 = (IDX) blockIdx.x * tile; t0 < nunits; t0 += (IDX) gridDim.x * tile)
+        yk_bytes_tile<IDX, V, DIR, U>(L, t0, nunits);
+}
+
+/* Many REPLACE requests in one launch (yaksa_gb300_batch*): the requests' tiles are
+ * numbered consecutively and every CTA takes tiles grid-stride, so all requests'
+ * memory traffic is in flight together and the launch cost is paid once. */
+template <int U>
+__global__ void __launch_bounds__(YK_THREADS)
+yk_batch_kernel(const __grid_constant__ yk_batch B)
+{
+    for (uint64_t g = blockIdx.x; g < B.tile_start[B.n]; g += gridDim.x) {
+        int r = 0;
+        while (g >= B.tile_start[r + 1])
+            r++;
+        const yk_launch & L = B.req[r];
+        const uint32_t nunits = (uint32_t) (L.nbytes / (uint64_t) L.vec);
+        const uint32_t t0 = (uint32_t) (g - B.tile_start[r]) * (uint32_t) (YK_THREADS * U);
+#define YK_BT(V) do { if (L.dir == 0) yk_bytes_tile<uint32_t, V, 0, U>(L, t0, nunits); \
+                      else yk_bytes_tile<uint32_t, V, 1, U>(L, t0, nunits); } while (0)
+        switch (L.vec) {
+            case 16: YK_BT(16); break;
+            case 8: YK_BT(8); break;
+            case 4: YK_BT(4); break;
+            case 2: YK_BT(2); break;
+            default: YK_BT(1); break;
         }
-        if (DIR == 0) {
-#pragma unroll
-            for (int k = 0; k < YK_UNROLL; k++) {
-                IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
-                if (u < nunits)
-                    v[k] = __ldg((const VT *) (typed + off[k]));
-            }
-#pragma unroll
-            for (int k = 0; k < YK_UNROLL; k++) {
-                IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
-                if (u < nunits)
-                    packed[u] = v[k];
-            }
-        } else {
-#pragma unroll
-            for (int k = 0; k < YK_UNROLL; k++) {
-                IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
-                if (u < nunits)
-                    v[k] = __ldg(packed + u);
-            }
-#pragma unroll
-            for (int k = 0; k < YK_UNROLL; k++) {
-                IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
-                if (u < nunits)
-                    *(VT *) (typed + off[k]) = v[k];
-            }
-        }
+#undef YK_BT
     }
 }
 
@@ -517,13 +720,26 @@ static unsigned yk_grid(uint64_t units, uint64_t per_block, int blocks_per_sm)
     return (unsigned) (need ? need : 1);
 }
 
-template <typename IDX>
-static void launch_bytes(const yk_launch * l, cudaStream_t s)
+/* Units per thread: a launch that fits in the GPU's resident threads a few times over
+ * keeps one unit per thread (most requests in flight at once); larger launches take
+ * four per thread in a grid-stride loop. */
+extern "C" int yk_cuda_batch_units_per_thread(uint64_t total_units)
 {
-    uint64_t units = l->nbytes / (uint64_t) l->vec;
-    unsigned g = yk_grid(units, YK_THREADS * YK_UNROLL, 8);
-#define YK_B(V) do { if (l->dir == 0) yk_bytes_kernel<IDX, V, 0><<<g, YK_THREADS, 0, s>>>(*l); \
-                     else yk_bytes_kernel<IDX, V, 1><<<g, YK_THREADS, 0, s>>>(*l); } while (0)
+    return total_units <= (uint64_t) yk_cuda_num_sms() * 2048u * 4u ? 1 : YK_UNROLL;
+}
+
+extern "C" uint64_t yk_cuda_tiles(uint64_t units, int units_per_thread)
+{
+    uint64_t per = (uint64_t) YK_THREADS * (uint64_t) units_per_thread;
+    return (units + per - 1) / per;
+}
+
+template <typename IDX, int U>
+static void launch_bytes_u(const yk_launch * l, cudaStream_t s, uint64_t units)
+{
+    unsigned g = yk_grid(units, (uint64_t) YK_THREADS * U, U == 1 ? 64 : 8);
+#define YK_B(V) do { if (l->dir == 0) yk_bytes_kernel<IDX, V, 0, U><<<g, YK_THREADS, 0, s>>>(*l); \
+                     else yk_bytes_kernel<IDX, V, 1, U><<<g, YK_THREADS, 0, s>>>(*l); } while (0)
     switch (l->vec) {
         case 16: YK_B(16); break;
         case 8: YK_B(8); break;
@@ -532,6 +748,61 @@ static void launch_bytes(const yk_launch * l, cudaStream_t s)
         default: YK_B(1); break;
     }
 #undef YK_B
+}
+
+template <int U>
+static void launch_regular_u(const yk_launch * l, cudaStream_t s, uint64_t units)
+{
+    unsigned g = yk_grid(units, (uint64_t) YK_THREADS * U, U == 1 ? 64 : 8);
+#define YK_R(V) do { if (l->dir == 0) yk_regular_kernel<V, 0, U><<<g, YK_THREADS, 0, s>>>(*l); \
+                     else yk_regular_kernel<V, 1, U><<<g, YK_THREADS, 0, s>>>(*l); } while (0)
+    switch (l->vec) {
+        case 16: YK_R(16); break;
+        case 8: YK_R(8); break;
+        case 4: YK_R(4); break;
+        case 2: YK_R(2); break;
+        default: YK_R(1); break;
+    }
+#undef YK_R
+}
+
+template <typename IDX>
+static void launch_bytes(const yk_launch * l, cudaStream_t s)
+{
+    uint64_t units = l->nbytes / (uint64_t) l->vec;
+    int u = yk_cuda_batch_units_per_thread(units);
+    if (l->regular >= 0 && sizeof(IDX) == 4) {
+        if (u == 1)
+            launch_regular_u<1>(l, s, units);
+        else
+            launch_regular_u<YK_UNROLL>(l, s, units);
+    } else if (u == 1) {
+        launch_bytes_u<IDX, 1>(l, s, units);
+    } else {
+        launch_bytes_u<IDX, YK_UNROLL>(l, s, units);
+    }
+}
+
+extern "C" int yk_cuda_launch_batch(const yk_batch * b, int units_per_thread, int regular,
+                                    void *stream)
+{
+    cudaStream_t s = (cudaStream_t) stream;
+    uint64_t tiles = b->tile_start[b->n];
+    if (!tiles)
+        return 0;
+    uint64_t cap = (uint64_t) yk_cuda_num_sms() * (units_per_thread == 1 ? 64u : 8u);
+    unsigned g = (unsigned) (tiles < cap ? tiles : cap);
+    if (regular) {
+        /* one unit per thread: the 40 inlined (vector width, direction, depth) variants
+         * fit in 32 registers only at this size, and full occupancy keeps enough loads
+         * in flight; large batches loop grid-stride */
+        yk_batch_regular_kernel<1><<<g, YK_THREADS, 0, s>>>(*b);
+    } else if (units_per_thread == 1) {
+        yk_batch_kernel<1><<<g, YK_THREADS, 0, s>>>(*b);
+    } else {
+        yk_batch_kernel<YK_UNROLL><<<g, YK_THREADS, 0, s>>>(*b);
+    }
+    return (int) cudaGetLastError();
 }
 
 extern "C" int yk_cuda_launch_pup(const yk_launch * l, void *stream)

@@ -26,6 +26,7 @@
 #include <string.h>
 #include <cuda_runtime_api.h>
 #include "yk_internal.h"
+#include "yaksa_gb300.h"
 
 typedef struct {
     int in_use;
@@ -39,7 +40,8 @@ static struct {
     int ready;
     int failed;
     int device;
-    int pageable_access;
+    int pageable_access;        /* the GPU reads/writes pageable host memory (ATS) */
+    int host_ptr_ok;            /* registered host memory uses the host address */
     cudaStream_t stream;
     yk_req *reqs;
     size_t nreqs;
@@ -47,7 +49,7 @@ static struct {
     size_t nev, capev;
     /* counters (yaksa_gb300_stats) */
     uint64_t launches, staged_calls, direct_calls, memcpy_calls;
-} R = { PTHREAD_MUTEX_INITIALIZER, 0, 0, 0, 0, NULL, NULL, 0, NULL, 0, 0, 0, 0, 0, 0 };
+} R = { PTHREAD_MUTEX_INITIALIZER, 0, 0, 0, 0, 0, NULL, NULL, 0, NULL, 0, 0, 0, 0, 0, 0 };
 
 static int cuda_err(cudaError_t e, const char *what)
 {
@@ -82,6 +84,14 @@ static int runtime_ready(void)
             cudaGetDevice(&R.device);
             cudaDeviceGetAttribute(&R.pageable_access, cudaDevAttrPageableMemoryAccess,
                                    R.device);
+            cudaDeviceGetAttribute(&R.host_ptr_ok, cudaDevAttrCanUseHostPointerForRegisteredMem,
+                                   R.device);
+            /* Opt-in: the L2 fetch granularity of this process's context (a hint the
+             * driver may clamp; it ends with the process).  Strided types whose runs
+             * are shorter than a sector move less DRAM traffic with 32-byte fetches. */
+            const char *l2 = getenv("YAKSA_GB300_L2_FETCH_BYTES");
+            if (l2 && atoi(l2) > 0)
+                cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t) atoi(l2));
             e = cudaStreamCreateWithFlags(&R.stream, cudaStreamNonBlocking);
             if (e != cudaSuccess) {
                 cuda_err(e, "cudaStreamCreate");
@@ -257,6 +267,12 @@ int yaksa_request_wait(yaksa_request_t request)
 static char *device_alias(const char *base, const char *probe, int host_hint, int *staged)
 {
     *staged = 0;
+    /* Grace-Blackwell: the GPU addresses device memory, pinned and pageable host memory
+     * alike through the caller's pointer, so no per-call attribute query is needed
+     * (the reference queries both pointers of every request,
+     * src/backend/src/yaksur_pup.c:31-58) */
+    if (R.pageable_access && R.host_ptr_ok)
+        return (char *) base;
     struct cudaPointerAttributes a;
     memset(&a, 0, sizeof(a));
     cudaError_t e = cudaPointerGetAttributes(&a, probe);
@@ -290,8 +306,19 @@ static int pow2_of(uint64_t v)
 }
 
 /* ------------------------------------------------------------------------- */
-/* launch construction                                                       */
+/* planning: byte range, typed span and pointer routing of one request        */
 /* ------------------------------------------------------------------------- */
+
+typedef struct {
+    int dir;                    /* 0 pack, 1 unpack */
+    yk_type *t;
+    uintptr_t count, b0, b1;
+    yaksa_op_t op;
+    char *typed, *packed;       /* caller's pointers */
+    char *dtyped, *dpacked;     /* device-usable aliases */
+    int staged;                 /* 1: the GPU cannot address one of the buffers */
+    int64_t lo, hi;             /* typed bytes touched, relative to typed */
+} yk_plan;
 
 static int op_needs_host_arith(yk_type * t, yaksa_op_t op)
 {
@@ -299,46 +326,99 @@ static int op_needs_host_arith(yk_type * t, yaksa_op_t op)
                                  op == YAKSA_OP__MIN || op == YAKSA_OP__MAX);
 }
 
-/* Enqueue the kernel(s) for [b0, b1) on `s`.  typed/packed are device-usable. */
-static int enqueue(int dir, char *typed, char *packed, yk_type * t, uintptr_t count,
-                   uintptr_t b0, uintptr_t b1, yaksa_op_t op, cudaStream_t s)
+/* Partial packs follow the reference: start at `offset` and stop at the last builtin
+ * boundary that fits (src/frontend/pup/yaksi_ipack.c:12-107). */
+static int plan(int dir, const void *packed_in, void *packed_out, char *typed, uintptr_t count,
+                yk_type * t, uintptr_t offset, uintptr_t maxbytes, yk_info * info, yaksa_op_t op,
+                yk_plan * p)
 {
-    uintptr_t n = b1 - b0;
+    memset(p, 0, sizeof(*p));
+    p->dir = dir;
+    p->t = t;
+    p->count = count;
+    p->op = op;
+    if (count == 0 || t->size == 0)
+        return YAKSA_SUCCESS;
+    if (op >= YAKSA_OP__LAST)
+        return YAKSA_ERR__INTERNAL;
+    uintptr_t total = count * t->size;
+    if (offset >= total)
+        return YAKSA_SUCCESS;
+    uintptr_t b0 = offset;
+    if (yk_builtin_floor(t, count, b0) != b0)
+        return YAKSA_ERR__INTERNAL;     /* offset inside a builtin: a precondition */
+    uintptr_t b1 = yk_builtin_floor(t, count, b0 + YK_MIN(maxbytes, total - b0));
+    if (b1 <= b0)
+        return YAKSA_SUCCESS;
+    if (op != YAKSA_OP__REPLACE && op_needs_host_arith(t, op))
+        return YAKSA_ERR__NOT_SUPPORTED;        /* long double arithmetic has no GPU form */
+    int rc = runtime_ready();
+    if (rc)
+        return rc;
+    p->b0 = b0;
+    p->b1 = b1;
+    p->typed = typed;
+    p->packed = dir == 0 ? (char *) packed_out : (char *) packed_in;
+    uintptr_t e0 = b0 / t->size, e1 = (b1 + t->size - 1) / t->size;
+    int64_t ext = t->extent;
+    p->lo = (ext >= 0 ? (int64_t) e0 * ext : (int64_t) (e1 - 1) * ext) + t->true_lb;
+    p->hi = (ext >= 0 ? (int64_t) (e1 - 1) * ext : (int64_t) e0 * ext) + t->true_ub;
+    int host_hint = info && info->gpu_driver == 2;
+    int st_t = 0, st_p = 0;
+    p->dtyped = device_alias(typed, typed + p->lo, host_hint, &st_t);
+    p->dpacked = device_alias(p->packed, p->packed, host_hint, &st_p);
+    p->staged = st_t | (st_p << 1);
+    return YAKSA_SUCCESS;
+}
+
+/* ------------------------------------------------------------------------- */
+/* launch construction                                                       */
+/* ------------------------------------------------------------------------- */
+
+enum { YK_X_MEMCPY, YK_X_BYTES, YK_X_TYPED, YK_X_ORDERED };
+
+static int prepare(const yk_plan * p, char *typed, char *packed, yk_launch * L, int *kind,
+                   int *sorted)
+{
+    yk_type *t = p->t;
+    uintptr_t count = p->count, b0 = p->b0, n = p->b1 - p->b0;
+    yaksa_op_t op = p->op;
+    memset(L, 0, sizeof(*L));
+    L->typed = typed;
+    L->packed = packed;
+    L->p0 = b0;
+    L->nbytes = n;
+    L->op = op;
+    L->dir = p->dir;
+    L->use64 = (p->b1 > 0xffffffffull);
+    *sorted = 0;
     if (op == YAKSA_OP__REPLACE && t->is_contig) {
-        /* contiguous: the packed bytes are the memory bytes from true_lb */
-        char *mem = typed + t->true_lb + b0;
-        __atomic_add_fetch(&R.memcpy_calls, 1, __ATOMIC_RELAXED);
-        return cuda_err(cudaMemcpyAsync(dir == 0 ? packed : mem, dir == 0 ? mem : packed, n,
-                                        cudaMemcpyDefault, s), "cudaMemcpyAsync");
+        *kind = YK_X_MEMCPY;
+        return YAKSA_SUCCESS;
     }
     int typed_op = (op != YAKSA_OP__REPLACE);
     yk_devdesc *dd;
     int rc = yk_desc_get(t, typed_op, &dd);
     if (rc)
         return rc;
-    int overlap = dir == 1 && (dd->may_overlap ||
-                               (count > 1 && (int64_t) (t->extent < 0 ? -t->extent : t->extent)
-                                < dd->elem_span));
+    uint64_t ext = (uint64_t) (t->extent < 0 ? -t->extent : t->extent);
+    int overlap = p->dir == 1 && (dd->may_overlap || (count > 1 && (int64_t) ext < dd->elem_span));
     yk_devdesc *ddo = dd;
     if (overlap && !typed_op) {
-        /* ordered REPLACE reuses the typed descriptor's element structure when the
-         * type is homogeneous (owner-computes), else the bytes descriptor */
+        /* ordered REPLACE uses the typed descriptor's element structure when the
+         * sorted-block kernel applies to it */
         yk_devdesc *tdd;
         if (t->base_type > 0 && yk_desc_get(t, 1, &tdd) == YAKSA_SUCCESS && tdd->sorted_blocks)
             ddo = tdd;
     }
-
-    yk_launch L;
-    memset(&L, 0, sizeof(L));
-    yk_make_launch_desc(ddo, t, count, &L.desc);
-    L.typed = typed;
-    L.packed = packed;
-    L.p0 = b0;
-    L.nbytes = n;
-    L.op = op;
-    L.dir = dir;
-    L.use64 = (b1 > 0xffffffffull);
-    uint64_t ext = (uint64_t) (t->extent < 0 ? -t->extent : t->extent);
+    yk_make_launch_desc(ddo, t, count, &L->desc);
+    L->regular = -1;
+    if (!L->use64 && L->desc.leaf == YK_LEAF_RUN && L->desc.nlev <= YK_REGULAR_MAX) {
+        L->regular = L->desc.nlev;
+        for (int i = 0; i < L->desc.nlev; i++)
+            if (L->desc.lv[i].kind != YK_LV_VEC)
+                L->regular = -1;
+    }
     if (ddo == dd && !typed_op) {
         /* widest unit that every run, offset, pointer and range bound allows */
         int v = ddo->vec_align;
@@ -349,122 +429,102 @@ static int enqueue(int dir, char *typed, char *packed, yk_type * t, uintptr_t co
         v = YK_MIN(v, pow2_of(t->size));
         if (count > 1)
             v = YK_MIN(v, pow2_of(ext));
-        L.vec = v;
-        L.typed_op = 0;
+        L->vec = v;
+        L->typed_op = 0;
     } else {
         /* element granularity; alignment is checked per access in the kernel */
-        L.typed_op = 1;
-        L.vec = ddo->unit;
+        L->typed_op = 1;
+        L->vec = ddo->unit;
         if (!typed_op)
-            L.op = YAKSA_OP__REPLACE;
+            L->op = YAKSA_OP__REPLACE;
+    }
+    if (overlap) {
+        *kind = YK_X_ORDERED;
+        *sorted = ddo->sorted_blocks && L->typed_op && L->desc.nlev == 1 &&
+            L->desc.lv[0].kind == YK_LV_IDX &&
+            ddo->elem_align >= yk_base_type_size(t->base_type);
+        if (!L->typed_op && !*sorted)
+            L->vec = (int) YK_MIN((uint64_t) L->vec, (uint64_t) ddo->vec_align);
+    } else {
+        *kind = L->typed_op ? YK_X_TYPED : YK_X_BYTES;
+    }
+    return YAKSA_SUCCESS;
+}
+
+static int launch_prepared(const yk_plan * p, const yk_launch * L, int kind, int sorted,
+                           cudaStream_t s)
+{
+    if (kind == YK_X_MEMCPY) {
+        /* contiguous: the packed bytes are the memory bytes from true_lb */
+        char *mem = L->typed + p->t->true_lb + L->p0;
+        __atomic_add_fetch(&R.memcpy_calls, 1, __ATOMIC_RELAXED);
+        return cuda_err(cudaMemcpyAsync(p->dir == 0 ? L->packed : mem,
+                                        p->dir == 0 ? mem : L->packed, L->nbytes,
+                                        cudaMemcpyDefault, s), "cudaMemcpyAsync");
     }
     __atomic_add_fetch(&R.launches, 1, __ATOMIC_RELAXED);
-    int e;
-    if (overlap) {
-        int sorted = ddo->sorted_blocks && L.typed_op && L.desc.nlev == 1 &&
-            L.desc.lv[0].kind == YK_LV_IDX && ddo->elem_align >= yk_base_type_size(t->base_type);
-        if (!L.typed_op && !sorted)
-            L.vec = (int) YK_MIN((uint64_t) L.vec, (uint64_t) ddo->vec_align);
-        e = yk_cuda_launch_unpack_ordered(&L, sorted, s);
-    } else {
-        e = yk_cuda_launch_pup(&L, s);
-    }
+    int e = (kind == YK_X_ORDERED) ? yk_cuda_launch_unpack_ordered(L, sorted, s) :
+        yk_cuda_launch_pup(L, s);
     return cuda_err((cudaError_t) e, "kernel launch");
 }
 
-/* ------------------------------------------------------------------------- */
-/* the pack/unpack entry                                                     */
-/* ------------------------------------------------------------------------- */
-
-int yk_pup(int dir, const void *packed_in, void *packed_out, char *typed, uintptr_t count,
-           yk_type * t, uintptr_t offset, uintptr_t maxbytes, uintptr_t * actual,
-           yk_info * info, yaksa_op_t op, int mode, void *stream, yaksa_request_t * request)
+static int enqueue(const yk_plan * p, char *typed, char *packed, cudaStream_t s)
 {
-    if (request)
-        *request = YAKSA_REQUEST__NULL;
-    *actual = 0;
-    if (count == 0 || t->size == 0)
-        return YAKSA_SUCCESS;
-    if (op >= YAKSA_OP__LAST)
-        return YAKSA_ERR__INTERNAL;
-    uintptr_t total = count * t->size;
-    if (offset >= total)
-        return YAKSA_SUCCESS;
-    uintptr_t b0 = offset;
-    uintptr_t b1 = yk_builtin_floor(t, count, b0 + YK_MIN(maxbytes, total - b0));
-    if (yk_builtin_floor(t, count, b0) != b0)
-        return YAKSA_ERR__INTERNAL;     /* offset inside a builtin: a precondition */
-    if (b1 <= b0)
-        return YAKSA_SUCCESS;
-    if (op != YAKSA_OP__REPLACE && op_needs_host_arith(t, op))
-        return YAKSA_ERR__NOT_SUPPORTED;        /* long double arithmetic has no GPU form */
-
-    int rc = runtime_ready();
+    yk_launch L;
+    int kind, sorted;
+    int rc = prepare(p, typed, packed, &L, &kind, &sorted);
     if (rc)
         return rc;
+    return launch_prepared(p, &L, kind, sorted, s);
+}
 
-    char *packed = dir == 0 ? (char *) packed_out : (char *) packed_in;
-    cudaStream_t s = (mode == YK_MODE_STREAM && stream) ? *(cudaStream_t *) stream : R.stream;
-    int host_hint = info && info->gpu_driver == 2;
-
-    /* typed span touched by elements [e0, e1) */
-    uintptr_t e0 = b0 / t->size, e1 = (b1 + t->size - 1) / t->size;
-    int64_t ext = t->extent;
-    int64_t lo = (ext >= 0 ? (int64_t) e0 * ext : (int64_t) (e1 - 1) * ext) + t->true_lb;
-    int64_t hi = (ext >= 0 ? (int64_t) (e1 - 1) * ext : (int64_t) e0 * ext) + t->true_ub;
-
-    int st_t = 0, st_p = 0;
-    char *dtyped = device_alias(typed, typed + lo, host_hint, &st_t);
-    char *dpacked = device_alias(packed, packed, host_hint, &st_p);
+/* The GPU cannot address a buffer: copy the touched span to device memory from the
+ * stream-ordered pool, run, copy back; completes before returning. */
+static int run_staged(const yk_plan * p, cudaStream_t s)
+{
+    __atomic_add_fetch(&R.staged_calls, 1, __ATOMIC_RELAXED);
     void *scr_t = NULL, *scr_p = NULL;
-    uintptr_t n = b1 - b0;
-
-    if (st_t || st_p) {
-        /* staged: copy what the kernel reads into device memory, run, copy back */
-        __atomic_add_fetch(&R.staged_calls, 1, __ATOMIC_RELAXED);
-        if (st_t) {
-            rc = cuda_err(cudaMallocAsync(&scr_t, (size_t) (hi - lo), s), "cudaMallocAsync");
-            if (rc)
-                return rc;
-            rc = cuda_err(cudaMemcpyAsync(scr_t, typed + lo, (size_t) (hi - lo),
-                                          cudaMemcpyHostToDevice, s), "stage in");
-            dtyped = (char *) scr_t - lo;
-        }
-        if (!rc && st_p) {
-            rc = cuda_err(cudaMallocAsync(&scr_p, n, s), "cudaMallocAsync");
-            if (!rc && (dir == 1 || op != YAKSA_OP__REPLACE))
-                rc = cuda_err(cudaMemcpyAsync(scr_p, packed, n, cudaMemcpyHostToDevice, s),
-                              "stage in");
-            dpacked = scr_p;
-        }
+    char *dtyped = p->dtyped, *dpacked = p->dpacked;
+    uintptr_t n = p->b1 - p->b0;
+    size_t span = (size_t) (p->hi - p->lo);
+    int rc = YAKSA_SUCCESS;
+    if (p->staged & 1) {
+        rc = cuda_err(cudaMallocAsync(&scr_t, span, s), "cudaMallocAsync");
         if (!rc)
-            rc = enqueue(dir, dtyped, dpacked, t, count, b0, b1, op, s);
-        if (!rc && dir == 0 && st_p)
-            rc = cuda_err(cudaMemcpyAsync(packed, scr_p, n, cudaMemcpyDeviceToHost, s),
-                          "stage out");
-        if (!rc && dir == 1 && st_t)
-            rc = cuda_err(cudaMemcpyAsync(typed + lo, scr_t, (size_t) (hi - lo),
-                                          cudaMemcpyDeviceToHost, s), "stage out");
-        if (scr_t)
-            cudaFreeAsync(scr_t, s);
-        if (scr_p)
-            cudaFreeAsync(scr_p, s);
-        if (!rc)
-            rc = cuda_err(cudaStreamSynchronize(s), "staged completion");
-        if (!rc)
-            *actual = n;
-        return rc;
+            rc = cuda_err(cudaMemcpyAsync(scr_t, p->typed + p->lo, span, cudaMemcpyHostToDevice, s),
+                          "stage in");
+        dtyped = (char *) scr_t - p->lo;
     }
+    if (!rc && (p->staged & 2)) {
+        rc = cuda_err(cudaMallocAsync(&scr_p, n, s), "cudaMallocAsync");
+        if (!rc && (p->dir == 1 || p->op != YAKSA_OP__REPLACE))
+            rc = cuda_err(cudaMemcpyAsync(scr_p, p->packed, n, cudaMemcpyHostToDevice, s),
+                          "stage in");
+        dpacked = scr_p;
+    }
+    if (!rc)
+        rc = enqueue(p, dtyped, dpacked, s);
+    if (!rc && p->dir == 0 && (p->staged & 2))
+        rc = cuda_err(cudaMemcpyAsync(p->packed, scr_p, n, cudaMemcpyDeviceToHost, s), "stage out");
+    if (!rc && p->dir == 1 && (p->staged & 1))
+        rc = cuda_err(cudaMemcpyAsync(p->typed + p->lo, scr_t, span, cudaMemcpyDeviceToHost, s),
+                      "stage out");
+    if (scr_t)
+        cudaFreeAsync(scr_t, s);
+    if (scr_p)
+        cudaFreeAsync(scr_p, s);
+    if (!rc)
+        rc = cuda_err(cudaStreamSynchronize(s), "staged completion");
+    return rc;
+}
 
-    __atomic_add_fetch(&R.direct_calls, 1, __ATOMIC_RELAXED);
-    rc = enqueue(dir, dtyped, dpacked, t, count, b0, b1, op, s);
-    if (rc)
-        return rc;
-    *actual = n;
+/* completion for nonblocking / blocking modes: one pooled event */
+static int complete(yk_type * t, int mode, cudaStream_t s, yaksa_request_t * request)
+{
     if (mode == YK_MODE_STREAM)
         return YAKSA_SUCCESS;
     cudaEvent_t ev;
-    rc = event_get(&ev);
+    int rc = event_get(&ev);
     if (rc)
         return rc;
     rc = cuda_err(cudaEventRecord(ev, s), "cudaEventRecord");
@@ -477,14 +537,42 @@ int yk_pup(int dir, const void *packed_in, void *packed_out, char *typed, uintpt
         event_put(ev);
         return rc;
     }
-    yk_type_ref(t);
+    if (t)
+        yk_type_ref(t);
     rc = request_new(ev, t, NULL, NULL, request);
     if (rc) {
         cudaEventSynchronize(ev);
         event_put(ev);
-        yk_type_unref(t);
+        if (t)
+            yk_type_unref(t);
     }
     return rc;
+}
+
+int yk_pup(int dir, const void *packed_in, void *packed_out, char *typed, uintptr_t count,
+           yk_type * t, uintptr_t offset, uintptr_t maxbytes, uintptr_t * actual,
+           yk_info * info, yaksa_op_t op, int mode, void *stream, yaksa_request_t * request)
+{
+    if (request)
+        *request = YAKSA_REQUEST__NULL;
+    *actual = 0;
+    yk_plan p;
+    int rc = plan(dir, packed_in, packed_out, typed, count, t, offset, maxbytes, info, op, &p);
+    if (rc || p.b1 == p.b0)
+        return rc;
+    cudaStream_t s = (mode == YK_MODE_STREAM && stream) ? *(cudaStream_t *) stream : R.stream;
+    if (p.staged) {
+        rc = run_staged(&p, s);
+        if (!rc)
+            *actual = p.b1 - p.b0;
+        return rc;
+    }
+    __atomic_add_fetch(&R.direct_calls, 1, __ATOMIC_RELAXED);
+    rc = enqueue(&p, p.dtyped, p.dpacked, s);
+    if (rc)
+        return rc;
+    *actual = p.b1 - p.b0;
+    return complete(t, mode, s, request);
 }
 
 /* ------------------------------------------------------------------------- */
@@ -498,10 +586,9 @@ int yaksa_ipack(const void *inbuf, uintptr_t incount, yaksa_type_t type, uintptr
                 yaksa_info_t info, yaksa_op_t op, yaksa_request_t * request)
 {
     *request = YAKSA_REQUEST__NULL;
-    if (incount == 0) {
-        *actual_pack_bytes = 0;
+    *actual_pack_bytes = 0;
+    if (incount == 0)
         return YAKSA_SUCCESS;
-    }
     TYPE_OR_FAIL(type, t);
     return yk_pup(0, NULL, outbuf, (char *) inbuf, incount, t, inoffset, max_pack_bytes,
                   actual_pack_bytes, info, op, YK_MODE_NONBLOCKING, NULL, request);
@@ -511,10 +598,9 @@ int yaksa_pack(const void *inbuf, uintptr_t incount, yaksa_type_t type, uintptr_
                void *outbuf, uintptr_t max_pack_bytes, uintptr_t * actual_pack_bytes,
                yaksa_info_t info, yaksa_op_t op)
 {
-    if (incount == 0) {
-        *actual_pack_bytes = 0;
+    *actual_pack_bytes = 0;
+    if (incount == 0)
         return YAKSA_SUCCESS;
-    }
     TYPE_OR_FAIL(type, t);
     return yk_pup(0, NULL, outbuf, (char *) inbuf, incount, t, inoffset, max_pack_bytes,
                   actual_pack_bytes, info, op, YK_MODE_BLOCKING, NULL, NULL);
@@ -524,10 +610,9 @@ int yaksa_pack_stream(const void *inbuf, uintptr_t incount, yaksa_type_t type, u
                       void *outbuf, uintptr_t max_pack_bytes, uintptr_t * actual_pack_bytes,
                       yaksa_info_t info, yaksa_op_t op, void *stream)
 {
-    if (incount == 0) {
-        *actual_pack_bytes = 0;
+    *actual_pack_bytes = 0;
+    if (incount == 0)
         return YAKSA_SUCCESS;
-    }
     TYPE_OR_FAIL(type, t);
     return yk_pup(0, NULL, outbuf, (char *) inbuf, incount, t, inoffset, max_pack_bytes,
                   actual_pack_bytes, info, op, YK_MODE_STREAM, stream, NULL);
@@ -538,10 +623,9 @@ int yaksa_iunpack(const void *inbuf, uintptr_t insize, void *outbuf, uintptr_t o
                   yaksa_info_t info, yaksa_op_t op, yaksa_request_t * request)
 {
     *request = YAKSA_REQUEST__NULL;
-    if (outcount == 0) {
-        *actual_unpack_bytes = 0;
+    *actual_unpack_bytes = 0;
+    if (outcount == 0)
         return YAKSA_SUCCESS;
-    }
     TYPE_OR_FAIL(type, t);
     return yk_pup(1, inbuf, NULL, (char *) outbuf, outcount, t, outoffset, insize,
                   actual_unpack_bytes, info, op, YK_MODE_NONBLOCKING, NULL, request);
@@ -551,10 +635,9 @@ int yaksa_unpack(const void *inbuf, uintptr_t insize, void *outbuf, uintptr_t ou
                  yaksa_type_t type, uintptr_t outoffset, uintptr_t * actual_unpack_bytes,
                  yaksa_info_t info, yaksa_op_t op)
 {
-    if (outcount == 0) {
-        *actual_unpack_bytes = 0;
+    *actual_unpack_bytes = 0;
+    if (outcount == 0)
         return YAKSA_SUCCESS;
-    }
     TYPE_OR_FAIL(type, t);
     return yk_pup(1, inbuf, NULL, (char *) outbuf, outcount, t, outoffset, insize,
                   actual_unpack_bytes, info, op, YK_MODE_BLOCKING, NULL, NULL);
@@ -564,13 +647,253 @@ int yaksa_unpack_stream(const void *inbuf, uintptr_t insize, void *outbuf, uintp
                         yaksa_type_t type, uintptr_t outoffset, uintptr_t * actual_unpack_bytes,
                         yaksa_info_t info, yaksa_op_t op, void *stream)
 {
-    if (outcount == 0) {
-        *actual_unpack_bytes = 0;
+    *actual_unpack_bytes = 0;
+    if (outcount == 0)
         return YAKSA_SUCCESS;
-    }
     TYPE_OR_FAIL(type, t);
     return yk_pup(1, inbuf, NULL, (char *) outbuf, outcount, t, outoffset, insize,
                   actual_unpack_bytes, info, op, YK_MODE_STREAM, stream, NULL);
+}
+
+/* ------------------------------------------------------------------------- */
+/* batches: many independent requests, one launch for the byte-moving ones    */
+/* ------------------------------------------------------------------------- */
+
+/* One launch per group of at most YK_BATCH_MAX requests of one shape class
+ * (regular nests, everything else). */
+static int flush_class(yk_launch * ls, int n, int regular, cudaStream_t s)
+{
+    uint64_t units = 0;
+    for (int i = 0; i < n; i++)
+        units += ls[i].nbytes / (uint64_t) ls[i].vec;
+    int u = regular ? 1 : yk_cuda_batch_units_per_thread(units);
+    static __thread yk_batch B;
+    for (int i0 = 0; i0 < n; i0 += YK_BATCH_MAX) {
+        int m = YK_MIN(YK_BATCH_MAX, n - i0);
+        B.n = m;
+        B.tile_start[0] = 0;
+        for (int i = 0; i < m; i++) {
+            B.req[i] = ls[i0 + i];
+            B.tile_start[i + 1] = B.tile_start[i] +
+                yk_cuda_tiles(ls[i0 + i].nbytes / (uint64_t) ls[i0 + i].vec, u);
+        }
+        __atomic_add_fetch(&R.launches, 1, __ATOMIC_RELAXED);
+        int rc = cuda_err((cudaError_t) yk_cuda_launch_batch(&B, u, regular, s), "batch launch");
+        if (rc)
+            return rc;
+    }
+    return YAKSA_SUCCESS;
+}
+
+static int flush_batch(yk_launch * ls, int n, cudaStream_t s)
+{
+    /* regular requests first (stable partition), then the rest */
+    yk_launch *tmp = malloc(sizeof(yk_launch) * (n > 0 ? n : 1));
+    if (!tmp)
+        return YAKSA_ERR__OUT_OF_MEM;
+    int nr = 0, ng = 0;
+    for (int i = 0; i < n; i++)
+        if (ls[i].regular >= 0)
+            tmp[nr++] = ls[i];
+    for (int i = 0; i < n; i++)
+        if (ls[i].regular < 0)
+            tmp[nr + ng++] = ls[i];
+    int rc = YAKSA_SUCCESS;
+    if (nr)
+        rc = flush_class(tmp, nr, 1, s);
+    if (!rc && ng)
+        rc = flush_class(tmp + nr, ng, 0, s);
+    free(tmp);
+    return rc;
+}
+
+static int batch_run(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info, cudaStream_t s)
+{
+    yk_launch *ls = malloc(sizeof(yk_launch) * (n > 0 ? n : 1));
+    if (!ls)
+        return YAKSA_ERR__OUT_OF_MEM;
+    int nb = 0, rc = YAKSA_SUCCESS;
+    for (int i = 0; i < n && !rc; i++) {
+        yaksa_gb300_pup_t *o = &ops[i];
+        o->actual = 0;
+        if (o->count == 0)
+            continue;
+        yk_type *t = yk_type_get(o->type);
+        if (!t) {
+            rc = YAKSA_ERR__INTERNAL;
+            break;
+        }
+        yk_plan p;
+        if (o->kind == 0)
+            rc = plan(0, NULL, o->outbuf, (char *) o->inbuf, o->count, t, o->offset, o->maxbytes,
+                      info, o->op, &p);
+        else
+            rc = plan(1, o->inbuf, NULL, (char *) o->outbuf, o->count, t, o->offset, o->maxbytes,
+                      info, o->op, &p);
+        if (rc || p.b1 == p.b0)
+            continue;
+        o->actual = p.b1 - p.b0;
+        if (p.staged) {
+            rc = run_staged(&p, s);
+            continue;
+        }
+        __atomic_add_fetch(&R.direct_calls, 1, __ATOMIC_RELAXED);
+        int kind, sorted;
+        rc = prepare(&p, p.dtyped, p.dpacked, &ls[nb], &kind, &sorted);
+        if (rc)
+            break;
+        if (kind == YK_X_BYTES && !ls[nb].use64)
+            nb++;
+        else
+            rc = launch_prepared(&p, &ls[nb], kind, sorted, s);
+    }
+    if (!rc && nb)
+        rc = flush_batch(ls, nb, s);
+    free(ls);
+    return rc;
+}
+
+int yaksa_gb300_pup_batch_stream(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info, void *stream)
+{
+    int rc = runtime_ready();
+    if (rc)
+        return rc;
+    cudaStream_t s = stream ? *(cudaStream_t *) stream : R.stream;
+    return batch_run(ops, n, info, s);
+}
+
+int yaksa_gb300_pup_batch(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info)
+{
+    int rc = runtime_ready();
+    if (rc)
+        return rc;
+    rc = batch_run(ops, n, info, R.stream);
+    if (rc)
+        return rc;
+    return complete(NULL, YK_MODE_BLOCKING, R.stream, NULL);
+}
+
+int yaksa_gb300_ipup_batch(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info,
+                           yaksa_request_t * request)
+{
+    *request = YAKSA_REQUEST__NULL;
+    int rc = runtime_ready();
+    if (rc)
+        return rc;
+    rc = batch_run(ops, n, info, R.stream);
+    if (rc)
+        return rc;
+    return complete(NULL, YK_MODE_NONBLOCKING, R.stream, request);
+}
+
+/* ------------------------------------------------------------------------- */
+/* captured graphs: a fixed sequence of batches replayed with one launch      */
+/* ------------------------------------------------------------------------- */
+
+struct yaksa_gb300_graph_s {
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    yk_type **types;            /* held while the graph exists */
+    int ntypes;
+};
+
+int yaksa_gb300_graph_create(yaksa_gb300_pup_t * ops, const int *batch_ends, int nbatches,
+                             yaksa_info_t info, yaksa_gb300_graph_t * graph)
+{
+    *graph = NULL;
+    int rc = runtime_ready();
+    if (rc)
+        return rc;
+    int n = nbatches ? batch_ends[nbatches - 1] : 0;
+    struct yaksa_gb300_graph_s *g = calloc(1, sizeof(*g));
+    if (!g)
+        return YAKSA_ERR__OUT_OF_MEM;
+    g->types = calloc(n ? n : 1, sizeof(yk_type *));
+    if (!g->types) {
+        free(g);
+        return YAKSA_ERR__OUT_OF_MEM;
+    }
+    /* build every descriptor and refuse staged requests before capturing: nothing
+     * inside the capture may allocate or synchronize */
+    for (int i = 0; i < n; i++) {
+        yaksa_gb300_pup_t *o = &ops[i];
+        if (o->count == 0)
+            continue;
+        yk_type *t = yk_type_get(o->type);
+        if (!t) {
+            rc = YAKSA_ERR__INTERNAL;
+            break;
+        }
+        yk_plan p;
+        rc = o->kind == 0 ?
+            plan(0, NULL, o->outbuf, (char *) o->inbuf, o->count, t, o->offset, o->maxbytes,
+                 info, o->op, &p) :
+            plan(1, o->inbuf, NULL, (char *) o->outbuf, o->count, t, o->offset, o->maxbytes,
+                 info, o->op, &p);
+        if (rc)
+            break;
+        if (p.b1 == p.b0)
+            continue;
+        if (p.staged) {
+            rc = YAKSA_ERR__NOT_SUPPORTED;
+            break;
+        }
+        yk_devdesc *dd;
+        if ((rc = yk_desc_get(t, o->op != YAKSA_OP__REPLACE, &dd)) ||
+            (o->op == YAKSA_OP__REPLACE && t->base_type > 0 && (rc = yk_desc_get(t, 1, &dd))))
+            break;
+        yk_type_ref(t);
+        g->types[g->ntypes++] = t;
+    }
+    cudaStream_t cs = NULL;
+    if (!rc)
+        rc = cuda_err(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking), "cudaStreamCreate");
+    if (!rc)
+        rc = cuda_err(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed), "capture");
+    if (!rc) {
+        int start = 0;
+        for (int b = 0; b < nbatches && !rc; b++) {
+            rc = batch_run(ops + start, batch_ends[b] - start, info, cs);
+            start = batch_ends[b];
+        }
+        cudaError_t e = cudaStreamEndCapture(cs, &g->graph);
+        if (!rc)
+            rc = cuda_err(e, "capture");
+        if (!rc)
+            rc = cuda_err(cudaGraphInstantiate(&g->exec, g->graph, 0), "cudaGraphInstantiate");
+    }
+    if (cs)
+        cudaStreamDestroy(cs);
+    if (rc) {
+        yaksa_gb300_graph_free(g);
+        return rc;
+    }
+    *graph = g;
+    return YAKSA_SUCCESS;
+}
+
+int yaksa_gb300_graph_launch(yaksa_gb300_graph_t g, void *stream)
+{
+    if (!g)
+        return YAKSA_ERR__INTERNAL;
+    cudaStream_t s = stream ? *(cudaStream_t *) stream : R.stream;
+    __atomic_add_fetch(&R.launches, 1, __ATOMIC_RELAXED);
+    return cuda_err(cudaGraphLaunch(g->exec, s), "cudaGraphLaunch");
+}
+
+int yaksa_gb300_graph_free(yaksa_gb300_graph_t g)
+{
+    if (!g)
+        return YAKSA_SUCCESS;
+    if (g->exec)
+        cudaGraphExecDestroy(g->exec);
+    if (g->graph)
+        cudaGraphDestroy(g->graph);
+    for (int i = 0; i < g->ntypes; i++)
+        yk_type_unref(g->types[i]);
+    free(g->types);
+    free(g);
+    return YAKSA_SUCCESS;
 }
 
 /* runtime counters for tests and the bench */
