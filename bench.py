@@ -175,6 +175,152 @@ def run_reference(args):
 METRIC = "pack+unpack GB/s vs HBM peak (bit-exact); batched p50/p99 us vs plain path"
 
 
+# ---------------------------------------------------------------------------
+# the other configurations: one JSON line per (config, direction) with a full-size
+# byte comparison against the oracle and the oracle's own time on the host
+# ---------------------------------------------------------------------------
+
+def suite_types(y, yk, np, rng_seed=7):
+    """Seeded synthetic inputs with the shapes and distributions of each config."""
+    rng = np.random.default_rng(rng_seed)
+    out = {}
+    # hvector of double: 4-column block of a 1024x16 row-major matrix
+    out["hvector"] = dict(mk=lambda L: L.type_create_hvector(1024, 4, 128, yk.TYPE_DOUBLE),
+                          base="double", count=1, extent=1024 * 16 * 8)
+    # hindexed int32: 2^20 blocks, lognormal lengths (median 16, sigma 1, clipped 1..4096),
+    # non-overlapping blocks in shuffled order with random gaps inside 1 GiB
+    nb = 1 << 20
+    blens = np.clip(np.round(np.exp(np.log(16) + rng.standard_normal(nb))), 1, 4096).astype(np.int64)
+    slots_total = (1 << 30) // 4
+    free = slots_total - int(blens.sum())
+    gaps = rng.integers(0, 2 * (free // nb), nb)
+    order = rng.permutation(nb)
+    starts = np.cumsum(blens[order] + gaps) - blens[order]
+    displs = np.empty(nb, dtype=np.int64)
+    displs[order] = starts * 4
+    assert int(starts[-1] + blens[order][-1]) <= slots_total
+
+    def mk_hindexed(L):
+        h = L.type_create_hindexed_arrays(nb, blens.ctypes.data, displs.ctypes.data, yk.TYPE_INT32_T)
+        r = L.type_create_resized(h, 0, 1 << 30)
+        L.type_free(h)
+        return r
+    out["hindexed"] = dict(mk=mk_hindexed, base="int32", count=1, extent=1 << 30,
+                           keep=(blens, displs))
+
+    def mk_struct(L):
+        s = L.type_create_struct([1, 3], [0, 8], [yk.TYPE_INT64_T, yk.TYPE_FLOAT])
+        r = L.type_create_resized(s, 0, 32)
+        L.type_free(s)
+        return r
+    out["struct"] = dict(mk=mk_struct, base="float", count=8 << 20, extent=32 * (8 << 20))
+    # indexed_block: 2^22 blocks of 8 elements at sorted random element offsets
+    for base, h, es, op in (("double", yk.TYPE_DOUBLE, 8, yk.OP_SUM),
+                            ("int64", yk.TYPE_INT64_T, 8, yk.OP_MAX),
+                            ("uint32", yk.TYPE_UINT32_T, 4, yk.OP_BXOR),
+                            ("c_complex", yk.TYPE_C_COMPLEX, 8, yk.OP_PROD)):
+        nel = (256 << 20) // es
+        offs = np.sort(rng.integers(0, nel - 8, 1 << 22)).astype(np.int64)
+        out[f"reduce_{base}"] = dict(
+            mk=lambda L, offs=offs, h=h: L.type_create_indexed_block_array(1 << 22, 8, offs.ctypes.data, h),
+            base=base, count=1, extent=256 << 20, op=op, keep=(offs,))
+    return out
+
+
+def suite_fill(np, rng, base, nbytes):
+    if base == "double":
+        return rng.standard_normal(nbytes // 8).view(np.uint8)
+    if base == "int64":
+        return rng.integers(-(1 << 63), (1 << 63) - 1, nbytes // 8, dtype=np.int64).view(np.uint8)
+    if base == "uint32" or base == "int32":
+        return rng.integers(0, 1 << 32, nbytes // 4, dtype=np.uint64).astype(np.uint32).view(np.uint8)
+    if base == "c_complex":
+        n = nbytes // 8
+        r = np.exp(rng.uniform(np.log(0.9), np.log(1.1), n))
+        a = rng.uniform(0, 2 * np.pi, n)
+        return (r * np.exp(1j * a)).astype(np.complex64).view(np.uint8)
+    return rng.uniform(-1, 1, nbytes // 4).astype(np.float32).view(np.uint8)
+
+
+def run_suite(out_path, steps, cpu_seconds):
+    import numpy as np
+    import torch
+    import yaksa_gb300 as yk
+    oracle_path = os.path.join(ROOT, "oracle", "_ref", "liboracle_yaksa.so")
+    if not os.path.exists(oracle_path):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    y, o = yk.Yaksa(), yk.Yaksa(oracle_path)
+    y.init()
+    o.init()
+    hbm, peak_kind = peaks()
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+    sh = ctypes.c_void_p(stream.cuda_stream)
+    shp = ctypes.addressof(sh)
+    rng = np.random.default_rng(11)
+    lines = []
+    for name, w in suite_types(y, yk, np).items():
+        tp, to = w["mk"](y), w["mk"](o)
+        size = y.size(tp)
+        count = w["count"]
+        P = size * count
+        ext = w["extent"] * (1 if count == 1 else 1)
+        typed_h = suite_fill(np, rng, w["base"], ext)
+        packed0 = suite_fill(np, rng, w["base"], P)
+        typed_d = torch.from_numpy(typed_h).cuda()
+        packed_d = torch.from_numpy(packed0).cuda()
+        op = w.get("op", yk.OP_REPLACE)
+        dirs = ["unpack"] if op != yk.OP_REPLACE else ["pack", "unpack"]
+        for d in dirs:
+            def call():
+                if d == "pack":
+                    y.pack_stream(typed_d.data_ptr(), count, tp, 0, packed_d.data_ptr(), P, shp, op=op)
+                else:
+                    y.unpack_stream(packed_d.data_ptr(), P, typed_d.data_ptr(), count, tp, 0, shp, op=op)
+            # correctness first, from fresh inputs, against the oracle on the host
+            typed_d.copy_(torch.from_numpy(typed_h))
+            packed_d.copy_(torch.from_numpy(packed0))
+            call()
+            torch.cuda.synchronize()
+            th, ph = typed_h.copy(), packed0.copy()
+            t0 = time.perf_counter()
+            if d == "pack":
+                o.pack(th.ctypes.data, count, to, 0, ph.ctypes.data, P, op=op)
+            else:
+                o.unpack(ph.ctypes.data, P, th.ctypes.data, count, to, 0, op=op)
+            cpu_t = time.perf_counter() - t0
+            exact = (np.array_equal(typed_d.cpu().numpy(), th) and np.array_equal(packed_d.cpu().numpy(), ph))
+            # timing: fresh L2 each launch, CUDA events on the launching stream
+            ts = []
+            for rep in range(max(3, steps)):
+                flush.zero_()
+                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                e0.record()
+                call()
+                e1.record()
+                e1.synchronize()
+                ts.append(e0.elapsed_time(e1) * 1e-3)
+            t = statistics.median(ts[1:])
+            alg = (2 if op == yk.OP_REPLACE else 3) * P
+            line = {"workload": name, "direction": d, "op": int(op), "packed_bytes": P,
+                    "algorithmic_bytes": alg, "time_us": t * 1e6, "packed_GBps": P / t / 1e9,
+                    "achieved_GBps": alg / t / 1e9, "hbm_frac": alg / t / 1e9 / hbm,
+                    "peak": hbm, "peak_source": peak_kind, "bit_exact": bool(exact),
+                    "cpu_oracle_s": cpu_t, "cpu_oracle_packed_GBps": P / cpu_t / 1e9,
+                    "gpu_over_cpu": cpu_t / t}
+            lines.append(line)
+            print(json.dumps(line), file=sys.stderr, flush=True)
+        y.type_free(tp)
+        o.type_free(to)
+        del typed_d, packed_d
+        torch.cuda.empty_cache()
+    if out_path:
+        with open(out_path, "w") as f:
+            for l in lines:
+                f.write(json.dumps(l) + "\n")
+    return lines
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -183,9 +329,17 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=5.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--suite", default=None,
+                    help="also run the hvector/hindexed/struct/reduction configs and write their "
+                         "JSON lines to this file")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.suite:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        run_suite(args.suite, args.steps, args.cpu_seconds)
+        return
 
     import numpy as np
     import torch

@@ -113,6 +113,30 @@ def test_benchmark_shapes(prod, oracle):
                 assert np.array_equal(got, expect)
 
 
+@pytest.mark.parametrize("nblk,zero_frac,count", [(1 << 14, 0.0, 1), (5000, 0.3, 2), (3, 0.0, 3),
+                                                  (1 << 12, 0.5, 1)])
+def test_hindexed_tile_table(prod, oracle, nblk, zero_frac, count):
+    """Lognormal block lengths (the irregular config's distribution, fewer blocks),
+    with empty blocks mixed in: every byte's address matches the oracle."""
+    rng = np.random.default_rng(nblk)
+    blens = np.clip(np.round(np.exp(np.log(16) + rng.standard_normal(nblk))), 1, 4096).astype(np.int64)
+    blens[rng.random(nblk) < zero_frac] = 0
+    if blens.sum() == 0:
+        blens[0] = 3
+    slots = rng.permutation(nblk)
+    gaps = rng.integers(0, 4, nblk)
+    starts = np.cumsum(blens[slots] + gaps) - blens[slots]
+    displs = np.empty(nblk, dtype=np.int64)
+    displs[slots] = starts * 4
+    hp = prod.type_create_hindexed(blens.tolist(), displs.tolist(), yk.TYPE_INT32_T)
+    ho = oracle.type_create_hindexed(blens.tolist(), displs.tolist(), yk.TYPE_INT32_T)
+    expect = typemap(oracle, ho, count)
+    got = locate(prod, hp, count, 0, np.arange(len(expect)))
+    assert np.array_equal(got, expect)
+    prod.type_free(hp)
+    oracle.type_free(ho)
+
+
 def desc_info(prod, h, typed):
     f = prod.lib.yaksa_gb300_debug_desc_info
     f.restype = ctypes.c_int

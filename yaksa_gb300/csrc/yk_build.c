@@ -500,6 +500,30 @@ void yk_level_set_magic(yk_level * l)
 
 /* Pack every table into one allocation: device memory, or (to_device == 0) host
  * memory for the CPU address check behind yaksa_gb300_debug_locate. */
+/* HIDX tile table: tile size 2^tshift chosen so a tile overlaps about eight blocks on
+ * average; tfb[t] = the block holding packed byte t * 2^tshift (clamped to count - 1) */
+static uint32_t hidx_tile_shift(const hlev * h)
+{
+    uint64_t total = h->pfx[h->count];
+    uint64_t want = h->count ? (total * 8) / h->count : 64;
+    uint32_t s = 6;
+    while (s < 40 && ((uint64_t) 1 << s) < want)
+        s++;
+    while (s < 40 && (total >> s) > (1u << 24))
+        s++;    /* at most 16M entries */
+    return s;
+}
+
+static uint64_t hidx_ntiles(const hlev * h, uint32_t s)
+{
+    return (h->pfx[h->count] >> s) + 2;
+}
+
+static int hidx_has_table(const hlev * h)
+{
+    return h->kind == YK_LV_HIDX && h->count > 1 && h->count < 0xffffffffull;
+}
+
 static int upload(hbuild * b, yk_devdesc * dd, int to_device)
 {
     /* table sizes */
@@ -509,6 +533,8 @@ static int upload(hbuild * b, yk_devdesc * dd, int to_device)
             bytes += b->lv[i].count * sizeof(int64_t);
         if (b->lv[i].pfx)
             bytes += (b->lv[i].count + 1) * sizeof(uint64_t);
+        if (hidx_has_table(&b->lv[i]))
+            bytes += hidx_ntiles(&b->lv[i], hidx_tile_shift(&b->lv[i])) * sizeof(uint32_t) + 8;
     }
     if (b->leaf == YK_LEAF_SEG)
         bytes += b->nseg * sizeof(int64_t) + (b->nseg + 1) * sizeof(uint64_t) + b->nseg + 16;
@@ -545,6 +571,23 @@ static int upload(hbuild * b, yk_devdesc * dd, int to_device)
             memcpy(host + pos, h->pfx, (h->count + 1) * sizeof(uint64_t));
             l->pfx = (const uint64_t *) (dev + pos);
             pos += (h->count + 1) * sizeof(uint64_t);
+        }
+        if (hidx_has_table(h)) {
+            uint32_t s = hidx_tile_shift(h);
+            uint64_t nt = hidx_ntiles(h, s);
+            uint32_t *tfb = (uint32_t *) (host + pos);
+            uint64_t j = 0;
+            for (uint64_t t = 0; t < nt; t++) {
+                uint64_t x = t << s;
+                /* largest j with pfx[j] <= x, walking forward (pfx is non-decreasing) */
+                while (j + 1 <= h->count && h->pfx[j + 1] <= x)
+                    j++;
+                tfb[t] = (uint32_t) (j < h->count ? j : h->count - 1);
+            }
+            l->tfb = (const uint32_t *) (dev + pos);
+            l->tshift = s;
+            pos += nt * sizeof(uint32_t);
+            pos = (pos + 7) & ~(size_t) 7;
         }
     }
     d->leaf = b->leaf;

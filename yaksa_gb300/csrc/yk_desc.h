@@ -69,6 +69,9 @@ typedef struct {
     uint8_t pad1[3];
     const int64_t *disp;        /* device: IDX/HIDX displacements */
     const uint64_t *pfx;        /* device: HIDX packed prefix, count + 1 entries */
+    const uint32_t *tfb;        /* device: HIDX first block of each 2^tshift-byte packed tile */
+    uint32_t tshift;
+    uint32_t pad2;
 } yk_level;
 
 typedef struct {
@@ -99,7 +102,7 @@ typedef struct {
     int32_t use64;              /* 1 = positions need 64-bit arithmetic */
     int32_t regular;            /* 0..YK_REGULAR_MAX: that many VEC levels over a RUN leaf
                                  * with 32-bit positions; -1: any other shape */
-    int32_t pad1;
+    int32_t hidx;               /* 1: one HIDX level of contiguous blocks over its run */
 } yk_launch;
 
 #define YK_REGULAR_MAX 3

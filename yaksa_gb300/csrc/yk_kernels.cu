@@ -274,6 +274,81 @@ yk_batch_regular_kernel(const __grid_constant__ yk_batch B)
     }
 }
 
+/* Contiguous-block hindexed (one HIDX level whose blocks are contiguous runs): each
+ * warp takes groups of 32 consecutive blocks; lane k holds block k's packed start and
+ * displacement in registers, the warp walks the group's packed bytes in coalesced
+ * strides of 32 units, and each unit finds its block with a 5-step shuffle search over
+ * the lanes' starts.  No shared memory, no block barriers, no per-unit index loads. */
+#define YK_HW_UNROLL 4
+
+template <int V, int DIR>
+__global__ void __launch_bounds__(YK_THREADS)
+yk_hidx_kernel(const __grid_constant__ yk_launch L)
+{
+    typedef typename yk_vec<V>::T VT;
+    const yk_level *lv = &L.desc.lv[0];
+    const uint64_t p0 = L.p0, p1 = L.p0 + L.nbytes;
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp = ((uint64_t) blockIdx.x * YK_THREADS + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t) gridDim.x * YK_THREADS) >> 5;
+    char *typed = L.typed + L.desc.base;
+    VT *packed = (VT *) L.packed;
+    /* blocks overlapping [p0, p1) (warp-uniform) */
+    const uint64_t jb = yk_hidx_block(lv, p0), je = yk_hidx_block(lv, p1 - 1);
+    const uint64_t ngroups = (je - jb + 32) / 32;
+    for (uint64_t g = warp; g < ngroups; g += nwarps) {
+        const uint64_t j0 = jb + g * 32;
+        const uint64_t jl = j0 + (uint64_t) lane;
+        const uint64_t my_pfx = jl <= je ? __ldg(lv->pfx + jl) : ~(uint64_t) 0;
+        const int64_t my_disp = jl <= je ? __ldg(lv->disp + jl) : 0;
+        const uint64_t jend = min(j0 + 32, je + 1);
+        uint64_t start = __shfl_sync(0xffffffffu, my_pfx, 0);
+        uint64_t end = __ldg(lv->pfx + jend);
+        start = max(start, p0);
+        end = min(end, p1);
+        for (uint64_t base = start; base < end; base += (uint64_t) 32 * V * YK_HW_UNROLL) {
+            int64_t off[YK_HW_UNROLL];
+            bool act[YK_HW_UNROLL];
+#pragma unroll
+            for (int k = 0; k < YK_HW_UNROLL; k++) {
+                const uint64_t p = base + (uint64_t) (k * 32 + lane) * V;
+                act[k] = p < end;
+                int idx = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    uint64_t c = __shfl_sync(0xffffffffu, my_pfx, idx + step);
+                    if (c <= p)
+                        idx += step;
+                }
+                const uint64_t bp = __shfl_sync(0xffffffffu, my_pfx, idx);
+                const int64_t bd = __shfl_sync(0xffffffffu, my_disp, idx);
+                off[k] = bd + (int64_t) (p - bp);
+            }
+            if (DIR == 0) {
+                VT v[YK_HW_UNROLL];
+#pragma unroll
+                for (int k = 0; k < YK_HW_UNROLL; k++)
+                    if (act[k])
+                        v[k] = yk_ldcg((const VT *) (typed + off[k]));
+#pragma unroll
+                for (int k = 0; k < YK_HW_UNROLL; k++)
+                    if (act[k])
+                        packed[(base + (uint64_t) (k * 32 + lane) * V - p0) / V] = v[k];
+            } else {
+                VT v[YK_HW_UNROLL];
+#pragma unroll
+                for (int k = 0; k < YK_HW_UNROLL; k++)
+                    if (act[k])
+                        v[k] = yk_ldcg((const VT *) (packed + (base + (uint64_t) (k * 32 + lane) * V - p0) / V));
+#pragma unroll
+                for (int k = 0; k < YK_HW_UNROLL; k++)
+                    if (act[k])
+                        *(VT *) (typed + off[k]) = v[k];
+            }
+        }
+    }
+}
+
 template <typename IDX, int V, int DIR, int U>
 __global__ void __launch_bounds__(YK_THREADS)
 yk_bytes_kernel(const __grid_constant__ yk_launch L)
@@ -558,7 +633,7 @@ __device__ __forceinline__ void yk_apply(int bt, int op, char *dst, const char *
     }
 }
 
-__device__ __forceinline__ int yk_bt_size(int bt)
+__host__ __device__ __forceinline__ int yk_bt_size(int bt)
 {
     switch (bt) {
         case YK_BT_BOOL: case YK_BT_CHAR: case YK_BT_I8: return 1;
@@ -599,6 +674,120 @@ yk_typed_kernel(const __grid_constant__ yk_launch L)
 /* ------------------------------------------------------------------------- */
 /* ordered unpack for overlapping targets                                    */
 /* ------------------------------------------------------------------------- */
+
+/* element types in registers, for the typed ordered-unpack kernel */
+template <int BT> struct yk_elem;
+template <> struct yk_elem<YK_BT_I8> {
+    typedef int8_t T;
+    static __device__ __forceinline__ bool op(int o, T in, T & out) { return yk_int_op<int8_t, uint8_t>(o, in, out); }
+};
+template <> struct yk_elem<YK_BT_I16> {
+    typedef int16_t T;
+    static __device__ __forceinline__ bool op(int o, T in, T & out) { return yk_int_op<int16_t, uint16_t>(o, in, out); }
+};
+template <> struct yk_elem<YK_BT_I32> {
+    typedef int32_t T;
+    static __device__ __forceinline__ bool op(int o, T in, T & out) { return yk_int_op<int32_t, uint32_t>(o, in, out); }
+};
+template <> struct yk_elem<YK_BT_I64> {
+    typedef int64_t T;
+    static __device__ __forceinline__ bool op(int o, T in, T & out) { return yk_int_op<int64_t, uint64_t>(o, in, out); }
+};
+template <> struct yk_elem<YK_BT_F32> {
+    typedef float T;
+    static __device__ __forceinline__ bool op(int o, T in, T & out) { return yk_flt_op<float>(o, in, out); }
+};
+template <> struct yk_elem<YK_BT_F64> {
+    typedef double T;
+    static __device__ __forceinline__ bool op(int o, T in, T & out) { return yk_flt_op<double>(o, in, out); }
+};
+template <> struct yk_elem<YK_BT_C32> {
+    typedef float2 T;
+    static __device__ __forceinline__ bool op(int o, T in, T & out)
+    {
+        float a[2] = { in.x, in.y }, b[2] = { out.x, out.y };
+        bool r = yk_cplx_op<float>(o, a, b);
+        out = make_float2(b[0], b[1]);
+        return r;
+    }
+};
+template <> struct yk_elem<YK_BT_C64> {
+    typedef double2 T;
+    static __device__ __forceinline__ bool op(int o, T in, T & out)
+    {
+        double a[2] = { in.x, in.y }, b[2] = { out.x, out.y };
+        bool r = yk_cplx_op<double>(o, a, b);
+        out = make_double2(b[0], b[1]);
+        return r;
+    }
+};
+
+/* Sorted blocks, typed: the same ownership rule as yk_owner_kernel below, with U
+ * elements per thread and every index and data load issued before the ordered
+ * combine, so the block-offset and target reads of neighbouring elements overlap
+ * instead of forming one dependent chain per element.  Requires elements aligned to
+ * their size on both sides (checked on the host). */
+template <typename IDX, int BT, int U>
+__global__ void __launch_bounds__(YK_THREADS)
+yk_owner_typed_kernel(const __grid_constant__ yk_launch L)
+{
+    typedef typename yk_elem<BT>::T T;
+    const yk_level & lv = L.desc.lv[0];
+    const IDX es = (IDX) sizeof(T);
+    const IDX R = (IDX) lv.cps;
+    const IDX p0 = (IDX) L.p0, p1 = (IDX) (L.p0 + L.nbytes);
+    const IDX nunits = (IDX) (L.nbytes / sizeof(T));
+    const IDX nblk = (IDX) lv.count;
+    const int op = (int) L.op;
+    const T *packed = (const T *) L.packed;
+    char *typed = L.typed + L.desc.base;
+    for (IDX t0 = (IDX) blockIdx.x * (YK_THREADS * U); t0 < nunits;
+         t0 += (IDX) gridDim.x * (YK_THREADS * U)) {
+        int64_t x[U], dnext[U];
+        IDX b[U];
+        bool own[U];
+        T in[U], out[U];
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
+            own[k] = u < nunits;
+            if (!own[k])
+                continue;
+            IDX p = p0 + u * es;
+            b[k] = yk_div(p, lv);
+            IDX j = p - b[k] * R;
+            int64_t db = __ldg(lv.disp + b[k]);
+            int64_t dprev = b[k] > 0 ? __ldg(lv.disp + b[k] - 1) : 0;
+            dnext[k] = b[k] + 1 < nblk ? __ldg(lv.disp + b[k] + 1) : INT64_MAX;
+            x[k] = db + (int64_t) j;
+            if (b[k] > 0 && x[k] < dprev + (int64_t) R && (b[k] - 1) * R + (IDX) (x[k] - dprev) >= p0)
+                own[k] = false;         /* an earlier in-range block owns this element */
+        }
+#pragma unroll
+        for (int k = 0; k < U; k++)
+            if (own[k]) {
+                out[k] = *(const T *) (typed + x[k]);
+                in[k] = packed[t0 + (IDX) (k * YK_THREADS + threadIdx.x)];
+            }
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            if (!own[k])
+                continue;
+            yk_elem<BT>::op(op, in[k], out[k]);
+            IDX bb = b[k] + 1;
+            int64_t d = dnext[k];
+            while (bb < nblk && d <= x[k]) {
+                IDX pp = bb * R + (IDX) (x[k] - d);
+                if (pp >= p1)
+                    break;
+                yk_elem<BT>::op(op, packed[(pp - p0) / es], out[k]);
+                bb++;
+                d = bb < nblk ? __ldg(lv.disp + bb) : INT64_MAX;
+            }
+            *(T *) (typed + x[k]) = out[k];
+        }
+    }
+}
 
 /* Sorted blocks: descriptor = IDX(nblk, disp sorted ascending, cps = R) over a run of
  * R bytes of one base type.  Every target element that receives data gets exactly one
@@ -810,7 +999,23 @@ extern "C" int yk_cuda_launch_pup(const yk_launch * l, void *stream)
     cudaStream_t s = (cudaStream_t) stream;
     if (l->nbytes == 0)
         return 0;
-    if (!l->typed_op) {
+    if (!l->typed_op && l->hidx) {
+        /* one warp per group of 32 blocks, 8 warps per CTA */
+        uint64_t groups = (l->desc.lv[0].count + 31) / 32;
+        uint64_t ctas = (groups + (YK_THREADS / 32) - 1) / (YK_THREADS / 32);
+        uint64_t cap = (uint64_t) yk_cuda_num_sms() * 8u;
+        unsigned g = (unsigned) (ctas < cap ? (ctas ? ctas : 1) : cap);
+#define YK_H(V) do { if (l->dir == 0) yk_hidx_kernel<V, 0><<<g, YK_THREADS, 0, s>>>(*l); \
+                     else yk_hidx_kernel<V, 1><<<g, YK_THREADS, 0, s>>>(*l); } while (0)
+        switch (l->vec) {
+            case 16: YK_H(16); break;
+            case 8: YK_H(8); break;
+            case 4: YK_H(4); break;
+            case 2: YK_H(2); break;
+            default: YK_H(1); break;
+        }
+#undef YK_H
+    } else if (!l->typed_op) {
         if (l->use64)
             launch_bytes<uint64_t>(l, s);
         else
@@ -840,7 +1045,29 @@ extern "C" int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blo
     if (l->nbytes == 0)
         return 0;
     const yk_launch & c = *l;
-    if (sorted_blocks) {
+    int bt = c.desc.leaf_type;
+    bool typed_ok = sorted_blocks == 2 && (bt == YK_BT_I8 || bt == YK_BT_I16 || bt == YK_BT_I32 ||
+                                           bt == YK_BT_I64 || bt == YK_BT_F32 || bt == YK_BT_F64 ||
+                                           bt == YK_BT_C32 || bt == YK_BT_C64);
+    if (typed_ok) {
+        uint64_t units = c.nbytes / (uint64_t) yk_bt_size(bt);
+        unsigned g = yk_grid(units, YK_THREADS * 4, 8);
+#define YK_OT(IDX) do { switch (bt) {                                                          \
+            case YK_BT_I8: yk_owner_typed_kernel<IDX, YK_BT_I8, 4><<<g, YK_THREADS, 0, s>>>(c); break;   \
+            case YK_BT_I16: yk_owner_typed_kernel<IDX, YK_BT_I16, 4><<<g, YK_THREADS, 0, s>>>(c); break; \
+            case YK_BT_I32: yk_owner_typed_kernel<IDX, YK_BT_I32, 4><<<g, YK_THREADS, 0, s>>>(c); break; \
+            case YK_BT_I64: yk_owner_typed_kernel<IDX, YK_BT_I64, 4><<<g, YK_THREADS, 0, s>>>(c); break; \
+            case YK_BT_F32: yk_owner_typed_kernel<IDX, YK_BT_F32, 4><<<g, YK_THREADS, 0, s>>>(c); break; \
+            case YK_BT_F64: yk_owner_typed_kernel<IDX, YK_BT_F64, 4><<<g, YK_THREADS, 0, s>>>(c); break; \
+            case YK_BT_C32: yk_owner_typed_kernel<IDX, YK_BT_C32, 4><<<g, YK_THREADS, 0, s>>>(c); break; \
+            default: yk_owner_typed_kernel<IDX, YK_BT_C64, 4><<<g, YK_THREADS, 0, s>>>(c); break;       \
+        } } while (0)
+        if (c.use64)
+            YK_OT(uint64_t);
+        else
+            YK_OT(uint32_t);
+#undef YK_OT
+    } else if (sorted_blocks) {
         uint64_t units = c.nbytes / (uint64_t) c.vec;
         unsigned g = yk_grid(units, YK_THREADS, 16);
         if (c.use64)

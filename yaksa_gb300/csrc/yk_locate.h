@@ -44,6 +44,34 @@ YK_HD uint64_t yk_div64(uint64_t n, const yk_level * l)
     return (t + ((n - t) >> sh1)) >> sh2;
 }
 
+/* largest j in [lo, hi) with pfx[j] <= r, given pfx[lo] <= r < pfx[hi] */
+YK_HD uint64_t yk_search_range(const uint64_t * pfx, uint64_t lo, uint64_t hi, uint64_t r)
+{
+    while (hi - lo > 1) {
+        uint64_t mid = (lo + hi) >> 1;
+        if (YK_LD(pfx + mid) <= r)
+            lo = mid;
+        else
+            hi = mid;
+    }
+    return lo;
+}
+
+/* HIDX block of packed position r: the tile table narrows the search to the blocks
+ * overlapping r's 2^tshift-byte tile (tfb[t] is the block holding tile t's first byte) */
+YK_HD uint64_t yk_hidx_block(const yk_level * l, uint64_t r)
+{
+    if (l->tfb) {
+        uint64_t t = r >> l->tshift;
+        uint64_t lo = YK_LD(l->tfb + t);
+        uint64_t hi = (uint64_t) YK_LD(l->tfb + t + 1) + 1;
+        if (hi > l->count)
+            hi = l->count;
+        return yk_search_range(l->pfx, lo, hi, r);
+    }
+    return yk_search_range(l->pfx, 0, l->count, r);
+}
+
 /* largest j in [0, n) with pfx[j] <= r, given pfx[0] <= r < pfx[n] */
 YK_HD uint64_t yk_search(const uint64_t * pfx, uint64_t n, uint64_t r)
 {
@@ -68,7 +96,7 @@ YK_HD int64_t NAME(const yk_desc * d, IDX p, int *bt, uint64_t * inseg)         
     for (int i = 0; i < d->nlev; i++) {                                                \
         const yk_level *l = &d->lv[i];                                                 \
         if (l->kind == YK_LV_HIDX) {                                                   \
-            uint64_t j = yk_search(l->pfx, l->count, (uint64_t) r);                    \
+            uint64_t j = yk_hidx_block(l, (uint64_t) r);                               \
             r -= (IDX) YK_LD(l->pfx + j);                                              \
             off += YK_LD(l->disp + j);                                                 \
             IDX q = DIV(r, l);                                                         \

@@ -419,6 +419,9 @@ static int prepare(const yk_plan * p, char *typed, char *packed, yk_launch * L, 
             if (L->desc.lv[i].kind != YK_LV_VEC)
                 L->regular = -1;
     }
+    L->hidx = L->desc.leaf == YK_LEAF_RUN && L->desc.nlev == 1 &&
+        L->desc.lv[0].kind == YK_LV_HIDX && L->desc.lv[0].tfb &&
+        L->desc.lv[0].stride == (int64_t) L->desc.lv[0].cps && L->desc.run == L->desc.lv[0].cps;
     if (ddo == dd && !typed_op) {
         /* widest unit that every run, offset, pointer and range bound allows */
         int v = ddo->vec_align;
@@ -443,6 +446,14 @@ static int prepare(const yk_plan * p, char *typed, char *packed, yk_launch * L, 
         *sorted = ddo->sorted_blocks && L->typed_op && L->desc.nlev == 1 &&
             L->desc.lv[0].kind == YK_LV_IDX &&
             ddo->elem_align >= yk_base_type_size(t->base_type);
+        if (*sorted) {
+            /* register-typed variant: both sides aligned to the element size */
+            uint64_t es = (uint64_t) yk_base_type_size(L->desc.leaf_type);
+            uint64_t a = (uint64_t) (uintptr_t) (typed + L->desc.base) | (uint64_t) (uintptr_t) packed |
+                b0 | (uint64_t) ddo->elem_align;
+            if (es && (a % es) == 0 && (uint64_t) ddo->elem_align >= es)
+                *sorted = 2;
+        }
         if (!L->typed_op && !*sorted)
             L->vec = (int) YK_MIN((uint64_t) L->vec, (uint64_t) ddo->vec_align);
     } else {
@@ -742,7 +753,7 @@ static int batch_run(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info, cudaStre
         rc = prepare(&p, p.dtyped, p.dpacked, &ls[nb], &kind, &sorted);
         if (rc)
             break;
-        if (kind == YK_X_BYTES && !ls[nb].use64)
+        if (kind == YK_X_BYTES && !ls[nb].use64 && !ls[nb].hidx)
             nb++;
         else
             rc = launch_prepared(&p, &ls[nb], kind, sorted, s);
