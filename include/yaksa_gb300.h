@@ -56,6 +56,33 @@ int yaksa_gb300_graph_create(yaksa_gb300_pup_t * ops, const int *batch_ends, int
 int yaksa_gb300_graph_launch(yaksa_gb300_graph_t graph, void *stream);
 int yaksa_gb300_graph_free(yaksa_gb300_graph_t graph);
 
+/* Request server (no counterpart in the reference, whose progress engine launches
+ * one kernel per request chunk, src/backend/src/yaksuri_progress.c:2862-3088).  A
+ * persistent kernel keeps one CTA group resident per SM and drains a work queue in
+ * pinned, device-mapped host memory; requests are split into work items of up to
+ * 512 KiB of packed bytes, so requests of any size and type share the GPU as they
+ * arrive (continuous batching).
+ *   create: ring_requests request slots (0: 4096), budget_bytes of packed bytes in
+ *           flight (0: 64 GiB);
+ *   submit: admits one request or returns YAKSA_ERR__OUT_OF_MEM when the rings or the
+ *           byte budget are full (call progress/test and retry); requests whose buffers
+ *           the GPU cannot address return YAKSA_ERR__NOT_SUPPORTED;
+ *   test/wait: completion of a ticket (wait gives up with YAKSA_ERR__INTERNAL after
+ *           20 s); progress: reclaims finished requests and keeps a kernel resident.
+ * Resident CTAs that find no work for a few milliseconds leave; the next submit or
+ * progress call relaunches them.  Requests in flight together must be independent. */
+typedef struct yaksa_gb300_server_s *yaksa_gb300_server_t;
+int yaksa_gb300_server_create(uint32_t ring_requests, uint64_t budget_bytes,
+                              yaksa_gb300_server_t * server);
+int yaksa_gb300_server_submit(yaksa_gb300_server_t server, yaksa_gb300_pup_t * op,
+                              yaksa_info_t info, uint64_t * ticket);
+int yaksa_gb300_server_test(yaksa_gb300_server_t server, uint64_t ticket, int *done);
+int yaksa_gb300_server_wait(yaksa_gb300_server_t server, uint64_t ticket);
+int yaksa_gb300_server_progress(yaksa_gb300_server_t server);
+int yaksa_gb300_server_stats(yaksa_gb300_server_t server, uint64_t * requests, uint64_t * items,
+                             uint64_t * relaunches, uint32_t * idle_exits);
+int yaksa_gb300_server_destroy(yaksa_gb300_server_t server);
+
 /* Runtime counters since load: kernel launches, calls served in place (device or
  * GPU-addressable host memory), calls that staged host data through device memory,
  * and contiguous calls served by one copy. */

@@ -41,6 +41,8 @@ class Pair:
 def dev_copy(torch, arr):
     t = torch.empty(arr.nbytes, dtype=torch.uint8, device="cuda")
     t.copy_(torch.from_numpy(arr))
+    # the engine runs on its own streams: make the copy complete device-wide
+    torch.cuda.synchronize()
     return t
 
 

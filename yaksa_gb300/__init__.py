@@ -141,7 +141,62 @@ def load_library(path):
         lib.yaksa_gb300_graph_launch.argtypes = [_vp, _vp]
         lib.yaksa_gb300_graph_free.restype = ctypes.c_int
         lib.yaksa_gb300_graph_free.argtypes = [_vp]
+        for name, args in (("yaksa_gb300_server_create", [ctypes.c_uint32, _u64, ctypes.POINTER(_vp)]),
+                           ("yaksa_gb300_server_submit", [_vp, ctypes.POINTER(PupOp), _vp,
+                                                          ctypes.POINTER(_u64)]),
+                           ("yaksa_gb300_server_test", [_vp, _u64, ctypes.POINTER(ctypes.c_int)]),
+                           ("yaksa_gb300_server_wait", [_vp, _u64]),
+                           ("yaksa_gb300_server_progress", [_vp]),
+                           ("yaksa_gb300_server_stats", [_vp, ctypes.POINTER(_u64), ctypes.POINTER(_u64),
+                                                         ctypes.POINTER(_u64),
+                                                         ctypes.POINTER(ctypes.c_uint32)]),
+                           ("yaksa_gb300_server_destroy", [_vp])):
+            f = getattr(lib, name)
+            f.restype = ctypes.c_int
+            f.argtypes = args
     return lib
+
+
+class Server:
+    """Persistent-kernel request server (yaksa_gb300_server_*)."""
+
+    def __init__(self, y, ring_requests=4096, budget_bytes=0):
+        self.y = y
+        self.h = _vp()
+        y._chk("yaksa_gb300_server_create",
+               y.lib.yaksa_gb300_server_create(ring_requests, budget_bytes, ctypes.byref(self.h)))
+
+    def submit(self, op, info=None):
+        """Returns a ticket, or None when admission is refused (retry after progress)."""
+        t = _u64()
+        rc = self.y.lib.yaksa_gb300_server_submit(self.h, ctypes.byref(op), info, ctypes.byref(t))
+        if rc == ERR_OUT_OF_MEM:
+            return None
+        self.y._chk("yaksa_gb300_server_submit", rc)
+        return t.value
+
+    def test(self, ticket):
+        d = ctypes.c_int()
+        self.y._chk("yaksa_gb300_server_test", self.y.lib.yaksa_gb300_server_test(self.h, ticket,
+                                                                                  ctypes.byref(d)))
+        return bool(d.value)
+
+    def wait(self, ticket):
+        self.y._chk("yaksa_gb300_server_wait", self.y.lib.yaksa_gb300_server_wait(self.h, ticket))
+
+    def progress(self):
+        self.y._chk("yaksa_gb300_server_progress", self.y.lib.yaksa_gb300_server_progress(self.h))
+
+    def stats(self):
+        a, b, c, d = _u64(), _u64(), _u64(), ctypes.c_uint32()
+        self.y.lib.yaksa_gb300_server_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
+                                            ctypes.byref(d))
+        return dict(requests=a.value, items=b.value, relaunches=c.value, idle_exits=d.value)
+
+    def destroy(self):
+        if self.h:
+            self.y._chk("yaksa_gb300_server_destroy", self.y.lib.yaksa_gb300_server_destroy(self.h))
+            self.h = None
 
 
 def _arr(ctype, seq):

@@ -613,7 +613,18 @@ static int upload(hbuild * b, yk_devdesc * dd, int to_device)
         pos += b->nseg;
     }
     if (bytes && to_device) {
-        cudaError_t e = cudaMemcpy(dev, host, pos, cudaMemcpyHostToDevice);
+        /* A synchronous cudaMemcpy from pageable memory may return before the DMA
+         * lands; a kernel already resident (the request server) would then read the
+         * tables early.  Copy on a private stream and wait for that stream. */
+        cudaStream_t us;
+        cudaError_t e = cudaStreamCreateWithFlags(&us, cudaStreamNonBlocking);
+        if (e == cudaSuccess) {
+            e = cudaMemcpyAsync(dev, host, pos, cudaMemcpyHostToDevice, us);
+            cudaError_t e2 = cudaStreamSynchronize(us);
+            if (e == cudaSuccess)
+                e = e2;
+            cudaStreamDestroy(us);
+        }
         free(host);
         if (e != cudaSuccess) {
             cudaFree(dev);

@@ -122,6 +122,34 @@ int yk_cuda_batch_units_per_thread(uint64_t total_units);
 uint64_t yk_cuda_tiles(uint64_t units, int units_per_thread);
 int yk_cuda_launch_batch(const yk_batch * b, int units_per_thread, int regular, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Persistent request server: a device-visible work queue drained by resident CTAs.
+ * ------------------------------------------------------------------------- */
+enum { YK_SRV_REGULAR = 0, YK_SRV_BYTES, YK_SRV_TYPED, YK_SRV_OWNER, YK_SRV_ORDERED, YK_SRV_HIDX };
+
+typedef struct {
+    uint64_t seq;               /* item sequence number (the GPU checks it) */
+    uint32_t req;               /* request record slot */
+    uint32_t kind;              /* YK_SRV_* */
+    uint64_t pb, pe;            /* packed byte range of this item */
+} yk_item;
+
+typedef struct {
+    yk_launch *reqs;            /* request records (host-mapped, written by the host) */
+    yk_item *items;             /* work items (host-mapped, written by the host) */
+    volatile uint64_t *item_done;       /* item sequence + 1 once done (written by the GPU) */
+    const volatile uint64_t *items_published;   /* items visible to the GPU (host) */
+    const volatile int *stop;   /* host asks resident CTAs to leave */
+    unsigned long long *next_item;      /* device memory: next item to claim */
+    volatile uint32_t *status;  /* [0] idle exits, [1] stop exits, [2] rejected items */
+    uint32_t qi, qr;            /* ring sizes */
+    uint32_t max_idle_spins;    /* bounded wait for new items */
+    uint32_t pad;
+} yk_server_args;
+
+int yk_cuda_server_launch(const yk_server_args * a, int ctas, void *stream);
+int yk_cuda_server_ctas(void);
+
 /* Granlund-Montgomery constants for dividing by l->cps (host side). */
 void yk_level_set_magic(yk_level * l);
 

@@ -883,6 +883,352 @@ __global__ void yk_ordered_warp_kernel(const __grid_constant__ yk_launch L)
 }
 
 /* ------------------------------------------------------------------------- */
+/* persistent request server                                                 */
+/* ------------------------------------------------------------------------- */
+
+/* Each function processes the units [ub, ue) of one request with the CTA's threads. */
+template <int V, int DIR>
+__device__ __forceinline__ void yk_srv_regular(const yk_launch & L, uint64_t ub, uint64_t ue)
+{
+    for (uint32_t t0 = (uint32_t) ub; t0 < (uint32_t) ue; t0 += YK_THREADS)
+        yk_regular_dispatch<V, DIR, 1>(L, t0, (uint32_t) ue);
+}
+
+template <int V, int DIR>
+__device__ __forceinline__ void yk_srv_bytes(const yk_launch & L, uint64_t ub, uint64_t ue)
+{
+    for (uint64_t t0 = ub; t0 < ue; t0 += YK_THREADS)
+        yk_bytes_tile<uint64_t, V, DIR, 1>(L, t0, ue);
+}
+
+__device__ void yk_srv_typed(const yk_launch & L, uint64_t ub, uint64_t ue)
+{
+    const uint64_t g = (uint64_t) L.vec;
+    const int op = (int) L.op;
+    for (uint64_t u = ub + threadIdx.x; u < ue; u += YK_THREADS) {
+        int bt;
+        uint64_t inseg;
+        int64_t off = yk_locate<uint64_t>(L.desc, L.p0 + u * g, &bt, &inseg);
+        if (inseg % (uint64_t) yk_bt_size(bt))
+            continue;
+        char *t = L.typed + off;
+        char *p = L.packed + u * g;
+        if (L.dir == 0)
+            yk_apply(bt, op, p, t);
+        else
+            yk_apply(bt, op, t, p);
+    }
+}
+
+__device__ void yk_srv_owner(const yk_launch & L, uint64_t ub, uint64_t ue)
+{
+    const yk_level & lv = L.desc.lv[0];
+    const int bt = L.desc.leaf_type;
+    const uint64_t es = (uint64_t) yk_bt_size(bt), R = lv.cps;
+    const uint64_t p0 = L.p0, p1 = L.p0 + L.nbytes;
+    const int op = (int) L.op;
+    for (uint64_t u = ub + threadIdx.x; u < ue; u += YK_THREADS) {
+        uint64_t p = p0 + u * es;
+        uint64_t b = yk_div(p, lv);
+        uint64_t j = p - b * R;
+        int64_t x = __ldg(lv.disp + b) + (int64_t) j;
+        if (b > 0) {
+            int64_t dprev = __ldg(lv.disp + b - 1);
+            if (x < dprev + (int64_t) R && (b - 1) * R + (uint64_t) (x - dprev) >= p0)
+                continue;
+        }
+        char *t = L.typed + L.desc.base + x;
+        for (uint64_t bb = b; bb < lv.count; bb++) {
+            int64_t db = __ldg(lv.disp + bb);
+            if (db > x)
+                break;
+            uint64_t pp = bb * R + (uint64_t) (x - db);
+            if (pp >= p1)
+                break;
+            yk_apply(bt, op, t, L.packed + (pp - p0));
+        }
+    }
+}
+
+/* the whole request, in order, by warp 0 (targets that overlap arbitrarily) */
+__device__ void yk_srv_ordered(const yk_launch & L, uint64_t ub, uint64_t ue)
+{
+    if (threadIdx.x >= 32)
+        return;
+    const int lane = threadIdx.x;
+    const uint64_t g = (uint64_t) L.vec;
+    for (uint64_t c0 = ub; c0 < ue; c0 += 32) {
+        uint64_t u = c0 + (uint64_t) lane;
+        bool active = u < ue;
+        int bt = YK_BT_NONE;
+        uint64_t inseg = 0;
+        int64_t off = 0;
+        int len = 0;
+        if (active) {
+            off = yk_locate<uint64_t>(L.desc, L.p0 + u * g, &bt, &inseg);
+            if (L.typed_op) {
+                int es = yk_bt_size(bt);
+                if (inseg % (uint64_t) es)
+                    active = false;
+                else
+                    len = es;
+            } else {
+                len = (int) g;
+            }
+        }
+        bool conflict = false;
+        for (int k = 0; k < 31; k++) {
+            int64_t ooff = __shfl_sync(0xffffffffu, off, k);
+            int olen = __shfl_sync(0xffffffffu, active ? len : 0, k);
+            if (k < lane && active && olen && off < ooff + olen && ooff < off + len)
+                conflict = true;
+        }
+        bool serial = __any_sync(0xffffffffu, conflict);
+        for (int k = 0; k < 32; k++) {
+            if ((!serial || k == lane) && active) {
+                char *t = L.typed + off;
+                char *p = L.packed + u * g;
+                if (L.typed_op)
+                    yk_apply(bt, (int) L.op, t, p);
+                else
+                    for (int i = 0; i < len; i++)
+                        t[i] = p[i];
+            }
+            __syncwarp();
+            if (!serial)
+                break;
+        }
+    }
+}
+
+/* contiguous-block hindexed over the packed range [pb, pe): the CTA's warps split the
+ * overlapping block groups (see yk_hidx_kernel) */
+template <int V, int DIR>
+__device__ void yk_srv_hidx(const yk_launch & L, uint64_t pb, uint64_t pe)
+{
+    typedef typename yk_vec<V>::T VT;
+    const yk_level *lv = &L.desc.lv[0];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    char *typed = L.typed + L.desc.base;
+    VT *packed = (VT *) L.packed;
+    const uint64_t jb = yk_hidx_block(lv, pb), je = yk_hidx_block(lv, pe - 1);
+    const uint64_t ngroups = (je - jb + 32) / 32;
+    for (uint64_t gi = (uint64_t) w; gi < ngroups; gi += YK_THREADS / 32) {
+        const uint64_t j0 = jb + gi * 32, jl = j0 + (uint64_t) lane;
+        const uint64_t my_pfx = jl <= je ? __ldg(lv->pfx + jl) : ~(uint64_t) 0;
+        const int64_t my_disp = jl <= je ? __ldg(lv->disp + jl) : 0;
+        uint64_t start = max(__shfl_sync(0xffffffffu, my_pfx, 0), pb);
+        uint64_t end = min(__ldg(lv->pfx + min(j0 + 32, je + 1)), pe);
+        for (uint64_t base = start; base < end; base += (uint64_t) 32 * V) {
+            const uint64_t p = base + (uint64_t) lane * V;
+            int idx = 0;
+#pragma unroll
+            for (int step = 16; step > 0; step >>= 1) {
+                uint64_t c = __shfl_sync(0xffffffffu, my_pfx, idx + step);
+                if (c <= p)
+                    idx += step;
+            }
+            const uint64_t bp = __shfl_sync(0xffffffffu, my_pfx, idx);
+            const int64_t bd = __shfl_sync(0xffffffffu, my_disp, idx);
+            if (p < end) {
+                char *t = typed + bd + (int64_t) (p - bp);
+                VT *q = packed + (p - L.p0) / V;
+                if (DIR == 0)
+                    *q = yk_ldcg((const VT *) t);
+                else
+                    *(VT *) t = yk_ldcg((const VT *) q);
+            }
+        }
+    }
+}
+
+__device__ __forceinline__ uint64_t yk_ld_acquire_sys(const volatile uint64_t * p)
+{
+    uint64_t v;
+    asm volatile ("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+/* host-written queue data is read at system scope: never from a stale cached copy */
+__device__ __forceinline__ uint64_t yk_ld_sys(const void *p)
+{
+    uint64_t v;
+    asm volatile ("ld.relaxed.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+/* a record the GPU can act on: a known kind, a sane unit and an ordered range */
+__device__ __forceinline__ bool yk_item_ok(const yk_item & it, const yk_launch & L)
+{
+    if (it.kind > YK_SRV_HIDX || it.pe <= it.pb || it.pb < L.p0 || it.pe > L.p0 + L.nbytes)
+        return false;
+    if (L.vec != 1 && L.vec != 2 && L.vec != 4 && L.vec != 8 && L.vec != 16)
+        return false;
+    return L.dir == 0 || L.dir == 1;
+}
+
+/* Resident CTAs claim work items one at a time (a compare-and-swap that never runs past
+ * the published count), stage the item's request record in shared memory, process the
+ * item, and publish its completion.  Every wait is bounded: a CTA that finds no new
+ * item for max_idle_spins polls, or sees the stop flag, leaves; the host relaunches the
+ * kernel when items are pending and no CTA is resident. */
+__global__ void __launch_bounds__(YK_THREADS)
+yk_server_kernel(const __grid_constant__ yk_server_args A)
+{
+    __shared__ yk_launch sL;
+    __shared__ uint64_t s_item;
+    __shared__ int s_cmd;
+    __shared__ yk_item s_it;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            int cmd = 0;
+            for (uint32_t spins = 0;; spins++) {
+                if (*A.stop) {
+                    cmd = 2;
+                    break;
+                }
+                uint64_t pub = yk_ld_acquire_sys(A.items_published);
+                unsigned long long nxt = *(volatile unsigned long long *) A.next_item;
+                if (nxt < pub) {
+                    if (atomicCAS(A.next_item, nxt, nxt + 1) == nxt) {
+                        s_item = nxt;
+                        cmd = 1;
+                        break;
+                    }
+                    if (spins >= 64u * A.max_idle_spins) {
+                        cmd = 3;        /* hard bound: leave; the host relaunches */
+                        break;
+                    }
+                    continue;
+                }
+                if (spins >= A.max_idle_spins) {
+                    cmd = 3;
+                    break;
+                }
+                __nanosleep(200);
+            }
+            if (cmd == 1) {
+                /* the item carries its own sequence number: re-read (bounded) until the
+                 * host's write is the one seen */
+                const yk_item *src = &A.items[s_item % A.qi];
+                uint64_t w[4];
+                uint32_t tries = 0;
+                do {
+                    for (int i = 0; i < 4; i++)
+                        w[i] = yk_ld_sys((const uint64_t *) src + i);
+                } while (w[0] != s_item && ++tries < 1000);
+                if (w[0] != s_item)
+                    cmd = 4;
+                uint64_t *dst = (uint64_t *) &s_it;
+                for (int i = 0; i < 4; i++)
+                    dst[i] = w[i];
+            }
+            s_cmd = cmd;
+        }
+        __syncthreads();
+        int cmd = s_cmd;
+        if (cmd == 2 || cmd == 3) {
+            if (threadIdx.x == 0)
+                atomicAdd((unsigned int *) &A.status[cmd == 2 ? 1 : 0], 1u);
+            return;
+        }
+        if (cmd == 1) {
+            /* request record -> shared memory (8-byte words, system-scope loads) */
+            const uint64_t *src = (const uint64_t *) (A.reqs + (s_it.req % A.qr));
+            uint64_t *dst = (uint64_t *) &sL;
+            for (uint32_t i = threadIdx.x; i < sizeof(yk_launch) / 8; i += YK_THREADS)
+                dst[i] = yk_ld_sys(src + i);
+        }
+        __syncthreads();
+        if (threadIdx.x == 0 && cmd == 1 && !yk_item_ok(s_it, sL))
+            s_cmd = 4;
+        __syncthreads();
+        cmd = s_cmd;
+        if (cmd == 4) {
+            /* unusable item: count it, mark it done, move on (never loop on it) */
+            if (threadIdx.x == 0) {
+                atomicAdd((unsigned int *) &A.status[2], 1u);
+                __threadfence_system();
+                A.item_done[s_item % A.qi] = s_item + 1;
+            }
+            __syncthreads();
+            continue;
+        }
+        const yk_item it = s_it;
+        const uint64_t g = (uint64_t) sL.vec;
+        const uint64_t ub = (it.pb - sL.p0) / g, ue = (it.pe - sL.p0) / g;
+        switch (it.kind) {
+            case YK_SRV_REGULAR:
+#define YK_SV(V) do { if (sL.dir == 0) yk_srv_regular<V, 0>(sL, ub, ue); \
+                      else yk_srv_regular<V, 1>(sL, ub, ue); } while (0)
+                switch (sL.vec) {
+                    case 16: YK_SV(16); break;
+                    case 8: YK_SV(8); break;
+                    case 4: YK_SV(4); break;
+                    case 2: YK_SV(2); break;
+                    default: YK_SV(1); break;
+                }
+#undef YK_SV
+                break;
+            case YK_SRV_BYTES:
+#define YK_SB(V) do { if (sL.dir == 0) yk_srv_bytes<V, 0>(sL, ub, ue); \
+                      else yk_srv_bytes<V, 1>(sL, ub, ue); } while (0)
+                switch (sL.vec) {
+                    case 16: YK_SB(16); break;
+                    case 8: YK_SB(8); break;
+                    case 4: YK_SB(4); break;
+                    case 2: YK_SB(2); break;
+                    default: YK_SB(1); break;
+                }
+#undef YK_SB
+                break;
+            case YK_SRV_TYPED:
+                yk_srv_typed(sL, ub, ue);
+                break;
+            case YK_SRV_OWNER:
+                yk_srv_owner(sL, (it.pb - sL.p0) / (uint64_t) yk_bt_size(sL.desc.leaf_type),
+                             (it.pe - sL.p0) / (uint64_t) yk_bt_size(sL.desc.leaf_type));
+                break;
+            case YK_SRV_ORDERED:
+                yk_srv_ordered(sL, ub, ue);
+                break;
+            default:
+#define YK_SH(V) do { if (sL.dir == 0) yk_srv_hidx<V, 0>(sL, it.pb, it.pe); \
+                      else yk_srv_hidx<V, 1>(sL, it.pb, it.pe); } while (0)
+                switch (sL.vec) {
+                    case 16: YK_SH(16); break;
+                    case 8: YK_SH(8); break;
+                    case 4: YK_SH(4); break;
+                    case 2: YK_SH(2); break;
+                    default: YK_SH(1); break;
+                }
+#undef YK_SH
+                break;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence_system();
+            A.item_done[s_item % A.qi] = s_item + 1;
+        }
+    }
+}
+
+extern "C" int yk_cuda_server_ctas(void)
+{
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, yk_server_kernel, YK_THREADS, 0);
+    if (per_sm < 1)
+        per_sm = 1;
+    return per_sm * yk_cuda_num_sms();
+}
+
+extern "C" int yk_cuda_server_launch(const yk_server_args * a, int ctas, void *stream)
+{
+    yk_server_kernel<<<ctas, YK_THREADS, 0, (cudaStream_t) stream>>>(*a);
+    return (int) cudaGetLastError();
+}
+
+/* ------------------------------------------------------------------------- */
 /* host-side launchers                                                       */
 /* ------------------------------------------------------------------------- */
 

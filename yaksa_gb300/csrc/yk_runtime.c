@@ -24,6 +24,7 @@
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 #include <cuda_runtime_api.h>
 #include "yk_internal.h"
 #include "yaksa_gb300.h"
@@ -795,6 +796,317 @@ int yaksa_gb300_ipup_batch(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info,
     if (rc)
         return rc;
     return complete(NULL, YK_MODE_NONBLOCKING, R.stream, request);
+}
+
+/* ------------------------------------------------------------------------- */
+/* persistent request server                                                 */
+/* ------------------------------------------------------------------------- */
+
+#define YK_ITEM_BYTES (512u << 10)
+
+typedef struct {
+    uint64_t seq;               /* request sequence number (ticket) */
+    uint64_t item0, nitems;
+    uint64_t bytes;
+    yk_type *t;
+    int busy;
+} yk_srv_slot;
+
+struct yaksa_gb300_server_s {
+    pthread_mutex_t mu;
+    int ctas, running;
+    cudaStream_t stream;
+    uint32_t qr, qi;
+    yk_launch *reqs;            /* pinned, mapped */
+    yk_item *items;             /* pinned, mapped */
+    uint64_t *item_done;        /* pinned, mapped */
+    uint64_t *ctl;              /* pinned, mapped: [0] items published, [1] stop, [2] status */
+    unsigned long long *next_item;      /* device */
+    yk_srv_slot *slots;
+    uint64_t req_seq, item_seq, oldest_req;
+    uint64_t inflight_bytes, budget;
+    uint64_t relaunches;
+    yk_server_args args;
+};
+
+static void *pinned(size_t n)
+{
+    void *p = NULL;
+    if (cudaHostAlloc(&p, n, cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess)
+        return NULL;
+    memset(p, 0, n);
+    return p;
+}
+
+int yaksa_gb300_server_create(uint32_t ring_requests, uint64_t budget_bytes,
+                              yaksa_gb300_server_t * server)
+{
+    *server = NULL;
+    int rc = runtime_ready();
+    if (rc)
+        return rc;
+    struct yaksa_gb300_server_s *S = calloc(1, sizeof(*S));
+    if (!S)
+        return YAKSA_ERR__OUT_OF_MEM;
+    pthread_mutex_init(&S->mu, NULL);
+    S->qr = ring_requests ? ring_requests : 4096;
+    S->qi = 16 * S->qr;
+    S->budget = budget_bytes ? budget_bytes : (64ull << 30);
+    S->reqs = pinned(sizeof(yk_launch) * S->qr);
+    S->items = pinned(sizeof(yk_item) * S->qi);
+    S->item_done = pinned(sizeof(uint64_t) * S->qi);
+    S->ctl = pinned(64);
+    S->slots = calloc(S->qr, sizeof(yk_srv_slot));
+    if (!S->reqs || !S->items || !S->item_done || !S->ctl || !S->slots ||
+        cudaMalloc((void **) &S->next_item, sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMemset(S->next_item, 0, sizeof(unsigned long long)) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        yaksa_gb300_server_destroy(S);
+        return YAKSA_ERR__OUT_OF_MEM;
+    }
+    cudaDeviceSynchronize();
+    S->ctas = yk_cuda_server_ctas();
+    S->args.reqs = S->reqs;
+    S->args.items = S->items;
+    S->args.item_done = S->item_done;
+    S->args.items_published = &S->ctl[0];
+    S->args.stop = (const volatile int *) &S->ctl[1];
+    S->args.next_item = S->next_item;
+    S->args.status = (volatile uint32_t *) &S->ctl[2];
+    S->args.qi = S->qi;
+    S->args.qr = S->qr;
+    S->args.max_idle_spins = 20000;     /* a few milliseconds without work */
+    *server = S;
+    return YAKSA_SUCCESS;
+}
+
+/* reclaim finished requests (oldest first) and keep a kernel resident while items are
+ * pending; caller holds S->mu */
+static int server_progress_locked(struct yaksa_gb300_server_s *S)
+{
+    while (S->oldest_req < S->req_seq) {
+        yk_srv_slot *sl = &S->slots[S->oldest_req % S->qr];
+        if (sl->busy) {
+            int done = 1;
+            for (uint64_t i = sl->item0; i < sl->item0 + sl->nitems; i++)
+                if (__atomic_load_n(&S->item_done[i % S->qi], __ATOMIC_ACQUIRE) != i + 1) {
+                    done = 0;
+                    break;
+                }
+            if (!done)
+                break;
+            sl->busy = 0;
+            S->inflight_bytes -= sl->bytes;
+            if (sl->t)
+                yk_type_unref(sl->t);
+            sl->t = NULL;
+        }
+        S->oldest_req++;
+    }
+    if (S->running && cudaStreamQuery(S->stream) != cudaErrorNotReady) {
+        S->running = 0;
+        cudaGetLastError();
+    }
+    uint64_t claimed_upto = S->item_seq;
+    int pending = S->oldest_req < S->req_seq;
+    if (pending && !S->running && claimed_upto) {
+        int e = yk_cuda_server_launch(&S->args, S->ctas, S->stream);
+        if (e)
+            return cuda_err((cudaError_t) e, "server launch");
+        S->running = 1;
+        S->relaunches++;
+    }
+    return YAKSA_SUCCESS;
+}
+
+int yaksa_gb300_server_progress(yaksa_gb300_server_t S)
+{
+    pthread_mutex_lock(&S->mu);
+    int rc = server_progress_locked(S);
+    pthread_mutex_unlock(&S->mu);
+    return rc;
+}
+
+int yaksa_gb300_server_submit(yaksa_gb300_server_t S, yaksa_gb300_pup_t * o, yaksa_info_t info,
+                              uint64_t * ticket)
+{
+    o->actual = 0;
+    yk_type *t = yk_type_get(o->type);
+    if (!t)
+        return YAKSA_ERR__INTERNAL;
+    yk_plan p;
+    int rc = o->kind == 0 ?
+        plan(0, NULL, o->outbuf, (char *) o->inbuf, o->count, t, o->offset, o->maxbytes, info,
+             o->op, &p) :
+        plan(1, o->inbuf, NULL, (char *) o->outbuf, o->count, t, o->offset, o->maxbytes, info,
+             o->op, &p);
+    if (rc)
+        return rc;
+    if (p.staged)
+        return YAKSA_ERR__NOT_SUPPORTED;        /* the GPU cannot address a buffer */
+    yk_launch L;
+    int kind = YK_X_BYTES, sorted = 0;
+    if (p.b1 > p.b0) {
+        rc = prepare(&p, p.dtyped, p.dpacked, &L, &kind, &sorted);
+        if (rc)
+            return rc;
+    } else {
+        memset(&L, 0, sizeof(L));
+    }
+    uint32_t skind;
+    uint64_t gran;
+    if (kind == YK_X_MEMCPY) {
+        /* contiguous: an empty level chain over one run starting at true_lb */
+        memset(&L.desc, 0, sizeof(L.desc));
+        L.desc.leaf = YK_LEAF_RUN;
+        L.desc.run = ~(uint64_t) 0;
+        L.desc.base = t->true_lb;
+        L.regular = 0;
+        int v = pow2_of((uint64_t) (uintptr_t) p.dtyped + (uint64_t) t->true_lb);
+        v = YK_MIN(v, pow2_of((uint64_t) (uintptr_t) p.dpacked));
+        v = YK_MIN(v, pow2_of(p.b0));
+        v = YK_MIN(v, pow2_of(p.b1 - p.b0));
+        L.vec = v;
+        L.use64 = p.b1 > 0xffffffffull;
+        skind = L.use64 ? YK_SRV_BYTES : YK_SRV_REGULAR;
+        gran = (uint64_t) v;
+    } else if (kind == YK_X_BYTES) {
+        skind = L.hidx ? YK_SRV_HIDX : L.regular >= 0 ? YK_SRV_REGULAR : YK_SRV_BYTES;
+        gran = (uint64_t) L.vec;
+    } else if (kind == YK_X_TYPED) {
+        skind = YK_SRV_TYPED;
+        gran = (uint64_t) L.vec;
+    } else {
+        skind = sorted ? YK_SRV_OWNER : YK_SRV_ORDERED;
+        gran = sorted ? (uint64_t) yk_base_type_size(L.desc.leaf_type) : (uint64_t) L.vec;
+    }
+    uint64_t n = p.b1 - p.b0;
+    uint64_t chunk = skind == YK_SRV_ORDERED ? (n ? n : 1) : (YK_ITEM_BYTES / gran) * gran;
+    uint64_t nitems = n ? (n + chunk - 1) / chunk : 0;
+    if (nitems > S->qi)
+        return YAKSA_ERR__NOT_SUPPORTED;        /* larger than the whole item ring */
+
+    pthread_mutex_lock(&S->mu);
+    server_progress_locked(S);
+    uint64_t oldest_item = S->oldest_req < S->req_seq ?
+        S->slots[S->oldest_req % S->qr].item0 : S->item_seq;
+    if (S->req_seq - S->oldest_req >= S->qr || S->item_seq + nitems - oldest_item > S->qi ||
+        (S->inflight_bytes && S->inflight_bytes + n > S->budget)) {
+        pthread_mutex_unlock(&S->mu);
+        return YAKSA_ERR__OUT_OF_MEM;   /* admission refused: retry after progress */
+    }
+    uint64_t seq = S->req_seq++;
+    uint32_t slot = (uint32_t) (seq % S->qr);
+    yk_srv_slot *sl = &S->slots[slot];
+    sl->seq = seq;
+    sl->item0 = S->item_seq;
+    sl->nitems = nitems;
+    sl->bytes = n;
+    sl->busy = 1;
+    sl->t = t;
+    yk_type_ref(t);
+    S->inflight_bytes += n;
+    if (nitems) {
+        memcpy(&S->reqs[slot], &L, sizeof(L));
+        for (uint64_t i = 0; i < nitems; i++) {
+            yk_item *it = &S->items[(S->item_seq + i) % S->qi];
+            it->seq = S->item_seq + i;
+            it->req = slot;
+            it->kind = skind;
+            it->pb = p.b0 + i * chunk;
+            it->pe = YK_MIN(p.b1, p.b0 + (i + 1) * chunk);
+        }
+        S->item_seq += nitems;
+        /* publish: every record store above happens-before this release store */
+        __atomic_store_n(&S->ctl[0], S->item_seq, __ATOMIC_RELEASE);
+    }
+    o->actual = n;
+    rc = server_progress_locked(S);
+    pthread_mutex_unlock(&S->mu);
+    *ticket = seq;
+    return rc;
+}
+
+int yaksa_gb300_server_test(yaksa_gb300_server_t S, uint64_t ticket, int *done)
+{
+    pthread_mutex_lock(&S->mu);
+    int rc = server_progress_locked(S);
+    *done = ticket < S->oldest_req ||
+        (ticket < S->req_seq && !S->slots[ticket % S->qr].busy);
+    pthread_mutex_unlock(&S->mu);
+    return rc;
+}
+
+int yaksa_gb300_server_wait(yaksa_gb300_server_t S, uint64_t ticket)
+{
+    /* bounded: 20 s without completion is reported as an error */
+    struct timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    for (;;) {
+        int done, rc = yaksa_gb300_server_test(S, ticket, &done);
+        if (rc || done)
+            return rc;
+        clock_gettime(CLOCK_MONOTONIC, &t1);
+        if (t1.tv_sec - t0.tv_sec > 20)
+            return YAKSA_ERR__INTERNAL;
+    }
+}
+
+int yaksa_gb300_server_stats(yaksa_gb300_server_t S, uint64_t * requests, uint64_t * items,
+                             uint64_t * relaunches, uint32_t * idle_exits)
+{
+    pthread_mutex_lock(&S->mu);
+    *requests = S->req_seq;
+    *items = S->item_seq;
+    *relaunches = S->relaunches;
+    *idle_exits = ((volatile uint32_t *) &S->ctl[2])[0];
+    uint32_t rejected = ((volatile uint32_t *) &S->ctl[2])[2];
+    if (rejected)
+        fprintf(stderr, "yaksa-gb300: server rejected %u work items\n", rejected);
+    pthread_mutex_unlock(&S->mu);
+    return YAKSA_SUCCESS;
+}
+
+int yaksa_gb300_server_destroy(yaksa_gb300_server_t S)
+{
+    if (!S)
+        return YAKSA_SUCCESS;
+    int rc = YAKSA_SUCCESS;
+    if (S->ctl)
+        __atomic_store_n((int *) &S->ctl[1], 1, __ATOMIC_RELEASE);
+    if (S->stream) {
+        /* resident CTAs leave at their next poll; bounded wait */
+        struct timespec t0, t1;
+        clock_gettime(CLOCK_MONOTONIC, &t0);
+        while (cudaStreamQuery(S->stream) == cudaErrorNotReady) {
+            clock_gettime(CLOCK_MONOTONIC, &t1);
+            if (t1.tv_sec - t0.tv_sec > 30) {
+                rc = YAKSA_ERR__INTERNAL;
+                break;
+            }
+        }
+        if (!rc)
+            cudaStreamDestroy(S->stream);
+    }
+    for (uint32_t i = 0; S->slots && i < S->qr; i++)
+        if (S->slots[i].t)
+            yk_type_unref(S->slots[i].t);
+    if (!rc) {
+        if (S->next_item)
+            cudaFree(S->next_item);
+        if (S->reqs)
+            cudaFreeHost(S->reqs);
+        if (S->items)
+            cudaFreeHost(S->items);
+        if (S->item_done)
+            cudaFreeHost(S->item_done);
+        if (S->ctl)
+            cudaFreeHost(S->ctl);
+    }
+    free(S->slots);
+    pthread_mutex_destroy(&S->mu);
+    free(S);
+    return rc;
 }
 
 /* ------------------------------------------------------------------------- */
