@@ -321,6 +321,254 @@ def run_suite(out_path, steps, cpu_seconds):
     return lines
 
 
+# ---------------------------------------------------------------------------
+# the mixed request stream: plain one-launch-per-request path vs the persistent server
+# ---------------------------------------------------------------------------
+
+STREAM_CLASSES = [256 << k for k in range(19)]          # packed sizes 256 B .. 64 MiB
+STREAM_REDUCE = (("double", "TYPE_DOUBLE", 8, "OP_SUM"), ("int64", "TYPE_INT64_T", 8, "OP_MAX"),
+                 ("uint32", "TYPE_UINT32_T", 4, "OP_BXOR"), ("c_complex", "TYPE_C_COMPLEX", 8, "OP_PROD"))
+
+
+def stream_family_types(yk, np, seed):
+    """(family, class) -> dict(mk, base, count, extent, op, dirs): one type per packed-size
+    class for each type family of the plain configurations, packed size == class size
+    (struct: the largest multiple of its 20-byte element)."""
+    rng = np.random.default_rng(seed)
+    out = {}
+    for S in STREAM_CLASSES:
+        # 4-column blocks of an (S/32) x 16 row-major double matrix
+        out[("hvector", S)] = dict(mk=lambda L, S=S: L.type_create_hvector(S // 32, 4, 128, yk.TYPE_DOUBLE),
+                                   base="double", count=1, extent=(S // 32) * 128, op=yk.OP_REPLACE)
+        # x-face of a {Z, Y, 512} float grid, depth 2: 8-byte runs at a 2 KiB row stride
+        Y = min(512, S // 8)
+        Z = S // 8 // Y
+        x0 = int(rng.choice([0, 510]))
+        out[("halo", S)] = dict(mk=lambda L, Z=Z, Y=Y, x0=x0: L.type_create_subarray(
+            [Z, Y, 512], [Z, Y, 2], [0, 0, x0], yk.SUBARRAY_ORDER_C, yk.TYPE_FLOAT),
+            base="float", count=1, extent=Z * Y * 2048, op=yk.OP_REPLACE)
+        # hindexed int32: lognormal block lengths (median 16, sigma 1, clipped 1..4096),
+        # non-overlapping blocks in shuffled order inside a resized extent of 4 S
+        nel = S // 4
+        draw = np.clip(np.round(np.exp(np.log(16) + rng.standard_normal(nel // 8 + 64))), 1, 4096)
+        cum = np.cumsum(draw.astype(np.int64))
+        nb = int(np.searchsorted(cum, nel)) + 1
+        assert nb <= len(draw)
+        blens = draw[:nb].astype(np.int64)
+        blens[-1] -= int(cum[nb - 1]) - nel
+        free = 4 * nel - nel
+        gaps = rng.integers(0, 2 * (free // nb) + 1, nb)
+        if int(gaps.sum()) > free:
+            gaps = gaps * free // int(gaps.sum())
+        order = rng.permutation(nb)
+        starts = np.cumsum(blens[order] + gaps) - blens[order]
+        assert int(starts[-1] + blens[order][-1]) <= 4 * nel
+        displs = np.empty(nb, dtype=np.int64)
+        displs[order] = starts * 4
+
+        def mk_hind(L, nb=nb, blens=blens, displs=displs, S=S):
+            h = L.type_create_hindexed_arrays(nb, blens.ctypes.data, displs.ctypes.data, yk.TYPE_INT32_T)
+            r = L.type_create_resized(h, 0, 4 * S)
+            L.type_free(h)
+            return r
+        out[("hindexed", S)] = dict(mk=mk_hind, base="int32", count=1, extent=4 * S, op=yk.OP_REPLACE,
+                                    keep=(blens, displs))
+
+        # {int64 x1, float x3} resized to 32 bytes
+        def mk_struct(L):
+            s = L.type_create_struct([1, 3], [0, 8], [yk.TYPE_INT64_T, yk.TYPE_FLOAT])
+            r = L.type_create_resized(s, 0, 32)
+            L.type_free(s)
+            return r
+        out[("struct", S)] = dict(mk=mk_struct, base="float", count=max(1, S // 20), extent=32 * max(1, S // 20),
+                                  op=yk.OP_REPLACE)
+        # indexed_block of 8-element blocks at sorted random offsets over a 4 S target,
+        # unpacked with the config's reduction op
+        for base, tname, es, opname in STREAM_REDUCE:
+            nbk = max(1, S // (8 * es))
+            tel = 4 * S // es
+            offs = np.sort(rng.integers(0, tel - 8, nbk)).astype(np.int64)
+            out[("reduce_" + base, S)] = dict(
+                mk=lambda L, nbk=nbk, offs=offs, tname=tname: L.type_create_indexed_block_array(
+                    nbk, 8, offs.ctypes.data, getattr(yk, tname)),
+                base=base, count=1, extent=4 * S, op=getattr(yk, opname), keep=(offs,), unpack_only=True)
+    return out
+
+
+def dev_fill(torch, base, nbytes, gen):
+    """Valid seeded values of `base` filling a new device buffer of nbytes."""
+    n = (nbytes + 15) // 16 * 16
+    out = torch.empty(n, dtype=torch.uint8, device="cuda")
+    if base == "double":
+        out.view(torch.float64).normal_(generator=gen)
+    elif base == "float":
+        out.view(torch.float32).uniform_(-1, 1, generator=gen)
+    elif base == "c_complex":
+        z = out.view(torch.float32).view(-1, 2)
+        r = torch.exp(torch.empty(z.shape[0], device="cuda").uniform_(-0.10536, 0.09531, generator=gen))
+        a = torch.empty(z.shape[0], device="cuda").uniform_(0, 6.283185307179586, generator=gen)
+        z[:, 0] = r * torch.cos(a)
+        z[:, 1] = r * torch.sin(a)
+    else:
+        out.random_(0, 256, generator=gen)
+    return out
+
+
+def run_stream(nreq=10000, rate=50e3, seed=5, check=True, log=None):
+    """10,000 pack/unpack requests with Poisson arrivals at `rate` req/s: families drawn
+    uniformly from hvector/halo/hindexed/struct/reduce, packed sizes log-uniform over
+    19 power-of-two classes 256 B .. 64 MiB, 20% with the packed buffer in pinned host
+    memory.  Each request uses its (family, class) arena: one typed buffer per family
+    and one packed buffer per (family, class, host); checked requests own private
+    buffers and are compared with the oracle after each path.  Returns a dict."""
+    import numpy as np
+    import torch
+    import yaksa_gb300 as yk
+    oracle_path = os.path.join(ROOT, "oracle", "_ref", "liboracle_yaksa.so")
+    if check and not os.path.exists(oracle_path):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    y = yk.Yaksa()
+    y.init()
+    specs = stream_family_types(yk, np, seed)
+    fams = ["hvector", "halo", "hindexed", "struct", "reduce"]
+    rng = np.random.default_rng(seed + 1)
+    gen = torch.Generator(device="cuda").manual_seed(seed)
+    fam_of = rng.integers(0, len(fams), nreq)
+    cls_of = rng.integers(0, len(STREAM_CLASSES), nreq)
+    red_of = rng.integers(0, len(STREAM_REDUCE), nreq)
+    dir_of = rng.integers(0, 2, nreq)
+    host_of = rng.random(nreq) < 0.2
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, nreq))
+    arrivals -= arrivals[0]
+    keys = []
+    for i in range(nreq):
+        f = fams[fam_of[i]]
+        if f == "reduce":
+            f = "reduce_" + STREAM_REDUCE[red_of[i]][0]
+        keys.append((f, STREAM_CLASSES[cls_of[i]]))
+    used = sorted(set(keys), key=lambda k: (k[0], k[1]))
+    types = {k: specs[k]["mk"](y) for k in used}
+    sizes = {k: y.size(types[k]) * specs[k]["count"] for k in used}
+    # arenas: one typed buffer per family (largest extent), packed buffers per key
+    arena = {}
+    for k in used:
+        arena[k[0]] = max(arena.get(k[0], 0), specs[k]["extent"])
+    typed = {f: dev_fill(torch, specs[next(k for k in used if k[0] == f)]["base"], n + 256, gen)
+             for f, n in arena.items()}
+    packed_d = {k: dev_fill(torch, specs[k]["base"], sizes[k] + 256, gen) for k in used}
+    packed_h = {}
+    for i in range(nreq):
+        if host_of[i] and keys[i] not in packed_h:
+            packed_h[keys[i]] = packed_d[keys[i]].cpu().pin_memory()
+    # checked requests: small ones, private buffers
+    small = [i for i in range(nreq) if keys[i][1] <= (256 << 10)]
+    chk = set(rng.choice(small, size=min(len(small), 120), replace=False).tolist()) if check else set()
+    priv = {}
+    for i in sorted(chk):
+        k = keys[i]
+        t0 = typed[k[0]][:specs[k]["extent"] + 256].clone()
+        p0 = packed_d[k][:sizes[k] + 256].clone()
+        priv[i] = dict(t_init=t0.cpu().numpy(), p_init=p0.cpu().numpy(), t=t0,
+                       p=(p0.cpu().pin_memory() if host_of[i] else p0))
+    torch.cuda.synchronize()
+
+    def make_ops():
+        ops = (yk.PupOp * nreq)()
+        for i in range(nreq):
+            k = keys[i]
+            sp = specs[k]
+            if i in priv:
+                tptr, pptr = priv[i]["t"].data_ptr(), priv[i]["p"].data_ptr()
+            else:
+                tptr = typed[k[0]].data_ptr()
+                pptr = (packed_h[k] if host_of[i] else packed_d[k]).data_ptr()
+            unpack = sp.get("unpack_only") or dir_of[i] == 1
+            if unpack:
+                ops[i] = yk.unpack_op(pptr, sizes[k], tptr, sp["count"], types[k], 0, op=sp["op"])
+            else:
+                ops[i] = yk.pack_op(tptr, sp["count"], types[k], 0, pptr, sizes[k], op=sp["op"])
+        return ops
+
+    def reset_private():
+        for i, pv in priv.items():
+            pv["t"].copy_(torch.from_numpy(pv["t_init"]))
+            pv["p"].copy_(torch.from_numpy(pv["p_init"]))
+        torch.cuda.synchronize()
+
+    o = None
+    expect = {}
+    if check:
+        o = yk.Yaksa(oracle_path)
+        o.init()
+        for i in sorted(priv):
+            k = keys[i]
+            sp = specs[k]
+            to = sp["mk"](o)
+            th, ph = priv[i]["t_init"].copy(), priv[i]["p_init"].copy()
+            if sp.get("unpack_only") or dir_of[i] == 1:
+                o.unpack(ph.ctypes.data, sizes[k], th.ctypes.data, sp["count"], to, 0, op=sp["op"])
+            else:
+                o.pack(th.ctypes.data, sp["count"], to, 0, ph.ctypes.data, sizes[k], op=sp["op"])
+            o.type_free(to)
+            expect[i] = (th, ph)
+
+    def verify():
+        bad = []
+        for i, (th, ph) in expect.items():
+            gt = priv[i]["t"].cpu().numpy()
+            gp = priv[i]["p"].cpu().numpy()
+            if not (np.array_equal(gt, th) and np.array_equal(gp, ph)):
+                bad.append(i)
+        return bad
+
+    total = float(sum(sizes[k] for k in keys))
+    res = {"requests": nreq, "rate_per_s": rate, "packed_bytes": total,
+           "checked_requests": len(chk), "families": fams,
+           "size_classes": [STREAM_CLASSES[0], STREAM_CLASSES[-1]],
+           "host_fraction": float(host_of.mean()),
+           "arena_bytes": int(sum(arena.values()))}
+    zero = np.zeros(nreq)
+    srv = yk.Server(y, ring_requests=4096, budget_bytes=8 << 30)
+    for mode in ("plain", "server"):
+        s = srv if mode == "server" else None
+        # warm: every descriptor built and uploaded once, outside the timed runs
+        ops = make_ops()
+        yk.serve_trace(y, ops, zero, server=s)
+        torch.cuda.synchronize()
+        reset_private()
+        ops = make_ops()
+        launches0 = y.stats()["launches"]
+        lat, mk = yk.serve_trace(y, ops, arrivals.tolist(), server=s)
+        torch.cuda.synchronize()
+        launches = y.stats()["launches"] - launches0
+        bad = verify() if check else []
+        lat_us = np.array(lat) * 1e6
+        # closed loop: everything arrives at once -> capacity
+        ops2 = make_ops()
+        _, mk2 = yk.serve_trace(y, ops2, zero, server=s)
+        torch.cuda.synchronize()
+        res[mode] = {"open_loop": {"GBps": total / mk / 1e9, "makespan_s": mk,
+                                   "p50_us": float(np.percentile(lat_us, 50)),
+                                   "p99_us": float(np.percentile(lat_us, 99)),
+                                   "mean_us": float(lat_us.mean()), "kernel_launches": launches},
+                     "closed_loop": {"GBps": total / mk2 / 1e9, "req_per_s": nreq / mk2, "makespan_s": mk2},
+                     "bit_exact": not bad, "mismatched": bad[:10]}
+        if log:
+            print(json.dumps({mode: res[mode]}), file=log, flush=True)
+    res["server_stats"] = srv.stats()
+    srv.destroy()
+    res["server_over_plain"] = {
+        "closed_loop_throughput": res["server"]["closed_loop"]["GBps"] / res["plain"]["closed_loop"]["GBps"],
+        "open_loop_p99": res["server"]["open_loop"]["p99_us"] / res["plain"]["open_loop"]["p99_us"]}
+    for k in used:
+        y.type_free(types[k])
+    if o:
+        o.finalize()
+    del typed, packed_d, packed_h, priv
+    torch.cuda.empty_cache()
+    return res
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -332,6 +580,10 @@ def main():
     ap.add_argument("--suite", default=None,
                     help="also run the hvector/hindexed/struct/reduction configs and write their "
                          "JSON lines to this file")
+    ap.add_argument("--stream", default=None,
+                    help="run only the mixed request stream (plain vs server) and write its JSON")
+    ap.add_argument("--stream-requests", type=int, default=10000)
+    ap.add_argument("--no-stream", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -339,6 +591,14 @@ def main():
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         run_suite(args.suite, args.steps, args.cpu_seconds)
+        return
+    if args.stream:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        r = run_stream(nreq=args.stream_requests, log=sys.stderr)
+        with open(args.stream, "w") as f:
+            f.write(json.dumps(r) + "\n")
+        print(json.dumps(r))
         return
 
     import numpy as np

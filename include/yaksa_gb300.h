@@ -83,6 +83,18 @@ int yaksa_gb300_server_stats(yaksa_gb300_server_t server, uint64_t * requests, u
                              uint64_t * relaunches, uint32_t * idle_exits);
 int yaksa_gb300_server_destroy(yaksa_gb300_server_t server);
 
+/* Serving loop (no counterpart in the reference, whose callers issue one
+ * yaksa_ipack/yaksa_iunpack per message, src/frontend/include/yaksa.h.in:484,520):
+ * replays n requests that arrive at arrival_s[i] seconds after the call starts.
+ * mode 0 issues each as yaksa_ipack/yaksa_iunpack on arrival (one launch per
+ * request); mode 1 submits them to `server`, admitting in arrival order and holding
+ * a refused request (rings or byte budget full) at the head until progress frees
+ * room. latency_s[i] = completion time seen by the loop - arrival_s[i];
+ * *makespan_s = time of the last completion. ops[i].actual is set. */
+int yaksa_gb300_serve_trace(yaksa_gb300_pup_t * ops, const double *arrival_s, int n, int mode,
+                            yaksa_gb300_server_t server, yaksa_info_t info, double *latency_s,
+                            double *makespan_s);
+
 /* Runtime counters since load: kernel launches, calls served in place (device or
  * GPU-addressable host memory), calls that staged host data through device memory,
  * and contiguous calls served by one copy. */

@@ -150,7 +150,11 @@ def load_library(path):
                            ("yaksa_gb300_server_stats", [_vp, ctypes.POINTER(_u64), ctypes.POINTER(_u64),
                                                          ctypes.POINTER(_u64),
                                                          ctypes.POINTER(ctypes.c_uint32)]),
-                           ("yaksa_gb300_server_destroy", [_vp])):
+                           ("yaksa_gb300_server_destroy", [_vp]),
+                           ("yaksa_gb300_serve_trace", [ctypes.POINTER(PupOp), ctypes.POINTER(ctypes.c_double),
+                                                        ctypes.c_int, ctypes.c_int, _vp, _vp,
+                                                        ctypes.POINTER(ctypes.c_double),
+                                                        ctypes.POINTER(ctypes.c_double)])):
             f = getattr(lib, name)
             f.restype = ctypes.c_int
             f.argtypes = args
@@ -197,6 +201,20 @@ class Server:
         if self.h:
             self.y._chk("yaksa_gb300_server_destroy", self.y.lib.yaksa_gb300_server_destroy(self.h))
             self.h = None
+
+
+def serve_trace(y, ops, arrival_s, server=None, info=None):
+    """Replay `ops` (a yaksa_gb300_pup_t array) arriving at `arrival_s` seconds through
+    the plain nonblocking path (server None) or `server`; returns (latencies, makespan)."""
+    n = len(ops)
+    arr = (ctypes.c_double * max(1, n))(*arrival_s)
+    lat = (ctypes.c_double * max(1, n))()
+    mk = ctypes.c_double()
+    y._chk("yaksa_gb300_serve_trace",
+           y.lib.yaksa_gb300_serve_trace(ops, arr, n, 1 if server is not None else 0,
+                                         server.h if server is not None else None, info, lat,
+                                         ctypes.byref(mk)))
+    return list(lat[:n]), mk.value
 
 
 def _arr(ctype, seq):

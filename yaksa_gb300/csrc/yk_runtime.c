@@ -46,11 +46,13 @@ static struct {
     cudaStream_t stream;
     yk_req *reqs;
     size_t nreqs;
+    size_t *freeidx;            /* stack of free request slots */
+    size_t nfree;
     cudaEvent_t *evpool;
     size_t nev, capev;
     /* counters (yaksa_gb300_stats) */
     uint64_t launches, staged_calls, direct_calls, memcpy_calls;
-} R = { PTHREAD_MUTEX_INITIALIZER, 0, 0, 0, 0, 0, NULL, NULL, 0, NULL, 0, 0, 0, 0, 0, 0 };
+} R = { PTHREAD_MUTEX_INITIALIZER, 0, 0, 0, 0, 0, NULL, NULL, 0, NULL, 0, NULL, 0, 0, 0, 0, 0, 0 };
 
 static int cuda_err(cudaError_t e, const char *what)
 {
@@ -127,6 +129,9 @@ void yk_runtime_finalize(void)
     free(R.reqs);
     R.reqs = NULL;
     R.nreqs = 0;
+    free(R.freeidx);
+    R.freeidx = NULL;
+    R.nfree = 0;
     free(R.evpool);
     R.evpool = NULL;
     R.capev = 0;
@@ -171,21 +176,23 @@ static void event_put(cudaEvent_t ev)
 static int request_new(cudaEvent_t ev, yk_type * t, void *s0, void *s1, yaksa_request_t * out)
 {
     pthread_mutex_lock(&R.mu);
-    size_t i;
-    for (i = 0; i < R.nreqs; i++)
-        if (!R.reqs[i].in_use)
-            break;
-    if (i == R.nreqs) {
+    if (!R.nfree) {
         size_t nn = R.nreqs ? 2 * R.nreqs : 64;
         yk_req *p = realloc(R.reqs, nn * sizeof(yk_req));
-        if (!p) {
+        size_t *f = p ? realloc(R.freeidx, nn * sizeof(size_t)) : NULL;
+        if (p)
+            R.reqs = p;
+        if (!f) {
             pthread_mutex_unlock(&R.mu);
             return YAKSA_ERR__OUT_OF_MEM;
         }
         memset(p + R.nreqs, 0, (nn - R.nreqs) * sizeof(yk_req));
-        R.reqs = p;
+        R.freeidx = f;
+        for (size_t k = nn; k > R.nreqs; k--)
+            R.freeidx[R.nfree++] = k - 1;       /* lowest index on top */
         R.nreqs = nn;
     }
+    size_t i = R.freeidx[--R.nfree];
     R.reqs[i].in_use = 1;
     R.reqs[i].ev = ev;
     R.reqs[i].type = t;
@@ -201,6 +208,7 @@ static void request_release(size_t i)
     pthread_mutex_lock(&R.mu);
     yk_req r = R.reqs[i];
     R.reqs[i].in_use = 0;
+    R.freeidx[R.nfree++] = i;
     pthread_mutex_unlock(&R.mu);
     event_put(r.ev);
     if (r.scratch[0])
@@ -807,6 +815,7 @@ int yaksa_gb300_ipup_batch(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info,
 typedef struct {
     uint64_t seq;               /* request sequence number (ticket) */
     uint64_t item0, nitems;
+    uint64_t checked;           /* leading items already seen done */
     uint64_t bytes;
     yk_type *t;
     int busy;
@@ -884,25 +893,27 @@ int yaksa_gb300_server_create(uint32_t ring_requests, uint64_t budget_bytes,
  * pending; caller holds S->mu */
 static int server_progress_locked(struct yaksa_gb300_server_s *S)
 {
-    while (S->oldest_req < S->req_seq) {
-        yk_srv_slot *sl = &S->slots[S->oldest_req % S->qr];
-        if (sl->busy) {
-            int done = 1;
-            for (uint64_t i = sl->item0; i < sl->item0 + sl->nitems; i++)
-                if (__atomic_load_n(&S->item_done[i % S->qi], __ATOMIC_ACQUIRE) != i + 1) {
-                    done = 0;
-                    break;
-                }
-            if (!done)
+    /* any request whose items are all done completes, in whatever order */
+    for (uint64_t s = S->oldest_req; s < S->req_seq; s++) {
+        yk_srv_slot *sl = &S->slots[s % S->qr];
+        if (!sl->busy)
+            continue;
+        while (sl->checked < sl->nitems) {
+            uint64_t i = sl->item0 + sl->checked;
+            if (__atomic_load_n(&S->item_done[i % S->qi], __ATOMIC_ACQUIRE) != i + 1)
                 break;
-            sl->busy = 0;
-            S->inflight_bytes -= sl->bytes;
-            if (sl->t)
-                yk_type_unref(sl->t);
-            sl->t = NULL;
+            sl->checked++;
         }
-        S->oldest_req++;
+        if (sl->checked < sl->nitems)
+            continue;
+        sl->busy = 0;
+        S->inflight_bytes -= sl->bytes;
+        if (sl->t)
+            yk_type_unref(sl->t);
+        sl->t = NULL;
     }
+    while (S->oldest_req < S->req_seq && !S->slots[S->oldest_req % S->qr].busy)
+        S->oldest_req++;
     if (S->running && cudaStreamQuery(S->stream) != cudaErrorNotReady) {
         S->running = 0;
         cudaGetLastError();
@@ -1001,6 +1012,7 @@ int yaksa_gb300_server_submit(yaksa_gb300_server_t S, yaksa_gb300_pup_t * o, yak
     sl->seq = seq;
     sl->item0 = S->item_seq;
     sl->nitems = nitems;
+    sl->checked = 0;
     sl->bytes = n;
     sl->busy = 1;
     sl->t = t;
@@ -1027,12 +1039,19 @@ int yaksa_gb300_server_submit(yaksa_gb300_server_t S, yaksa_gb300_pup_t * o, yak
     return rc;
 }
 
+static int server_done_locked(struct yaksa_gb300_server_s *S, uint64_t ticket)
+{
+    if (ticket < S->oldest_req)
+        return 1;
+    yk_srv_slot *sl = &S->slots[ticket % S->qr];
+    return ticket < S->req_seq && (sl->seq != ticket || !sl->busy);
+}
+
 int yaksa_gb300_server_test(yaksa_gb300_server_t S, uint64_t ticket, int *done)
 {
     pthread_mutex_lock(&S->mu);
     int rc = server_progress_locked(S);
-    *done = ticket < S->oldest_req ||
-        (ticket < S->req_seq && !S->slots[ticket % S->qr].busy);
+    *done = server_done_locked(S, ticket);
     pthread_mutex_unlock(&S->mu);
     return rc;
 }
@@ -1106,6 +1125,101 @@ int yaksa_gb300_server_destroy(yaksa_gb300_server_t S)
     free(S->slots);
     pthread_mutex_destroy(&S->mu);
     free(S);
+    return rc;
+}
+
+/* ------------------------------------------------------------------------- */
+/* serving loop: replay an arrival schedule through the plain or batched path */
+/* ------------------------------------------------------------------------- */
+
+static double now_s(void)
+{
+    struct timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return (double) t.tv_sec + 1e-9 * (double) t.tv_nsec;
+}
+
+int yaksa_gb300_serve_trace(yaksa_gb300_pup_t * ops, const double *arrival_s, int n, int mode,
+                            yaksa_gb300_server_t server, yaksa_info_t info, double *latency_s,
+                            double *makespan_s)
+{
+    int rc = runtime_ready();
+    if (rc)
+        return rc;
+    if (mode == 1 && !server)
+        return YAKSA_ERR__INTERNAL;
+    uint64_t *handle = calloc(n > 0 ? n : 1, sizeof(uint64_t));
+    char *state = calloc(n > 0 ? n : 1, 1);     /* 0 waiting, 1 in flight, 2 done */
+    if (!handle || !state) {
+        free(handle);
+        free(state);
+        return YAKSA_ERR__OUT_OF_MEM;
+    }
+    int next = 0, done = 0, oldest = 0;
+    double t0 = now_s(), last = t0;
+    while (done < n && !rc) {
+        double t = now_s() - t0;
+        /* admit arrivals in order; a refused request waits at the head (FIFO) */
+        while (next < n && arrival_s[next] <= t) {
+            yaksa_gb300_pup_t *o = &ops[next];
+            if (mode == 1) {
+                uint64_t tk;
+                int r = yaksa_gb300_server_submit(server, o, info, &tk);
+                if (r == YAKSA_ERR__OUT_OF_MEM)
+                    break;      /* rings or byte budget full: retry after progress */
+                if (r) {
+                    rc = r;
+                    break;
+                }
+                handle[next] = tk;
+            } else {
+                yaksa_request_t req;
+                uintptr_t actual;
+                int r = o->kind == 0 ?
+                    yaksa_ipack(o->inbuf, o->count, o->type, o->offset, o->outbuf, o->maxbytes,
+                                &actual, info, o->op, &req) :
+                    yaksa_iunpack(o->inbuf, o->maxbytes, o->outbuf, o->count, o->type, o->offset,
+                                  &actual, info, o->op, &req);
+                if (r) {
+                    rc = r;
+                    break;
+                }
+                o->actual = actual;
+                handle[next] = req;
+            }
+            state[next] = 1;
+            next++;
+        }
+        /* completions: one progress pass, then a cheap done check per request in flight
+         * (requests may finish out of order) */
+        if (mode == 1) {
+            pthread_mutex_lock(&server->mu);
+            rc = server_progress_locked(server);
+        }
+        double tc = now_s();
+        for (int i = oldest; i < next && !rc; i++) {
+            if (state[i] != 1)
+                continue;
+            int c = 0;
+            if (mode == 1)
+                c = server_done_locked(server, handle[i]);
+            else
+                rc = yaksa_request_test(handle[i], &c);
+            if (c) {
+                latency_s[i] = tc - t0 - arrival_s[i];
+                state[i] = 2;
+                done++;
+                last = tc;
+            }
+        }
+        if (mode == 1)
+            pthread_mutex_unlock(&server->mu);
+        while (oldest < next && state[oldest] == 2)
+            oldest++;
+    }
+    *makespan_s = last - t0;
+    free(handle);
+    free(state);
     return rc;
 }
 
