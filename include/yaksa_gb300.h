@@ -83,6 +83,26 @@ int yaksa_gb300_server_stats(yaksa_gb300_server_t server, uint64_t * requests, u
                              uint64_t * relaunches, uint32_t * idle_exits);
 int yaksa_gb300_server_destroy(yaksa_gb300_server_t server);
 
+/* One pack (kind 0) or unpack (kind 1) that allocates nothing (no counterpart in the
+ * reference).  For callers that must not allocate device memory: a library whose
+ * device memory is all owned by the application's allocator, or code issuing requests
+ * beside a resident persistent kernel, where the cudaFree that releases a type's
+ * table allocation would synchronize the device.  Same kernels and bytes as
+ * yaksa_pack_stream/yaksa_unpack_stream; the type's descriptor tables are copied into
+ * a static 8 MiB device array on *stream (NULL: the legacy default stream) just before
+ * the kernel; the call returns once both are enqueued and sets op->actual.
+ *   - The first call on a device resolves that array's address (and may load the
+ *     library's module): make it before any stream capture begins.  The first call
+ *     for a type builds the type's host-side tables on the host heap, kept with the
+ *     type until yaksa_type_free.
+ *   - Types whose tables exceed 8 MiB (about 500,000 hindexed blocks) are refused
+ *     with YAKSA_ERR__NOT_SUPPORTED and a message on stderr; so are buffers the GPU
+ *     cannot address (staging would need device memory).
+ *   - Nothing in the array needs to start at zero.  The array is shared: calls whose
+ *     work overlaps in time (different streams, no ordering between them) race on it,
+ *     so order them on one stream or by events. */
+int yaksa_gb300_pup_noalloc(yaksa_gb300_pup_t * op, void *stream);
+
 /* Serving loop (no counterpart in the reference, whose callers issue one
  * yaksa_ipack/yaksa_iunpack per message, src/frontend/include/yaksa.h.in:484,520):
  * replays n requests that arrive at arrival_s[i] seconds after the call starts.

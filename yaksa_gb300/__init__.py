@@ -151,6 +151,7 @@ def load_library(path):
                                                          ctypes.POINTER(_u64),
                                                          ctypes.POINTER(ctypes.c_uint32)]),
                            ("yaksa_gb300_server_destroy", [_vp]),
+                           ("yaksa_gb300_pup_noalloc", [ctypes.POINTER(PupOp), _vp]),
                            ("yaksa_gb300_serve_trace", [ctypes.POINTER(PupOp), ctypes.POINTER(ctypes.c_double),
                                                         ctypes.c_int, ctypes.c_int, _vp, _vp,
                                                         ctypes.POINTER(ctypes.c_double),
@@ -425,6 +426,11 @@ class Yaksa:
         self._chk("yaksa_gb300_graph_create",
                   self.lib.yaksa_gb300_graph_create(arr, e, len(ends), info, ctypes.byref(g)))
         return g, arr
+
+    def pup_noalloc(self, op, stream_ptr=None):
+        """yaksa_gb300_pup_noalloc: one request through the static descriptor scratch;
+        returns the YAKSA_* code (0 on success) and sets op.actual."""
+        return self.lib.yaksa_gb300_pup_noalloc(ctypes.byref(op), stream_ptr)
 
     def graph_launch(self, g, stream_ptr=None):
         self._chk("yaksa_gb300_graph_launch", self.lib.yaksa_gb300_graph_launch(g, stream_ptr))

@@ -725,6 +725,22 @@ int yk_desc_get(yk_type * t, int typed, yk_devdesc ** out)
     return dd->status;
 }
 
+/* The descriptor with its tables left on the host heap (built once, kept with the
+ * type): the no-allocation entry point copies them into its static device scratch
+ * per request instead of keeping a device allocation per type. */
+int yk_desc_get_host(yk_type * t, int typed, yk_devdesc ** out)
+{
+    yk_devdesc *dd = typed ? &t->host_typed_desc : &t->host_bytes_desc;
+    pthread_mutex_lock(&t->desc_mutex);
+    if (!dd->built) {
+        dd->status = build(t, typed, dd, 0);
+        dd->built = 1;
+    }
+    pthread_mutex_unlock(&t->desc_mutex);
+    *out = dd;
+    return dd->status;
+}
+
 /* the type's descriptor with the element level VEC(count, extent, size) in front
  * (merged into the first level or the leaf when the layout allows) */
 void yk_make_launch_desc(const yk_devdesc * dd, const yk_type * t, uintptr_t count, yk_desc * out)
@@ -808,6 +824,9 @@ void yk_desc_release(yk_type * t)
     if (t->typed_desc.dev_tables)
         cudaFree(t->typed_desc.dev_tables);
     t->bytes_desc.dev_tables = t->typed_desc.dev_tables = NULL;
+    free(t->host_bytes_desc.dev_tables);
+    free(t->host_typed_desc.dev_tables);
+    t->host_bytes_desc.dev_tables = t->host_typed_desc.dev_tables = NULL;
 }
 
 /* ------------------------------------------------------------------------- */

@@ -60,6 +60,10 @@ struct yk_type {
     pthread_mutex_t desc_mutex;
     yk_devdesc bytes_desc;      /* REPLACE: byte-exact, merges across base types */
     yk_devdesc typed_desc;      /* operators: segments carry their base type */
+    /* the same two descriptors with their tables on the host heap, for requests
+     * whose tables travel in the static device scratch (yaksa_gb300_pup_noalloc) */
+    yk_devdesc host_bytes_desc;
+    yk_devdesc host_typed_desc;
 };
 
 typedef struct {
@@ -85,6 +89,9 @@ int yk_base_type_size(int bt);
 
 /* descriptors (yk_build.c) */
 int yk_desc_get(yk_type * t, int typed, yk_devdesc ** out);
+int yk_desc_get_host(yk_type * t, int typed, yk_devdesc ** out);
+/* yk_noalloc.cu: the current device's address of the static descriptor scratch */
+int yk_noalloc_scratch(void **ptr, size_t * bytes);
 void yk_desc_release(yk_type * t);
 void yk_make_launch_desc(const yk_devdesc * dd, const yk_type * t, uintptr_t count, yk_desc * out);
 uintptr_t yk_builtin_floor(yk_type * t, uintptr_t count, uintptr_t pos);

@@ -386,8 +386,10 @@ static int plan(int dir, const void *packed_in, void *packed_out, char *typed, u
 
 enum { YK_X_MEMCPY, YK_X_BYTES, YK_X_TYPED, YK_X_ORDERED };
 
-static int prepare(const yk_plan * p, char *typed, char *packed, yk_launch * L, int *kind,
-                   int *sorted)
+typedef int (*yk_desc_getter)(yk_type * t, int typed, yk_devdesc ** out);
+
+static int prepare_with(const yk_plan * p, char *typed, char *packed, yk_launch * L, int *kind,
+                        int *sorted, yk_desc_getter get)
 {
     yk_type *t = p->t;
     uintptr_t count = p->count, b0 = p->b0, n = p->b1 - p->b0;
@@ -407,7 +409,7 @@ static int prepare(const yk_plan * p, char *typed, char *packed, yk_launch * L, 
     }
     int typed_op = (op != YAKSA_OP__REPLACE);
     yk_devdesc *dd;
-    int rc = yk_desc_get(t, typed_op, &dd);
+    int rc = get(t, typed_op, &dd);
     if (rc)
         return rc;
     uint64_t ext = (uint64_t) (t->extent < 0 ? -t->extent : t->extent);
@@ -417,7 +419,7 @@ static int prepare(const yk_plan * p, char *typed, char *packed, yk_launch * L, 
         /* ordered REPLACE uses the typed descriptor's element structure when the
          * sorted-block kernel applies to it */
         yk_devdesc *tdd;
-        if (t->base_type > 0 && yk_desc_get(t, 1, &tdd) == YAKSA_SUCCESS && tdd->sorted_blocks)
+        if (t->base_type > 0 && get(t, 1, &tdd) == YAKSA_SUCCESS && tdd->sorted_blocks)
             ddo = tdd;
     }
     yk_make_launch_desc(ddo, t, count, &L->desc);
@@ -469,6 +471,13 @@ static int prepare(const yk_plan * p, char *typed, char *packed, yk_launch * L, 
         *kind = L->typed_op ? YK_X_TYPED : YK_X_BYTES;
     }
     return YAKSA_SUCCESS;
+}
+
+/* launch construction over the type's device-resident descriptors */
+static int prepare(const yk_plan * p, char *typed, char *packed, yk_launch * L, int *kind,
+                   int *sorted)
+{
+    return prepare_with(p, typed, packed, L, kind, sorted, yk_desc_get);
 }
 
 static int launch_prepared(const yk_plan * p, const yk_launch * L, int kind, int sorted,
@@ -804,6 +813,104 @@ int yaksa_gb300_ipup_batch(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info,
     if (rc)
         return rc;
     return complete(NULL, YK_MODE_NONBLOCKING, R.stream, request);
+}
+
+/* ------------------------------------------------------------------------- */
+/* one pack/unpack that allocates nothing (no counterpart in the reference)   */
+/* ------------------------------------------------------------------------- */
+
+/* For callers that must not allocate device memory: a library sharing the device
+ * with an application allocator that owns all of it, or code issuing requests beside
+ * a resident persistent kernel, where the cudaFree that eventually releases a type's
+ * table allocation would synchronize the device.  The request runs the plain path's
+ * kernels; the type's tables (host copy, kept with the type) are written into the
+ * static scratch of yk_noalloc.cu on the caller's stream just before the launch. */
+
+#define YK_TABLE_PTRS(d, X)                                                   \
+    do {                                                                      \
+        for (int i_ = 0; i_ < (d)->nlev; i_++) {                              \
+            X((d)->lv[i_].disp);                                              \
+            X((d)->lv[i_].pfx);                                               \
+            X((d)->lv[i_].tfb);                                               \
+        }                                                                     \
+        X((d)->seg_off);                                                      \
+        X((d)->seg_pfx);                                                      \
+        X((d)->seg_type);                                                     \
+    } while (0)
+
+static int desc_tables_in(const yk_desc * d, const char *h, uint64_t n)
+{
+    int in = 0;
+#define YK_IN(p) in |= (p) && (const char *) (p) >= h && (const char *) (p) < h + n
+    YK_TABLE_PTRS(d, YK_IN);
+#undef YK_IN
+    return in;
+}
+
+static void desc_rebase(yk_desc * d, const char *h, char *scr)
+{
+#define YK_REBASE(p) if (p) (p) = (void *) (scr + ((const char *) (p) - h))
+    YK_TABLE_PTRS(d, YK_REBASE);
+#undef YK_REBASE
+}
+
+int yaksa_gb300_pup_noalloc(yaksa_gb300_pup_t * o, void *stream)
+{
+    o->actual = 0;
+    yk_type *t = yk_type_get(o->type);
+    if (!t)
+        return YAKSA_ERR__INTERNAL;
+    yk_plan p;
+    int rc = o->kind == 0 ?
+        plan(0, NULL, o->outbuf, (char *) o->inbuf, o->count, t, o->offset, o->maxbytes, NULL,
+             o->op, &p) :
+        plan(1, o->inbuf, NULL, (char *) o->outbuf, o->count, t, o->offset, o->maxbytes, NULL,
+             o->op, &p);
+    if (rc || p.b1 == p.b0)
+        return rc;
+    if (p.staged) {
+        fprintf(stderr, "yaksa-gb300: yaksa_gb300_pup_noalloc: a buffer is not addressable "
+                "by the GPU and staging it would need device memory\n");
+        return YAKSA_ERR__NOT_SUPPORTED;
+    }
+    void *scr = NULL;
+    size_t scr_bytes = 0;
+    rc = cuda_err((cudaError_t) yk_noalloc_scratch(&scr, &scr_bytes), "static scratch setup");
+    if (rc)
+        return rc;
+    cudaStream_t s = stream ? *(cudaStream_t *) stream : (cudaStream_t) 0;
+    yk_launch L;
+    int kind, sorted;
+    rc = prepare_with(&p, p.dtyped, p.dpacked, &L, &kind, &sorted, yk_desc_get_host);
+    if (rc)
+        return rc;
+    if (kind != YK_X_MEMCPY) {
+        /* the launch reads the tables of exactly one host descriptor (or none) */
+        yk_devdesc *src = NULL;
+        for (int typed = 0; typed < 2 && !src; typed++) {
+            yk_devdesc *dd = typed ? &t->host_typed_desc : &t->host_bytes_desc;
+            if (dd->built && dd->dev_tables &&
+                desc_tables_in(&L.desc, (const char *) dd->dev_tables, dd->table_bytes))
+                src = dd;
+        }
+        if (src) {
+            if (src->table_bytes > scr_bytes) {
+                fprintf(stderr, "yaksa-gb300: yaksa_gb300_pup_noalloc: the type's descriptor "
+                        "tables take %llu bytes, more than the %zu-byte static scratch\n",
+                        (unsigned long long) src->table_bytes, scr_bytes);
+                return YAKSA_ERR__NOT_SUPPORTED;
+            }
+            rc = cuda_err(cudaMemcpyAsync(scr, src->dev_tables, src->table_bytes,
+                                          cudaMemcpyHostToDevice, s), "table copy");
+            if (rc)
+                return rc;
+            desc_rebase(&L.desc, (const char *) src->dev_tables, (char *) scr);
+        }
+    }
+    rc = launch_prepared(&p, &L, kind, sorted, s);
+    if (!rc)
+        o->actual = p.b1 - p.b0;
+    return rc;
 }
 
 /* ------------------------------------------------------------------------- */
