@@ -140,8 +140,12 @@ def cpu_baseline(oracle_path, seconds, threads):
         if time.perf_counter() - t0 > seconds:
             break
     dt = time.perf_counter() - t0
-    # correctness of the sample: the faces of dst equal those of src
-    ok = all(np.array_equal(bufs[i], bufs[i]) for i in range(len(faces)))
+    # correctness of the sample: every face of dst equals that face of src
+    s3, d3 = src.reshape(N, N, N), dst.reshape(N, N, N)
+    ok = all(np.array_equal(s3[sl], d3[sl]) for sl in
+             ((slice(None), slice(None), slice(0, 2)), (slice(None), slice(None), slice(N - 2, N)),
+              (slice(None), slice(0, 2)), (slice(None), slice(N - 2, N)), (slice(0, 2),),
+              (slice(N - 2, N),)))
     o.finalize()
     moved = 2 * P * len(faces) * n
     return {"value": moved / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
@@ -164,15 +168,17 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": b["value"], "unit": "GB/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "dtype": "f32", "data": "synthetic",
-            "config": {"workload": "halo3d 512^3 float32, 6 depth-2 faces, pack+unpack REPLACE"},
+            "config": {"workload": WORKLOAD, "parallelism": "host threads", "l2": "host caches"},
             "cpu_baseline": {"value": b["value"], "unit": "GB/s", "cores": threads, "kind": "port",
-                             "sample": b["sample"]},
+                             "sample": b["sample"], "faces_equal": bool(b["ok"])},
             "e2e": {"value": b["value"], "unit": "GB/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
 METRIC = "pack+unpack GB/s vs HBM peak (bit-exact); batched p50/p99 us vs plain path"
+WORKLOAD = (f"halo3d: {N}^3 float32 grid, 6 depth-2 subarray faces ({2 * N * N * 4 >> 20} MiB "
+            "packed each), pack + unpack REPLACE per step")
 
 
 # ---------------------------------------------------------------------------
@@ -723,46 +729,59 @@ def main():
     value = step_bytes * world / (tot / args.steps) / 1e9
     plain_value = step_bytes * world / (tot_plain / args.steps) / 1e9
     hbm, peak_kind = peaks()
-    # dominant kernel: yk_batch_kernel; algorithmic bytes = 2 per packed byte per launch
+    # dominant kernel: yk_batch_regular_kernel; algorithmic bytes = 2 per packed byte per launch
     alg = 2 * P * len(faces)
     med = {d: statistics.median(v) for d, v in per.items()}
     mean_launch = (med["pack"] + med["unpack"]) / 2
     achieved = alg / mean_launch / 1e9
 
-    # e2e through the reference's C-ABI (yaksa_ipack / yaksa_iunpack + wait) with host
-    # pinned buffers: the kernels read and write host memory over NVLink-C2C inside the
-    # timed region
-    hsrc = src.cpu().pin_memory()
-    hdst = torch.zeros_like(hsrc).pin_memory()
+    # e2e through the reference's C-ABI (yaksa_ipack / yaksa_iunpack + wait per face):
+    # the exchange through host memory.  Every step packs the six faces of the
+    # device-resident grid into pinned host buffers (the step's result, read back to
+    # the host: d2h) and unpacks the six host buffers into the device grid (the step's
+    # input from the host: h2d); the kernels write and read the host buffers in place
+    # over NVLink-C2C inside the timed region.
     hpk = [torch.empty(P, dtype=torch.uint8).pin_memory() for _ in faces]
 
-    def e2e_step():
-        reqs = [y.ipack(hsrc.data_ptr(), 1, t, 0, pk.data_ptr(), P)[1] for (name, t), pk in zip(faces, hpk)]
-        for r in reqs:
-            y.wait(r)
-        reqs = [y.iunpack(pk.data_ptr(), P, hdst.data_ptr(), 1, t, 0)[1] for (name, t), pk in zip(faces, hpk)]
-        for r in reqs:
-            y.wait(r)
-    for _ in range(2):
-        e2e_step()
+    def e2e_run(gsrc, gdst, steps):
+        def one():
+            reqs = [y.ipack(gsrc.data_ptr(), 1, t, 0, pk.data_ptr(), P)[1] for (name, t), pk in zip(faces, hpk)]
+            for r in reqs:
+                y.wait(r)
+            reqs = [y.iunpack(pk.data_ptr(), P, gdst.data_ptr(), 1, t, 0)[1] for (name, t), pk in zip(faces, hpk)]
+            for r in reqs:
+                y.wait(r)
+        for _ in range(2):
+            one()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            one()
+        return (time.perf_counter() - t0) / steps
+
     e_steps = max(3, args.steps // 2)
-    t0 = time.perf_counter()
-    for _ in range(e_steps):
-        e2e_step()
-    e2e_t = (time.perf_counter() - t0) / e_steps
-    ok = ok and faces_equal(hsrc, hdst)
+    dst.zero_()
+    torch.cuda.synchronize()
+    e2e_t = e2e_run(src, dst, e_steps)
+    ok = ok and faces_equal(src, dst)
     e2e = {"value": step_bytes * world / e2e_t / 1e9, "unit": "GB/s",
-           "h2d_bytes_per_step": P * len(faces) * 2, "d2h_bytes_per_step": P * len(faces) * 2,
-           "mode": "yaksa_ipack/yaksa_iunpack + wait per face on host pinned buffers; the kernels "
-                   "access host memory in place over NVLink-C2C"}
+           "h2d_bytes_per_step": P * len(faces), "d2h_bytes_per_step": P * len(faces),
+           "mode": "yaksa_ipack (device grid -> pinned host buffer) and yaksa_iunpack (pinned host "
+                   "buffer -> device grid) + yaksa_request_wait per face; kernels access the host "
+                   "buffers in place over NVLink-C2C"}
+    # the same with the grids themselves in pinned host memory (every byte over the link)
+    hsrc = src.cpu().pin_memory()
+    hdst = torch.zeros_like(hsrc).pin_memory()
+    e2e_h = e2e_run(hsrc, hdst, e_steps)
+    ok = ok and faces_equal(hsrc, hdst)
+    e2e_host = {"value": step_bytes * world / e2e_h / 1e9, "unit": "GB/s",
+                "note": "grids and packed buffers all in pinned host memory"}
 
     line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform [-1,1))",
-            "config": {"workload": "halo3d: 512^3 float32 grid, 6 depth-2 subarray faces "
-                                   "(2 MiB packed each), pack + unpack REPLACE per step, batched "
-                                   "C-ABI (one launch per direction) captured once as a CUDA "
-                                   "graph and replayed per step",
+            "config": {"workload": WORKLOAD,
+                       "path": "batched C-ABI (one launch per direction) captured once as a CUDA "
+                               "graph and replayed per step",
                        "parallelism": f"replicas x{world}",
                        "l2": "flushed between steps (512 MiB write outside the event-timed span)"},
             "bit_exact": bool(ok),
@@ -775,20 +794,50 @@ def main():
                                            "planning inside the timed span"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "traffic": None,
-                         "kernel": "yk_batch_kernel (6 faces per launch; mean of pack and unpack)",
+                         "kernel": "yk_batch_regular_kernel (6 faces per launch; mean of pack and unpack)",
                          "peak_source": peak_kind,
                          "launch_us": {d: v * 1e6 for d, v in med.items()},
                          "algorithmic_bytes_per_launch": alg},
             "gpu_launches": launches,
             "clocks": clk,
             "e2e": e2e,
+            "e2e_host_grid": e2e_host,
             "wall_s": wall}
+    if not args.no_stream:
+        # the metric's second half: batched (persistent server) vs plain p50/p99 on the
+        # mixed request stream; the grids of the halo step are released first
+        y.graph_free(graph)
+        torch.cuda.synchronize()
+        del src, dst, packed, flush, hsrc, hdst, hpk
+        torch.cuda.empty_cache()
+        r = run_stream(nreq=args.stream_requests, check=True)
+        line["stream"] = {
+            "workload": f"{r['requests']} pack/unpack requests, Poisson {r['rate_per_s']:.0f}/s, "
+                        "families hvector/halo x-face/hindexed/struct/indexed_block-reduce, "
+                        "packed sizes log-uniform over 19 power-of-two classes 256 B..64 MiB, "
+                        f"{100 * r['host_fraction']:.0f}% packed side in pinned host memory",
+            "packed_bytes": r["packed_bytes"],
+            "plain": {"p50_us": r["plain"]["open_loop"]["p50_us"], "p99_us": r["plain"]["open_loop"]["p99_us"],
+                      "GBps": r["plain"]["open_loop"]["GBps"],
+                      "capacity_GBps": r["plain"]["closed_loop"]["GBps"],
+                      "capacity_req_per_s": r["plain"]["closed_loop"]["req_per_s"]},
+            "batched": {"p50_us": r["server"]["open_loop"]["p50_us"], "p99_us": r["server"]["open_loop"]["p99_us"],
+                        "GBps": r["server"]["open_loop"]["GBps"],
+                        "capacity_GBps": r["server"]["closed_loop"]["GBps"],
+                        "capacity_req_per_s": r["server"]["closed_loop"]["req_per_s"]},
+            "capacity_ratio": r["server_over_plain"]["closed_loop_throughput"],
+            "p99_ratio": r["server_over_plain"]["open_loop_p99"],
+            "bit_exact": r["plain"]["bit_exact"] and r["server"]["bit_exact"],
+            "checked_requests": r["checked_requests"],
+            "note": "p50/p99 from arrival to completion seen by the serving loop; capacity = all "
+                    "requests arriving at once; batched = persistent-kernel server"}
     if rank == 0 and not args.no_cpu:
         oracle_path = os.path.join(ROOT, "oracle", "_ref", "liboracle_yaksa.so")
         if not os.path.exists(oracle_path):
             subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
         b = cpu_baseline(oracle_path, args.cpu_seconds, 1)
         line["cpu_baseline"] = {k: b[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        line["cpu_baseline"]["faces_equal"] = bool(b["ok"])
     if rank == 0:
         print(json.dumps(line))
     if dist:

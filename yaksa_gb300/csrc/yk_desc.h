@@ -112,7 +112,11 @@ typedef struct {
 #define YK_BATCH_MAX 16
 typedef struct {
     int32_t n;
-    int32_t pad;
+    uint32_t tile_mul;          /* tile g of the launch runs tile (g * tile_mul) mod total,
+                                 * a bijection (tile_mul coprime with the total) that
+                                 * spreads consecutive CTAs over every request, so the
+                                 * bandwidth-bound requests overlap the latency-bound
+                                 * ones; 1 = request order */
     uint64_t tile_start[YK_BATCH_MAX + 1];      /* first tile of each request */
     yk_launch req[YK_BATCH_MAX];
 } yk_batch;

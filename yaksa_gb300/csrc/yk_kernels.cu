@@ -254,7 +254,9 @@ template <int U>
 __global__ void __launch_bounds__(YK_THREADS, (U == 1 ? 8 : 4))
 yk_batch_regular_kernel(const __grid_constant__ yk_batch B)
 {
-    for (uint64_t g = blockIdx.x; g < B.tile_start[B.n]; g += gridDim.x) {
+    const uint64_t ntiles = B.tile_start[B.n];
+    for (uint64_t g0 = blockIdx.x; g0 < ntiles; g0 += gridDim.x) {
+        const uint64_t g = B.tile_mul > 1 ? (g0 * B.tile_mul) % ntiles : g0;
         int r = 0;
         while (g >= B.tile_start[r + 1])
             r++;
@@ -366,7 +368,9 @@ template <int U>
 __global__ void __launch_bounds__(YK_THREADS)
 yk_batch_kernel(const __grid_constant__ yk_batch B)
 {
-    for (uint64_t g = blockIdx.x; g < B.tile_start[B.n]; g += gridDim.x) {
+    const uint64_t ntiles = B.tile_start[B.n];
+    for (uint64_t g0 = blockIdx.x; g0 < ntiles; g0 += gridDim.x) {
+        const uint64_t g = B.tile_mul > 1 ? (g0 * B.tile_mul) % ntiles : g0;
         int r = 0;
         while (g >= B.tile_start[r + 1])
             r++;

@@ -688,6 +688,31 @@ int yaksa_unpack_stream(const void *inbuf, uintptr_t insize, void *outbuf, uintp
 /* batches: many independent requests, one launch for the byte-moving ones    */
 /* ------------------------------------------------------------------------- */
 
+static uint64_t gcd_u64(uint64_t a, uint64_t b)
+{
+    while (b) {
+        uint64_t t = a % b;
+        a = b;
+        b = t;
+    }
+    return a;
+}
+
+/* Tile order of a batch launch: multiplying by the integer nearest 0.618 x total that
+ * is coprime with the total (Fibonacci hashing) permutes the tiles so that every
+ * wave of CTAs holds tiles of every request in proportion to its size. */
+static uint32_t tile_multiplier(uint64_t total)
+{
+    if (total < 3)
+        return 1;
+    uint64_t m = (uint64_t) ((double) total * 0.6180339887498949);
+    if (m < 2)
+        m = 2;
+    while (gcd_u64(m, total) != 1)
+        m++;
+    return m < total && m <= 0xffffffffull ? (uint32_t) m : 1;
+}
+
 /* One launch per group of at most YK_BATCH_MAX requests of one shape class
  * (regular nests, everything else). */
 static int flush_class(yk_launch * ls, int n, int regular, cudaStream_t s)
@@ -706,6 +731,7 @@ static int flush_class(yk_launch * ls, int n, int regular, cudaStream_t s)
             B.tile_start[i + 1] = B.tile_start[i] +
                 yk_cuda_tiles(ls[i0 + i].nbytes / (uint64_t) ls[i0 + i].vec, u);
         }
+        B.tile_mul = m > 1 ? tile_multiplier(B.tile_start[m]) : 1;
         __atomic_add_fetch(&R.launches, 1, __ATOMIC_RELAXED);
         int rc = cuda_err((cudaError_t) yk_cuda_launch_batch(&B, u, regular, s), "batch launch");
         if (rc)
