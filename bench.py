@@ -88,6 +88,20 @@ class Clocks:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+class ColdL2:
+    """Between timed launches: write a buffer larger than L2 (the flush), then read a
+    second one, so that the timed launch starts with a cold L2 that holds no dirty lines
+    (otherwise the flush's own write-backs land inside the timed kernel)."""
+
+    def __init__(self, torch):
+        self.w = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+        self.r = torch.zeros(L2_FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+
+    def __call__(self):
+        self.w.zero_()
+        self.sink = self.r.sum()
+
+
 def make_faces(y, yk):
     return [(name, y.type_create_subarray([N, N, N], sub, st, yk.SUBARRAY_ORDER_C, yk.TYPE_FLOAT))
             for name, sub, st in FACES]
@@ -186,18 +200,25 @@ WORKLOAD = (f"halo3d: {N}^3 float32 grid, 6 depth-2 subarray faces ({2 * N * N *
 # byte comparison against the oracle and the oracle's own time on the host
 # ---------------------------------------------------------------------------
 
-def suite_types(y, yk, np, rng_seed=7):
-    """Seeded synthetic inputs with the shapes and distributions of each config."""
+def suite_types(y, yk, np, rng_seed=7, scale=1):
+    """Seeded synthetic inputs with the shapes and distributions of each config (scale > 1
+    divides the block and element counts, for profiler captures of the same kernels)."""
     rng = np.random.default_rng(rng_seed)
     out = {}
     # hvector of double: 4-column block of a 1024x16 row-major matrix
     out["hvector"] = dict(mk=lambda L: L.type_create_hvector(1024, 4, 128, yk.TYPE_DOUBLE),
-                          base="double", count=1, extent=1024 * 16 * 8)
+                          base="double", count=1, extent=1024 * 16 * 8, gran=8)
+    # halo faces of the 512^3 float grid, one per orientation (the +/- faces mirror them)
+    for name, sub, st in face_specs(512)[0::2]:
+        out["halo_" + name[0]] = dict(
+            mk=lambda L, sub=sub, st=st: L.type_create_subarray([512, 512, 512], sub, st,
+                                                                yk.SUBARRAY_ORDER_C, yk.TYPE_FLOAT),
+            base="float", count=1, extent=512 ** 3 * 4, gran=4)
     # hindexed int32: 2^20 blocks, lognormal lengths (median 16, sigma 1, clipped 1..4096),
     # non-overlapping blocks in shuffled order with random gaps inside 1 GiB
-    nb = 1 << 20
+    nb = (1 << 20) // scale
     blens = np.clip(np.round(np.exp(np.log(16) + rng.standard_normal(nb))), 1, 4096).astype(np.int64)
-    slots_total = (1 << 30) // 4
+    slots_total = (1 << 30) // 4 // scale
     free = slots_total - int(blens.sum())
     gaps = rng.integers(0, 2 * (free // nb), nb)
     order = rng.permutation(nb)
@@ -208,28 +229,30 @@ def suite_types(y, yk, np, rng_seed=7):
 
     def mk_hindexed(L):
         h = L.type_create_hindexed_arrays(nb, blens.ctypes.data, displs.ctypes.data, yk.TYPE_INT32_T)
-        r = L.type_create_resized(h, 0, 1 << 30)
+        r = L.type_create_resized(h, 0, (1 << 30) // scale)
         L.type_free(h)
         return r
-    out["hindexed"] = dict(mk=mk_hindexed, base="int32", count=1, extent=1 << 30,
-                           keep=(blens, displs))
+    out["hindexed"] = dict(mk=mk_hindexed, base="int32", count=1, extent=(1 << 30) // scale,
+                           keep=(blens, displs), gran=4)
 
     def mk_struct(L):
         s = L.type_create_struct([1, 3], [0, 8], [yk.TYPE_INT64_T, yk.TYPE_FLOAT])
         r = L.type_create_resized(s, 0, 32)
         L.type_free(s)
         return r
-    out["struct"] = dict(mk=mk_struct, base="float", count=8 << 20, extent=32 * (8 << 20))
+    out["struct"] = dict(mk=mk_struct, base="float", count=(8 << 20) // scale,
+                         extent=32 * (8 << 20) // scale, gran=20)
     # indexed_block: 2^22 blocks of 8 elements at sorted random element offsets
     for base, h, es, op in (("double", yk.TYPE_DOUBLE, 8, yk.OP_SUM),
                             ("int64", yk.TYPE_INT64_T, 8, yk.OP_MAX),
                             ("uint32", yk.TYPE_UINT32_T, 4, yk.OP_BXOR),
                             ("c_complex", yk.TYPE_C_COMPLEX, 8, yk.OP_PROD)):
-        nel = (256 << 20) // es
-        offs = np.sort(rng.integers(0, nel - 8, 1 << 22)).astype(np.int64)
+        nel = (256 << 20) // es // scale
+        nbk = (1 << 22) // scale
+        offs = np.sort(rng.integers(0, nel - 8, nbk)).astype(np.int64)
         out[f"reduce_{base}"] = dict(
-            mk=lambda L, offs=offs, h=h: L.type_create_indexed_block_array(1 << 22, 8, offs.ctypes.data, h),
-            base=base, count=1, extent=256 << 20, op=op, keep=(offs,))
+            mk=lambda L, offs=offs, h=h, nbk=nbk: L.type_create_indexed_block_array(nbk, 8, offs.ctypes.data, h),
+            base=base, count=1, extent=(256 << 20) // scale, op=op, keep=(offs,), gran=0)
     return out
 
 
@@ -248,7 +271,7 @@ def suite_fill(np, rng, base, nbytes):
     return rng.uniform(-1, 1, nbytes // 4).astype(np.float32).view(np.uint8)
 
 
-def run_suite(out_path, steps, cpu_seconds):
+def run_suite(out_path, steps, cpu_seconds, only=None, scale=1):
     import numpy as np
     import torch
     import yaksa_gb300 as yk
@@ -259,13 +282,16 @@ def run_suite(out_path, steps, cpu_seconds):
     y.init()
     o.init()
     hbm, peak_kind = peaks()
-    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    flush = ColdL2(torch)
     stream = torch.cuda.current_stream()
     sh = ctypes.c_void_p(stream.cuda_stream)
     shp = ctypes.addressof(sh)
     rng = np.random.default_rng(11)
+    threads = os.cpu_count() or 1
     lines = []
-    for name, w in suite_types(y, yk, np).items():
+    for name, w in suite_types(y, yk, np, scale=scale).items():
+        if only and name not in only:
+            continue
         tp, to = w["mk"](y), w["mk"](o)
         size = y.size(tp)
         count = w["count"]
@@ -296,10 +322,33 @@ def run_suite(out_path, steps, cpu_seconds):
                 o.unpack(ph.ctypes.data, P, th.ctypes.data, count, to, 0, op=op)
             cpu_t = time.perf_counter() - t0
             exact = (np.array_equal(typed_d.cpu().numpy(), th) and np.array_equal(packed_d.cpu().numpy(), ph))
+            # the oracle on every host core: the packed range split at multiples of the
+            # granule (builtin boundaries) through the API's offset/max-bytes arguments;
+            # not for overlapping targets, whose order only one thread keeps
+            cpu_nt, nt_exact = None, None
+            if w["gran"]:
+                th2, ph2 = typed_h.copy(), packed0.copy()
+                chunk = max(w["gran"], P // threads // w["gran"] * w["gran"])
+                ranges = [(a, min(chunk, P - a)) for a in range(0, P, chunk)]
+
+                def part(rs, th2=th2, ph2=ph2):
+                    for a, n in rs:
+                        if d == "pack":
+                            o.pack(th2.ctypes.data, count, to, a, ph2.ctypes.data + a, n, op=op)
+                        else:
+                            o.unpack(ph2.ctypes.data + a, n, th2.ctypes.data, count, to, a, op=op)
+                ths = [threading.Thread(target=part, args=(ranges[k::threads],)) for k in range(threads)]
+                t0 = time.perf_counter()
+                for x in ths:
+                    x.start()
+                for x in ths:
+                    x.join()
+                cpu_nt = time.perf_counter() - t0
+                nt_exact = bool(np.array_equal(th2, th) and np.array_equal(ph2, ph))
             # timing: fresh L2 each launch, CUDA events on the launching stream
             ts = []
             for rep in range(max(3, steps)):
-                flush.zero_()
+                flush()
                 e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 e0.record()
                 call()
@@ -313,7 +362,10 @@ def run_suite(out_path, steps, cpu_seconds):
                     "achieved_GBps": alg / t / 1e9, "hbm_frac": alg / t / 1e9 / hbm,
                     "peak": hbm, "peak_source": peak_kind, "bit_exact": bool(exact),
                     "cpu_oracle_s": cpu_t, "cpu_oracle_packed_GBps": P / cpu_t / 1e9,
-                    "gpu_over_cpu": cpu_t / t}
+                    "gpu_over_cpu": cpu_t / t,
+                    "cpu_oracle_threads": threads if cpu_nt else None,
+                    "cpu_oracle_nthr_packed_GBps": P / cpu_nt / 1e9 if cpu_nt else None,
+                    "cpu_nthr_same_bytes": nt_exact}
             lines.append(line)
             print(json.dumps(line), file=sys.stderr, flush=True)
         y.type_free(tp)
@@ -586,6 +638,9 @@ def main():
     ap.add_argument("--suite", default=None,
                     help="also run the hvector/hindexed/struct/reduction configs and write their "
                          "JSON lines to this file")
+    ap.add_argument("--suite-only", default=None, help="comma-separated suite workloads")
+    ap.add_argument("--suite-scale", type=int, default=1,
+                    help="divide the suite's block/element counts (profiler captures)")
     ap.add_argument("--stream", default=None,
                     help="run only the mixed request stream (plain vs server) and write its JSON")
     ap.add_argument("--stream-requests", type=int, default=10000)
@@ -596,7 +651,8 @@ def main():
     if args.suite:
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        run_suite(args.suite, args.steps, args.cpu_seconds)
+        run_suite(args.suite, args.steps, args.cpu_seconds,
+                  only=args.suite_only.split(",") if args.suite_only else None, scale=args.suite_scale)
         return
     if args.stream:
         import torch
@@ -631,7 +687,7 @@ def main():
     src = torch.rand(N * N * N, device="cuda", generator=g, dtype=torch.float32) * 2 - 1
     dst = torch.zeros_like(src)
     packed = [torch.empty(P, dtype=torch.uint8, device="cuda") for _ in faces]
-    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    flush = ColdL2(torch)
     stream = torch.cuda.current_stream()
     sh = ctypes.c_void_p(stream.cuda_stream)
     shp = ctypes.addressof(sh)
@@ -665,7 +721,7 @@ def main():
     def timed(fn, steps):
         tot = 0.0
         for _ in range(steps):
-            flush.zero_()
+            flush()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
             fn()
@@ -675,9 +731,9 @@ def main():
         return tot
 
     for _ in range(args.warmup):
-        flush.zero_()
+        flush()
         step_batched()
-        flush.zero_()
+        flush()
         step_plain()
     torch.cuda.synchronize()
 
@@ -685,7 +741,7 @@ def main():
     per = {"pack": [], "unpack": []}
     for rep in range(5):
         for d, arr in (("pack", pack_batch), ("unpack", unpack_batch)):
-            flush.zero_()
+            flush()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
             y.pup_batch_stream(arr, shp)
@@ -783,7 +839,8 @@ def main():
                        "path": "batched C-ABI (one launch per direction) captured once as a CUDA "
                                "graph and replayed per step",
                        "parallelism": f"replicas x{world}",
-                       "l2": "flushed between steps (512 MiB write outside the event-timed span)"},
+                       "l2": "flushed between steps outside the event-timed span: 512 MiB written, then "
+                             "512 MiB read so that no dirty flush lines remain"},
             "bit_exact": bool(ok),
             "plain_path": {"value": plain_value, "unit": "GB/s",
                            "ms_per_step": tot_plain / args.steps * 1e3,

@@ -105,6 +105,35 @@ def test_sorted_overlapping_blocks_sum(cuda, prod, oracle):
         oracle.type_free(to)
 
 
+@pytest.mark.parametrize("bl", [4, 8, 16])
+def test_sorted_blocks_segmented(cuda, prod, oracle, bl):
+    """Sorted overlapping fixed-length blocks unpacked in several calls whose ranges
+    start and end inside blocks: each call keeps the block order within its range."""
+    rng = np.random.default_rng(100 + bl)
+    nblk = 3000
+    for base, op in (("int8", "sum"), ("int16", "max"), ("float", "sum"), ("double", "prod"),
+                     ("c_double_complex", "sum"), ("int32", "replace"), ("int64", "bxor")):
+        offs = np.sort(rng.integers(0, nblk * bl // 2, nblk)).astype(np.int64)
+        h, es = BASE[base][0], BASE[base][1]
+        tp = prod.type_create_indexed_block_array(nblk, bl, offs.ctypes.data, h)
+        to = oracle.type_create_indexed_block_array(nblk, bl, offs.ctypes.data, h)
+        total = nblk * bl * es
+        packed = fill(rng, total, base)
+        target = fill(rng, (nblk * bl // 2 + bl) * es, base)
+        d_o = target.copy()
+        pk, dv = dev_copy(cuda, packed), dev_copy(cuda, target)
+        cuts = sorted(set(int(c) * es for c in rng.integers(1, total // es, 6)))
+        bounds = [0] + cuts + [total]
+        for s0, s1 in zip(bounds[:-1], bounds[1:]):
+            ao = oracle.unpack(packed.ctypes.data + s0, s1 - s0, d_o.ctypes.data, 1, to, s0,
+                               op=yk.OP_NAMES[op])
+            ap = prod.unpack(pk.data_ptr() + s0, s1 - s0, dv.data_ptr(), 1, tp, s0, op=yk.OP_NAMES[op])
+            assert ao == ap
+        assert_same_bytes(host_of(cuda, dv), d_o, f"bl {bl} {base} {op}", base)
+        prod.type_free(tp)
+        oracle.type_free(to)
+
+
 def test_nonblocking_and_stream(cuda, prod, oracle):
     t = prod.type_create_hvector(1024, 4, 128, yk.TYPE_DOUBLE)
     src = cuda.randn(1024 * 16, dtype=cuda.float64, device="cuda")

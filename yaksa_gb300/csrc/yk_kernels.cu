@@ -793,6 +793,92 @@ yk_owner_typed_kernel(const __grid_constant__ yk_launch L)
     }
 }
 
+/* Sorted blocks of a power-of-two byte length R, one packed element per lane (32-bit
+ * positions), operator fixed at compile time.  The ownership rule of yk_owner_kernel
+ * below: element x = disp[b] + j of block b belongs to b unless block b-1 covers x from
+ * a position inside the range; no earlier block can cover x when b-1 does not, because
+ * the displacements ascend.  The owner folds in the blocks b+1, b+2, ... that start at
+ * or before x, in block order.  Lanes of one block read the same displacement words
+ * (one broadcast per warp), packed elements are read contiguously across the warp and
+ * each block's target run is read and written by consecutive lanes. */
+template <int BT, int OP>
+__global__ void __launch_bounds__(YK_THREADS)
+yk_owner_lane_kernel(const __grid_constant__ yk_launch L, int rshift)
+{
+    typedef typename yk_elem<BT>::T T;
+    constexpr uint32_t es = (uint32_t) sizeof(T);
+    /* elements per lane, loads issued together (complex pairs keep one, within the
+     * register budget of full occupancy) */
+    constexpr int U = (BT == YK_BT_C32 || BT == YK_BT_C64) ? 1 : 2;
+    const uint32_t R = 1u << rshift;
+    const yk_level & lv = L.desc.lv[0];
+    const uint32_t p0 = (uint32_t) L.p0, p1 = (uint32_t) (L.p0 + L.nbytes);
+    const uint32_t nblk = (uint32_t) lv.count;
+    const uint32_t nunits = (uint32_t) (L.nbytes / es);
+    const T *packed = (const T *) L.packed;     /* element 0 is packed byte p0 */
+    char *typed = L.typed + L.desc.base;
+    const uint32_t nthr = gridDim.x * YK_THREADS;
+    for (uint32_t u0 = blockIdx.x * YK_THREADS + threadIdx.x; u0 < nunits; u0 += U * nthr) {
+        /* every load that does not depend on another first: the block's displacement,
+         * its predecessor's and successor's, and the packed element */
+        int64_t x[U], dn[U];
+        uint32_t b[U];
+        bool own[U];
+        T in[U], out[U], in1[U];
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            const uint32_t u = u0 + k * nthr;
+            own[k] = u < nunits;
+            if (!own[k])
+                continue;
+            const uint32_t p = p0 + u * es;
+            b[k] = p >> rshift;
+            const int64_t d = __ldg(lv.disp + b[k]);
+            const int64_t dp = b[k] > 0 ? __ldg(lv.disp + b[k] - 1) : 0;
+            dn[k] = b[k] + 1 < nblk ? __ldg(lv.disp + b[k] + 1) : INT64_MAX;
+            in[k] = __ldg(packed + u);
+            x[k] = d + (int64_t) (p & (R - 1));
+            /* an earlier in-range block owns this element */
+            if (b[k] > 0 && x[k] < dp + (int64_t) R && (b[k] - 1) * R + (uint32_t) (x[k] - dp) >= p0)
+                own[k] = false;
+        }
+        /* then the target element and the next block's contribution, if any */
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            if (!own[k])
+                continue;
+            out[k] = *(const T *) (typed + x[k]);
+            if (dn[k] <= x[k]) {
+                const uint64_t pp = ((uint64_t) (b[k] + 1) << rshift) + (uint64_t) (x[k] - dn[k]);
+                if (pp < p1)
+                    in1[k] = __ldg(packed + ((uint32_t) pp - p0) / es);
+                else
+                    dn[k] = INT64_MAX;
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            if (!own[k])
+                continue;
+            yk_elem<BT>::op(OP, in[k], out[k]);
+            if (dn[k] <= x[k]) {
+                yk_elem<BT>::op(OP, in1[k], out[k]);
+                /* rarer: the blocks after that, in block order */
+                for (uint32_t bb = b[k] + 2; bb < nblk; bb++) {
+                    const int64_t d2 = __ldg(lv.disp + bb);
+                    if (d2 > x[k])
+                        break;
+                    const uint64_t pp = ((uint64_t) bb << rshift) + (uint64_t) (x[k] - d2);
+                    if (pp >= p1)
+                        break;  /* later blocks place x later still */
+                    yk_elem<BT>::op(OP, __ldg(packed + ((uint32_t) pp - p0) / es), out[k]);
+                }
+            }
+            *(T *) (typed + x[k]) = out[k];
+        }
+    }
+}
+
 /* Sorted blocks: descriptor = IDX(nblk, disp sorted ascending, cps = R) over a run of
  * R bytes of one base type.  Every target element that receives data gets exactly one
  * owner: the thread of its first in-range contributor, which applies the
@@ -1389,6 +1475,55 @@ extern "C" int yk_cuda_launch_pup(const yk_launch * l, void *stream)
     return (int) cudaGetLastError();
 }
 
+/* yk_owner_lane_kernel for (base type, operator) pairs in the operator table; false
+ * when the pair has no instance (the caller falls back to the runtime-op kernels) */
+template <int BT>
+static bool yk_owner_lane_int(const yk_launch & c, int rshift, cudaStream_t s, unsigned g)
+{
+    switch ((int) c.op) {
+#define YK_OL(O) case O: yk_owner_lane_kernel<BT, O><<<g, YK_THREADS, 0, s>>>(c, rshift); return true
+        YK_OL(OP_MAX); YK_OL(OP_MIN); YK_OL(OP_SUM); YK_OL(OP_PROD); YK_OL(OP_LAND); YK_OL(OP_BAND);
+        YK_OL(OP_LOR); YK_OL(OP_BOR); YK_OL(OP_LXOR); YK_OL(OP_BXOR); YK_OL(OP_REPLACE);
+    }
+    return false;
+}
+
+template <int BT>
+static bool yk_owner_lane_flt(const yk_launch & c, int rshift, cudaStream_t s, unsigned g)
+{
+    switch ((int) c.op) {
+        YK_OL(OP_MAX); YK_OL(OP_MIN); YK_OL(OP_SUM); YK_OL(OP_PROD); YK_OL(OP_REPLACE);
+    }
+    return false;
+}
+
+template <int BT>
+static bool yk_owner_lane_cplx(const yk_launch & c, int rshift, cudaStream_t s, unsigned g)
+{
+    switch ((int) c.op) {
+        YK_OL(OP_SUM); YK_OL(OP_PROD); YK_OL(OP_REPLACE);
+#undef YK_OL
+    }
+    return false;
+}
+
+static bool yk_owner_lane_launch(const yk_launch & c, int bt, int rshift, cudaStream_t s)
+{
+    const uint64_t units = c.nbytes / (uint64_t) yk_bt_size(bt);
+    const unsigned g = yk_grid(units, YK_THREADS, 16);
+    switch (bt) {
+        case YK_BT_I8: return yk_owner_lane_int<YK_BT_I8>(c, rshift, s, g);
+        case YK_BT_I16: return yk_owner_lane_int<YK_BT_I16>(c, rshift, s, g);
+        case YK_BT_I32: return yk_owner_lane_int<YK_BT_I32>(c, rshift, s, g);
+        case YK_BT_I64: return yk_owner_lane_int<YK_BT_I64>(c, rshift, s, g);
+        case YK_BT_F32: return yk_owner_lane_flt<YK_BT_F32>(c, rshift, s, g);
+        case YK_BT_F64: return yk_owner_lane_flt<YK_BT_F64>(c, rshift, s, g);
+        case YK_BT_C32: return yk_owner_lane_cplx<YK_BT_C32>(c, rshift, s, g);
+        case YK_BT_C64: return yk_owner_lane_cplx<YK_BT_C64>(c, rshift, s, g);
+    }
+    return false;
+}
+
 extern "C" int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blocks, void *stream)
 {
     cudaStream_t s = (cudaStream_t) stream;
@@ -1399,7 +1534,13 @@ extern "C" int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blo
     bool typed_ok = sorted_blocks == 2 && (bt == YK_BT_I8 || bt == YK_BT_I16 || bt == YK_BT_I32 ||
                                            bt == YK_BT_I64 || bt == YK_BT_F32 || bt == YK_BT_F64 ||
                                            bt == YK_BT_C32 || bt == YK_BT_C64);
-    if (typed_ok) {
+    const uint64_t R = c.desc.lv[0].cps;
+    int rshift = 0;
+    while (rshift < 31 && (1ull << rshift) < R)
+        rshift++;
+    if (typed_ok && !c.use64 && (1ull << rshift) == R && yk_owner_lane_launch(c, bt, rshift, s)) {
+        /* launched: power-of-two blocks, operator in the type's table */
+    } else if (typed_ok) {
         uint64_t units = c.nbytes / (uint64_t) yk_bt_size(bt);
         unsigned g = yk_grid(units, YK_THREADS * 4, 8);
 #define YK_OT(IDX) do { switch (bt) {                                                          \
