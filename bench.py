@@ -787,6 +787,10 @@ def main():
     hbm, peak_kind = peaks()
     # dominant kernel: yk_batch_regular_kernel; algorithmic bytes = 2 per packed byte per launch
     alg = 2 * P * len(faces)
+    # DRAM traffic of the same launches from one ncu capture on a 384^3 grid
+    # (dram__bytes_read.sum + dram__bytes_write.sum, pack 41.81 MB, unpack 16.14 MB),
+    # scaled by the packed bytes to this grid
+    traffic = (41.814e6 + 16.137e6) / 2 * (N / 384) ** 2
     med = {d: statistics.median(v) for d, v in per.items()}
     mean_launch = (med["pack"] + med["unpack"]) / 2
     achieved = alg / mean_launch / 1e9
@@ -850,7 +854,9 @@ def main():
                                    "note": "yaksa_gb300_pup_batch_stream per direction, host "
                                            "planning inside the timed span"},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": None,
+                         "frac": achieved / hbm, "traffic": traffic,
+                         "traffic_source": "ncu capture of the same kernel on a 384^3 grid, "
+                                           "scaled by packed bytes (profiles/yk_batch_regular_kernel_halo3d.md)",
                          "kernel": "yk_batch_regular_kernel (6 faces per launch; mean of pack and unpack)",
                          "peak_source": peak_kind,
                          "launch_us": {d: v * 1e6 for d, v in med.items()},

@@ -351,6 +351,81 @@ yk_hidx_kernel(const __grid_constant__ yk_launch L)
     }
 }
 
+/* The same walk for requests under 4 GiB, in packed positions relative to each group's
+ * first byte: 32-bit search keys (one shuffle per step instead of two) and per-lane
+ * state small enough for every warp slot of the SM to stay resident.  Lane k keeps its
+ * block's start relative to the group (0 for a block that starts before the range) and
+ * the typed offset of relative position 0 in that block, so a unit's typed offset is one
+ * shuffle and one add. */
+template <int V, int DIR>
+__global__ void __launch_bounds__(YK_THREADS)
+yk_hidx32_kernel(const __grid_constant__ yk_launch L)
+{
+    typedef typename yk_vec<V>::T VT;
+    const yk_level *lv = &L.desc.lv[0];
+    const uint64_t p0 = L.p0, p1 = L.p0 + L.nbytes;
+    const int lane = threadIdx.x & 31;
+    const uint64_t warp = ((uint64_t) blockIdx.x * YK_THREADS + threadIdx.x) >> 5;
+    const uint64_t nwarps = ((uint64_t) gridDim.x * YK_THREADS) >> 5;
+    char *typed = L.typed + L.desc.base;
+    const uint64_t jb = yk_hidx_block(lv, p0), je = yk_hidx_block(lv, p1 - 1);
+    const uint64_t ngroups = (je - jb + 32) / 32;
+    for (uint64_t g = warp; g < ngroups; g += nwarps) {
+        const uint64_t j0 = jb + g * 32;
+        const uint64_t jl = j0 + (uint64_t) lane;
+        const uint64_t jend = min(j0 + 32, je + 1);
+        const uint64_t gs = max(__ldg(lv->pfx + j0), p0);
+        const uint32_t n = (uint32_t) (min(__ldg(lv->pfx + jend), p1) - gs);
+        uint32_t my_rel = 0xffffffffu;
+        int64_t my_adj = 0;
+        if (jl < jend) {
+            const uint64_t bp = __ldg(lv->pfx + jl);
+            my_rel = bp <= gs ? 0u : (uint32_t) (bp - gs);
+            my_adj = __ldg(lv->disp + jl) - ((int64_t) bp - (int64_t) gs);
+        }
+        VT *pk = (VT *) (L.packed + (gs - p0));
+        for (uint32_t base = 0; base < n; base += 32u * V * YK_HW_UNROLL) {
+            int64_t off[YK_HW_UNROLL];
+            bool act[YK_HW_UNROLL];
+#pragma unroll
+            for (int k = 0; k < YK_HW_UNROLL; k++) {
+                const uint32_t r = base + (uint32_t) (k * 32 + lane) * V;
+                act[k] = r < n;
+                int idx = 0;
+#pragma unroll
+                for (int step = 16; step > 0; step >>= 1) {
+                    const uint32_t c = __shfl_sync(0xffffffffu, my_rel, idx + step);
+                    if (c <= r)
+                        idx += step;
+                }
+                off[k] = __shfl_sync(0xffffffffu, my_adj, idx) + (int64_t) r;
+            }
+            if (DIR == 0) {
+                VT v[YK_HW_UNROLL];
+#pragma unroll
+                for (int k = 0; k < YK_HW_UNROLL; k++)
+                    if (act[k])
+                        v[k] = yk_ldcg((const VT *) (typed + off[k]));
+#pragma unroll
+                for (int k = 0; k < YK_HW_UNROLL; k++)
+                    if (act[k])
+                        pk[base / V + (uint32_t) (k * 32 + lane)] = v[k];
+            } else {
+                VT v[YK_HW_UNROLL];
+#pragma unroll
+                for (int k = 0; k < YK_HW_UNROLL; k++)
+                    if (act[k])
+                        v[k] = yk_ldcg(pk + base / V + (uint32_t) (k * 32 + lane));
+#pragma unroll
+                for (int k = 0; k < YK_HW_UNROLL; k++)
+                    if (act[k])
+                        *(VT *) (typed + off[k]) = v[k];
+            }
+        }
+    }
+}
+
+
 template <typename IDX, int V, int DIR, int U>
 __global__ void __launch_bounds__(YK_THREADS)
 yk_bytes_kernel(const __grid_constant__ yk_launch L)
@@ -1441,7 +1516,10 @@ extern "C" int yk_cuda_launch_pup(const yk_launch * l, void *stream)
         uint64_t ctas = (groups + (YK_THREADS / 32) - 1) / (YK_THREADS / 32);
         uint64_t cap = (uint64_t) yk_cuda_num_sms() * 8u;
         unsigned g = (unsigned) (ctas < cap ? (ctas ? ctas : 1) : cap);
-#define YK_H(V) do { if (l->dir == 0) yk_hidx_kernel<V, 0><<<g, YK_THREADS, 0, s>>>(*l); \
+#define YK_H(V) do { if (l->nbytes <= 0xffffffffull) {                                     \
+                         if (l->dir == 0) yk_hidx32_kernel<V, 0><<<g, YK_THREADS, 0, s>>>(*l); \
+                         else yk_hidx32_kernel<V, 1><<<g, YK_THREADS, 0, s>>>(*l);            \
+                     } else if (l->dir == 0) yk_hidx_kernel<V, 0><<<g, YK_THREADS, 0, s>>>(*l); \
                      else yk_hidx_kernel<V, 1><<<g, YK_THREADS, 0, s>>>(*l); } while (0)
         switch (l->vec) {
             case 16: YK_H(16); break;
