@@ -95,7 +95,7 @@ class ColdL2:
 
     def __init__(self, torch):
         self.w = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
-        self.r = torch.zeros(L2_FLUSH_BYTES // 4, dtype=torch.int32, device="cuda")
+        self.r = torch.zeros(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
 
     def __call__(self):
         self.w.zero_()
