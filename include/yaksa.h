@@ -211,14 +211,18 @@ int yaksa_unpack_stream(const void *inbuf, uintptr_t insize, void *outbuf, uintp
                         yaksa_type_t type, uintptr_t outoffset, uintptr_t * actual_unpack_bytes,
                         yaksa_info_t info, yaksa_op_t op, void *stream);
 
-/* Contiguous-segment lists (yaksa.h.in:584-609). */
+/* Contiguous-segment lists (yaksa.h.in:584-609): the pieces of `count` elements in
+ * typemap order, with the reference's piece boundaries.  yaksa_iov_len_max reports the
+ * leading pieces whose bytes fit in max_iov_bytes, never splitting one builtin. */
 int yaksa_iov_len(uintptr_t count, yaksa_type_t type, uintptr_t * iov_len);
 int yaksa_iov_len_max(uintptr_t count, yaksa_type_t type, uintptr_t max_iov_bytes,
                       uintptr_t * iov_len, uintptr_t * actual_iov_bytes);
 int yaksa_iov(const char *buf, uintptr_t count, yaksa_type_t type, uintptr_t iov_offset,
               struct iovec *iov, uintptr_t max_iov_len, uintptr_t * actual_iov_len);
 
-/* Type serialisation (yaksa.h.in:618-634). */
+/* Type serialisation (yaksa.h.in:618-634).  The flattened bytes hold no pointers, so
+ * they can be sent to another process running this library; yaksa_unflatten creates a
+ * new handle with the same bounds, typemap and segment list. */
 int yaksa_flatten_size(yaksa_type_t type, uintptr_t * flattened_type_size);
 int yaksa_flatten(yaksa_type_t type, void *flattened_type);
 int yaksa_unflatten(yaksa_type_t * type, const void *flattened_type);

@@ -1427,7 +1427,7 @@ int yaksa_oracle_byte_offsets(yaksa_type_t type, uintptr_t count, int64_t * out)
 }
 
 /* ------------------------------------------------------------------------- */
-/* iov and flatten: not part of the pack/unpack oracle yet                   */
+/* segment lists (src/frontend/iov/yaksa_iov.c, yaksa_iov_len.c)              */
 /* ------------------------------------------------------------------------- */
 
 int yaksa_iov_len(uintptr_t count, yaksa_type_t type, uintptr_t * iov_len)
@@ -1438,47 +1438,343 @@ int yaksa_iov_len(uintptr_t count, yaksa_type_t type, uintptr_t * iov_len)
     return YAKSA_SUCCESS;
 }
 
-int yaksa_iov_len_max(uintptr_t count, yaksa_type_t type, uintptr_t max_iov_bytes,
-                      uintptr_t * iov_len, uintptr_t * actual_iov_bytes)
+/* first field size, second field offset and size of a pair builtin */
+static int o_pair_layout(yaksa_type_t h, size_t * s1, size_t * off2, size_t * s2)
 {
-    (void) count;
-    (void) type;
-    (void) max_iov_bytes;
-    *iov_len = 0;
-    *actual_iov_bytes = 0;
-    return YAKSA_ERR__NOT_SUPPORTED;
+#define PL(T1, T2) do { struct pl_ { T1 x; T2 y; }; *s1 = sizeof(T1);              \
+        *off2 = offsetof(struct pl_, y); *s2 = sizeof(T2); return 1; } while (0)
+    switch (h) {
+        case YAKSA_TYPE__FLOAT_INT:
+            PL(float, int);
+        case YAKSA_TYPE__DOUBLE_INT:
+            PL(double, int);
+        case YAKSA_TYPE__LONG_INT:
+            PL(long, int);
+        case YAKSA_TYPE__SHORT_INT:
+            PL(short, int);
+        case YAKSA_TYPE__LONG_DOUBLE_INT:
+            PL(long double, int);
+        default:
+            return 0;
+    }
+#undef PL
+}
+
+/* yaksi_iov (yaksa_iov.c:48-359): returns entries written at iov[0..) */
+static int o_iov(const char *buf, uintptr_t count, const otype * t, uintptr_t off,
+                 struct iovec *iov, uintptr_t max, uintptr_t * got)
+{
+    *got = 0;
+    if (max == 0)
+        return YAKSA_SUCCESS;
+    if (t->is_contig) {         /* :64-73, the offset is not applied */
+        iov[0].iov_base = (char *) buf + t->true_lb;
+        iov[0].iov_len = count * t->size;
+        *got = 1;
+        return YAKSA_SUCCESS;
+    }
+    if (off >= count * t->num_contig)
+        return YAKSA_SUCCESS;
+    if (t->kind == OK_BUILTIN) {        /* BUILTIN_PAIRTYPE_IOV, :12-46 */
+        size_t s1, off2, s2;
+        if (!o_pair_layout(t->builtin, &s1, &off2, &s2))
+            return YAKSA_ERR__INTERNAL;
+        if (off2 == s1) {
+            const char *z = buf + off * (uintptr_t) t->extent;
+            uintptr_t n = OMIN(max, count - off);
+            for (uintptr_t x = 0; x < n; x++, z += t->extent) {
+                iov[x].iov_base = (char *) z;
+                iov[x].iov_len = s1 + s2;
+            }
+            *got = n;
+        } else {
+            if (off % 2)
+                return YAKSA_ERR__INTERNAL;
+            const char *z = buf + off * (uintptr_t) t->extent / 2;
+            uintptr_t n = OMIN(max - 1, count * 2 - off);
+            for (uintptr_t x = 0; x < n; x += 2, z += t->extent) {
+                iov[x].iov_base = (char *) z;
+                iov[x].iov_len = s1;
+                iov[x + 1].iov_base = (char *) z + off2;
+                iov[x + 1].iov_len = s2;
+                *got += 2;
+            }
+        }
+        return YAKSA_SUCCESS;
+    }
+    if (t->kind == OK_CONTIG)
+        return o_iov(buf, count * (uintptr_t) t->count, t->child, off, iov, max, got);
+
+    /* every other kind: a sequence of (address, child count, child) blocks per element */
+    uintptr_t rem = max, roff = off;
+    struct iovec *out = iov;
+    const char *sub0 = t->kind == OK_SUBARRAY ? buf + t->true_lb - t->primary->true_lb : buf;
+    intptr_t nblk = (t->kind == OK_RESIZED || t->kind == OK_SUBARRAY) ? 1 : t->count;
+    for (uintptr_t i = 0; i < count; i++) {
+        for (intptr_t j = 0; j < nblk; j++) {
+            const otype *ch;
+            uintptr_t n;
+            const char *p;
+            switch (t->kind) {
+                case OK_RESIZED:
+                    ch = t->child, n = 1, p = buf + (intptr_t) i * t->extent;
+                    break;
+                case OK_SUBARRAY:
+                    ch = t->primary, n = 1, p = sub0 + (intptr_t) i * t->extent;
+                    break;
+                case OK_HVECTOR:
+                    ch = t->child, n = (uintptr_t) t->blocklength;
+                    p = buf + (intptr_t) i * t->extent + j * t->stride;
+                    break;
+                case OK_BLKHINDX:
+                    ch = t->child, n = (uintptr_t) t->blocklength;
+                    p = buf + (intptr_t) i * t->extent + t->displs[j];
+                    break;
+                case OK_HINDEXED:
+                    ch = t->child, n = (uintptr_t) t->blens[j];
+                    p = buf + (intptr_t) i * t->extent + t->displs[j];
+                    break;
+                default:       /* OK_STRUCT */
+                    ch = t->types[j], n = (uintptr_t) t->blens[j];
+                    p = buf + (intptr_t) i * t->extent + t->displs[j];
+                    break;
+            }
+            if (n == 0 && (t->kind == OK_HINDEXED || t->kind == OK_STRUCT))
+                continue;
+            uintptr_t k = ch->is_contig ? 1 : n * ch->num_contig;
+            if (roff >= k) {
+                roff -= k;
+                continue;
+            }
+            uintptr_t g;
+            int rc = o_iov(p, n, ch, roff, out, rem, &g);
+            if (rc)
+                return rc;
+            out += g;
+            rem -= g;
+            *got += g;
+            roff = 0;
+            /* the reference stops at a full list for every kind but subarray,
+             * whose loop runs on and lists nothing more (:331-354) */
+            if (rem == 0)
+                return YAKSA_SUCCESS;
+        }
+    }
+    return YAKSA_SUCCESS;
 }
 
 int yaksa_iov(const char *buf, uintptr_t count, yaksa_type_t type, uintptr_t iov_offset,
               struct iovec *iov, uintptr_t max_iov_len, uintptr_t * actual_iov_len)
 {
-    (void) buf;
-    (void) count;
-    (void) type;
-    (void) iov_offset;
-    (void) iov;
-    (void) max_iov_len;
-    *actual_iov_len = 0;
-    return YAKSA_ERR__NOT_SUPPORTED;
+    GET_OR_FAIL(type, t);
+    return o_iov(buf, count, t, iov_offset, iov, max_iov_len, actual_iov_len);
+}
+
+/* yaksi_iov_len_sub (yaksa_iov_len_max.c:20-148): pieces of the first element that
+ * does not fit whole, taken while they fit.  Two deliberate differences, both so that
+ * the count agrees with the list yaksa_iov returns: the block length of a contiguous
+ * child is the type's own (the reference reads the child's union member, :59-69), and
+ * zero-length hindexed/struct blocks are skipped as yaksa_iov skips them. */
+static void o_len_sub(const otype * t, uintptr_t * rem, uintptr_t * len)
+{
+    if (t->num_contig == 1 || t->kind == OK_BUILTIN)
+        return;         /* whole elements and whole pieces only */
+    switch (t->kind) {
+        case OK_CONTIG:
+        case OK_HVECTOR:
+        case OK_BLKHINDX:
+        case OK_HINDEXED:{
+                const otype *c = t->child;
+                if (c->is_contig) {
+                    if (t->kind == OK_HINDEXED) {
+                        for (intptr_t i = 0; i < t->count; i++) {
+                            uintptr_t sub = c->size * (uintptr_t) t->blens[i];
+                            if (t->blens[i] == 0)
+                                continue;
+                            if (*rem < sub)
+                                break;
+                            *rem -= sub;
+                            *len += 1;
+                        }
+                    } else {
+                        uintptr_t sub = c->size * (uintptr_t) t->blocklength;
+                        uintptr_t n = *rem / sub;
+                        *rem -= n * sub;
+                        *len += n;
+                    }
+                } else {
+                    uintptr_t n = *rem / c->size;
+                    *rem -= n * c->size;
+                    *len += n * c->num_contig;
+                    o_len_sub(c, rem, len);
+                }
+                return;
+            }
+        case OK_STRUCT:
+            for (intptr_t i = 0; i < t->count; i++) {
+                const otype *c = t->types[i];
+                uintptr_t n = (uintptr_t) t->blens[i];
+                if (n == 0)
+                    continue;
+                if (c->is_contig) {
+                    if (*rem < n * c->size)
+                        return;
+                    *rem -= n * c->size;
+                    *len += 1;
+                } else if (*rem >= n * c->size) {
+                    *rem -= n * c->size;
+                    *len += n * c->num_contig;
+                } else {
+                    n = *rem / c->size;
+                    *rem -= n * c->size;
+                    *len += n * c->num_contig;
+                    o_len_sub(c, rem, len);
+                    return;
+                }
+            }
+            return;
+        case OK_RESIZED:
+            o_len_sub(t->child, rem, len);
+            return;
+        case OK_SUBARRAY:
+            o_len_sub(t->primary, rem, len);
+            return;
+    }
+}
+
+/* yaksi_iov_len_max (yaksa_iov_len_max.c:151-193) */
+int yaksa_iov_len_max(uintptr_t count, yaksa_type_t type, uintptr_t max_iov_bytes,
+                      uintptr_t * iov_len, uintptr_t * actual_iov_bytes)
+{
+    GET_OR_FAIL(type, t);
+    if (t->is_contig) {
+        int fits = max_iov_bytes >= count * t->size;
+        *iov_len = fits;
+        *actual_iov_bytes = fits ? count * t->size : 0;
+        return YAKSA_SUCCESS;
+    }
+    if (max_iov_bytes >= count * t->size) {
+        *iov_len = count * t->num_contig;
+        *actual_iov_bytes = count * t->size;
+        return YAKSA_SUCCESS;
+    }
+    uintptr_t rem = max_iov_bytes, len = 0;
+    uintptr_t n = t->size ? rem / t->size : 0;
+    rem -= n * t->size;
+    len += n * t->num_contig;
+    o_len_sub(t, &rem, &len);
+    *iov_len = len;
+    *actual_iov_bytes = max_iov_bytes - rem;
+    return YAKSA_SUCCESS;
+}
+
+/* ------------------------------------------------------------------------- */
+/* flatten / unflatten: a serialisation of the oracle's own type tree (the      */
+/* reference copies its in-memory objects, src/frontend/flatten/); the bytes  */
+/* only have to round-trip through this library                               */
+/* ------------------------------------------------------------------------- */
+
+static uintptr_t o_flat_size(const otype * t)
+{
+    uintptr_t n = sizeof(otype);
+    switch (t->kind) {
+        case OK_CONTIG:
+        case OK_RESIZED:
+        case OK_HVECTOR:
+            return n + o_flat_size(t->child);
+        case OK_BLKHINDX:
+            return n + t->count * sizeof(intptr_t) + o_flat_size(t->child);
+        case OK_HINDEXED:
+            return n + 2 * t->count * sizeof(intptr_t) + o_flat_size(t->child);
+        case OK_STRUCT:
+            n += 2 * t->count * sizeof(intptr_t);
+            for (intptr_t i = 0; i < t->count; i++)
+                n += o_flat_size(t->types[i]);
+            return n;
+        case OK_SUBARRAY:
+            return n + o_flat_size(t->primary);
+        default:
+            return n;
+    }
+}
+
+static char *o_flat_put(const otype * t, char *p)
+{
+    memcpy(p, t, sizeof(otype));
+    p += sizeof(otype);
+    if (t->kind == OK_HINDEXED || t->kind == OK_STRUCT) {
+        memcpy(p, t->blens, t->count * sizeof(intptr_t));
+        p += t->count * sizeof(intptr_t);
+    }
+    if (t->kind == OK_BLKHINDX || t->kind == OK_HINDEXED || t->kind == OK_STRUCT) {
+        memcpy(p, t->displs, t->count * sizeof(intptr_t));
+        p += t->count * sizeof(intptr_t);
+    }
+    if (t->kind == OK_STRUCT) {
+        for (intptr_t i = 0; i < t->count; i++)
+            p = o_flat_put(t->types[i], p);
+        return p;
+    }
+    if (t->kind == OK_SUBARRAY)
+        return o_flat_put(t->primary, p);
+    if (t->kind != OK_BUILTIN)
+        return o_flat_put(t->child, p);
+    return p;
+}
+
+static otype *o_flat_get(const char **pp)
+{
+    otype tmp;
+    memcpy(&tmp, *pp, sizeof(otype));
+    *pp += sizeof(otype);
+    if (tmp.kind == OK_BUILTIN) {
+        otype *b = o_get(tmp.builtin);
+        o_ref(b);
+        return b;
+    }
+    otype *t = o_new(tmp.kind);
+    *t = tmp;
+    t->refcount = 1;
+    size_t arr = (size_t) t->count * sizeof(intptr_t);
+    if (t->kind == OK_HINDEXED || t->kind == OK_STRUCT) {
+        t->blens = malloc(arr ? arr : 1);
+        memcpy(t->blens, *pp, arr);
+        *pp += arr;
+    }
+    if (t->kind == OK_BLKHINDX || t->kind == OK_HINDEXED || t->kind == OK_STRUCT) {
+        t->displs = malloc(arr ? arr : 1);
+        memcpy(t->displs, *pp, arr);
+        *pp += arr;
+    }
+    if (t->kind == OK_STRUCT) {
+        t->types = malloc((t->count ? t->count : 1) * sizeof(otype *));
+        for (intptr_t i = 0; i < t->count; i++)
+            t->types[i] = o_flat_get(pp);
+    } else if (t->kind == OK_SUBARRAY) {
+        t->primary = o_flat_get(pp);
+    } else {
+        t->child = o_flat_get(pp);
+    }
+    return t;
 }
 
 int yaksa_flatten_size(yaksa_type_t type, uintptr_t * flattened_type_size)
 {
-    (void) type;
-    *flattened_type_size = 0;
-    return YAKSA_ERR__NOT_SUPPORTED;
+    GET_OR_FAIL(type, t);
+    *flattened_type_size = o_flat_size(t);
+    return YAKSA_SUCCESS;
 }
 
 int yaksa_flatten(yaksa_type_t type, void *flattened_type)
 {
-    (void) type;
-    (void) flattened_type;
-    return YAKSA_ERR__NOT_SUPPORTED;
+    GET_OR_FAIL(type, t);
+    o_flat_put(t, (char *) flattened_type);
+    return YAKSA_SUCCESS;
 }
 
 int yaksa_unflatten(yaksa_type_t * type, const void *flattened_type)
 {
-    (void) flattened_type;
-    *type = YAKSA_TYPE__NULL;
-    return YAKSA_ERR__NOT_SUPPORTED;
+    const char *p = (const char *) flattened_type;
+    *type = o_handle_alloc(o_flat_get(&p));
+    return YAKSA_SUCCESS;
 }

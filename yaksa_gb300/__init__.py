@@ -92,7 +92,17 @@ _PROTOS = {
     "yaksa_unpack_stream": (ctypes.c_int, [_vp, _up, _vp, _up, _u64, _up, ctypes.POINTER(_up), _vp,
                                            _u64, _vp]),
     "yaksa_iov_len": (ctypes.c_int, [_up, _u64, ctypes.POINTER(_up)]),
+    "yaksa_iov_len_max": (ctypes.c_int, [_up, _u64, _up, ctypes.POINTER(_up), ctypes.POINTER(_up)]),
+    "yaksa_iov": (ctypes.c_int, [_vp, _up, _u64, _up, _vp, _up, ctypes.POINTER(_up)]),
+    "yaksa_flatten_size": (ctypes.c_int, [_u64, ctypes.POINTER(_up)]),
+    "yaksa_flatten": (ctypes.c_int, [_u64, _vp]),
+    "yaksa_unflatten": (ctypes.c_int, [ctypes.POINTER(_u64), _vp]),
 }
+
+
+class IoVec(ctypes.Structure):
+    """struct iovec"""
+    _fields_ = [("iov_base", _vp), ("iov_len", _up)]
 
 
 class PupOp(ctypes.Structure):
@@ -340,6 +350,33 @@ class Yaksa:
         n = _up()
         self._chk("yaksa_iov_len", self.lib.yaksa_iov_len(count, t, ctypes.byref(n)))
         return n.value
+
+    def iov_len_max(self, count, t, max_bytes):
+        n, b = _up(), _up()
+        self._chk("yaksa_iov_len_max", self.lib.yaksa_iov_len_max(count, t, max_bytes, ctypes.byref(n),
+                                                                   ctypes.byref(b)))
+        return n.value, b.value
+
+    def iov(self, buf, count, t, offset, max_len):
+        """yaksa_iov; returns a list of (address, length)."""
+        arr = (IoVec * max(1, max_len))()
+        n = _up()
+        self._chk("yaksa_iov", self.lib.yaksa_iov(buf, count, t, offset, arr, max_len, ctypes.byref(n)))
+        return [(arr[i].iov_base or 0, arr[i].iov_len) for i in range(n.value)]
+
+    def flatten(self, t):
+        """yaksa_flatten_size + yaksa_flatten; returns the bytes."""
+        n = _up()
+        self._chk("yaksa_flatten_size", self.lib.yaksa_flatten_size(t, ctypes.byref(n)))
+        buf = ctypes.create_string_buffer(max(1, n.value))
+        self._chk("yaksa_flatten", self.lib.yaksa_flatten(t, buf))
+        return buf.raw[:n.value]
+
+    def unflatten(self, data):
+        buf = ctypes.create_string_buffer(data, len(data))
+        h = _u64()
+        self._chk("yaksa_unflatten", self.lib.yaksa_unflatten(ctypes.byref(h), buf))
+        return h.value
 
     # pack / unpack: pointers are plain integers (device or host addresses)
     def ipack(self, inbuf, incount, t, inoffset, outbuf, max_bytes, op=OP_REPLACE, info=None):

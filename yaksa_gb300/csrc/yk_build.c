@@ -117,7 +117,7 @@ static void add_seg(hbuild * b, int64_t off, uint64_t len, int bt)
 }
 
 /* field layout of a pair builtin: (offset, size, base type) x 2 */
-static int pair_fields(yaksa_type_t h, size_t off[2], size_t sz[2], int bt[2])
+int yk_pair_fields(yaksa_type_t h, size_t off[2], size_t sz[2], int bt[2])
 {
 #define PF(T1, B1, T2, B2) do { struct p_ { T1 x; T2 y; };                        \
         off[0] = 0; sz[0] = sizeof(T1); bt[0] = B1;                               \
@@ -155,7 +155,7 @@ static void emit_builtin(hbuild * b, const yk_type * t, int64_t off)
 {
     size_t fo[2], fs[2];
     int fb[2];
-    if (pair_fields(t->builtin, fo, fs, fb)) {
+    if (yk_pair_fields(t->builtin, fo, fs, fb)) {
         add_seg(b, off + (int64_t) fo[0], fs[0], fb[0]);
         add_seg(b, off + (int64_t) fo[1], fs[1], fb[1]);
     } else {
@@ -176,7 +176,7 @@ static int one_segment(const hbuild * b, const yk_type * t)
     if (t->kind == YK_K_BUILTIN) {
         size_t fo[2], fs[2];
         int fb[2];
-        return !pair_fields(t->builtin, fo, fs, fb) || fb[0] == fb[1];
+        return !yk_pair_fields(t->builtin, fo, fs, fb) || fb[0] == fb[1];
     }
     return 1;
 }

@@ -1,12 +1,18 @@
 /*
- * yk_iov.c -- segment-list and serialisation entry points.
+ * yk_iov.c -- segment lists: yaksa_iov_len, yaksa_iov, yaksa_iov_len_max.
  *
- * yaksa_iov_len follows src/frontend/iov/yaksa_iov_len.c:11-19 (1 for a contiguous
- * type, count * num_contig otherwise).  The segment list itself (yaksa_iov,
- * yaksa_iov_len_max) and type serialisation (yaksa_flatten*) sit next to the
- * pack/unpack path rather than on it; until they are built they report
- * YAKSA_ERR__NOT_SUPPORTED, which the reference also uses for operations a backend
- * does not provide.
+ * A segment list names the contiguous pieces of `count` elements of a type in typemap
+ * order, as (address, length) pairs for readv/writev-style and RDMA gather callers.  The
+ * pieces are those of the type tree, not of the flattened device descriptor: callers
+ * index them with iov_offset and size their arrays with yaksa_iov_len, so the list must
+ * have exactly count * num_contig entries with the reference's boundaries
+ * (src/frontend/iov/yaksa_iov.c:48-359):
+ *   - a contiguous type is one piece covering all `count` elements, whatever the offset;
+ *   - a pair builtin whose second field follows the first directly is one piece per
+ *     element, otherwise two (the reference's BUILTIN_PAIRTYPE_IOV, :12-46);
+ *   - every other kind lists its blocks in order, recursing into the child for each
+ *     block and skipping zero-length blocks of hindexed and struct types.
+ * The walk is host code: it writes the caller's host array and does no data movement.
  */
 #include "yk_internal.h"
 
@@ -19,47 +25,227 @@ int yaksa_iov_len(uintptr_t count, yaksa_type_t type, uintptr_t * iov_len)
     return YAKSA_SUCCESS;
 }
 
-int yaksa_iov_len_max(uintptr_t count, yaksa_type_t type, uintptr_t max_iov_bytes,
-                      uintptr_t * iov_len, uintptr_t * actual_iov_bytes)
+static uintptr_t pieces(uintptr_t count, const yk_type * t)
 {
-    (void) count;
-    (void) type;
-    (void) max_iov_bytes;
-    *iov_len = 0;
-    *actual_iov_bytes = 0;
-    return YAKSA_ERR__NOT_SUPPORTED;
+    return t->is_contig ? 1 : count * t->num_contig;
+}
+
+/* segment list state: entries still allowed, entries to skip, output cursor */
+typedef struct {
+    struct iovec *out;
+    uintptr_t room;
+    uintptr_t skip;
+    uintptr_t n;
+} iov_cur;
+
+static int iov_walk(const char *buf, uintptr_t count, const yk_type * t, iov_cur * c);
+
+/* one block of `n` children at `p`: skipped whole while the offset covers it */
+static int iov_block(const char *p, uintptr_t n, const yk_type * child, iov_cur * c)
+{
+    uintptr_t k = pieces(n, child);
+    if (c->skip >= k) {
+        c->skip -= k;
+        return YAKSA_SUCCESS;
+    }
+    return iov_walk(p, n, child, c);
+}
+
+static int iov_walk(const char *buf, uintptr_t count, const yk_type * t, iov_cur * c)
+{
+    if (c->room == 0)
+        return YAKSA_SUCCESS;
+    if (t->is_contig) {
+        /* one piece for the whole run; the offset does not apply inside it */
+        c->out[c->n].iov_base = (char *) buf + t->true_lb;
+        c->out[c->n].iov_len = count * t->size;
+        c->n++;
+        c->room--;
+        c->skip = 0;
+        return YAKSA_SUCCESS;
+    }
+    if (c->skip >= count * t->num_contig) {
+        c->skip -= count * t->num_contig;
+        return YAKSA_SUCCESS;
+    }
+    switch (t->kind) {
+        case YK_K_BUILTIN:{
+                size_t off[2], sz[2];
+                int bt[2];
+                if (!yk_pair_fields(t->builtin, off, sz, bt))
+                    return YAKSA_ERR__INTERNAL;
+                const uintptr_t ext = (uintptr_t) t->extent;
+                if (off[1] == sz[0]) {
+                    /* fields back to back: one piece per element */
+                    const char *z = buf + c->skip * ext;
+                    uintptr_t m = YK_MIN(c->room, count - c->skip);
+                    for (uintptr_t x = 0; x < m; x++, z += ext) {
+                        c->out[c->n].iov_base = (char *) z;
+                        c->out[c->n].iov_len = sz[0] + sz[1];
+                        c->n++;
+                    }
+                    c->room -= m;
+                } else {
+                    /* two pieces per element, never split: the offset must be even and
+                     * only whole pairs that fit are listed */
+                    if (c->skip % 2)
+                        return YAKSA_ERR__INTERNAL;
+                    const char *z = buf + (c->skip / 2) * ext;
+                    uintptr_t m = YK_MIN(c->room - 1, count * 2 - c->skip);
+                    for (uintptr_t x = 0; x < m; x += 2, z += ext) {
+                        c->out[c->n].iov_base = (char *) z;
+                        c->out[c->n].iov_len = sz[0];
+                        c->out[c->n + 1].iov_base = (char *) z + off[1];
+                        c->out[c->n + 1].iov_len = sz[1];
+                        c->n += 2;
+                        c->room -= 2;
+                    }
+                }
+                c->skip = 0;
+                return YAKSA_SUCCESS;
+            }
+        case YK_K_CONTIG:
+            return iov_walk(buf, count * (uintptr_t) t->count, t->child, c);
+        case YK_K_RESIZED:
+            for (uintptr_t i = 0; i < count && c->room; i++) {
+                int rc = iov_block(buf + (intptr_t) i * t->extent, 1, t->child, c);
+                if (rc)
+                    return rc;
+            }
+            return YAKSA_SUCCESS;
+        case YK_K_SUBARRAY:{
+                const char *p = buf + t->true_lb - t->primary->true_lb;
+                for (uintptr_t i = 0; i < count && c->room; i++, p += t->extent) {
+                    int rc = iov_block(p, 1, t->primary, c);
+                    if (rc)
+                        return rc;
+                }
+                return YAKSA_SUCCESS;
+            }
+        case YK_K_HVECTOR:
+        case YK_K_BLKHINDX:
+        case YK_K_HINDEXED:
+        case YK_K_STRUCT:
+            for (uintptr_t i = 0; i < count && c->room; i++) {
+                const char *el = buf + (intptr_t) i * t->extent;
+                for (intptr_t j = 0; j < t->count && c->room; j++) {
+                    const yk_type *ch = t->kind == YK_K_STRUCT ? t->types[j] : t->child;
+                    uintptr_t n;
+                    const char *p;
+                    if (t->kind == YK_K_HVECTOR) {
+                        n = (uintptr_t) t->blocklength;
+                        p = el + j * t->stride;
+                    } else if (t->kind == YK_K_BLKHINDX) {
+                        n = (uintptr_t) t->blocklength;
+                        p = el + t->displs[j];
+                    } else {
+                        n = (uintptr_t) t->blens[j];
+                        p = el + t->displs[j];
+                        if (n == 0)
+                            continue;
+                    }
+                    int rc = iov_block(p, n, ch, c);
+                    if (rc)
+                        return rc;
+                }
+            }
+            return YAKSA_SUCCESS;
+    }
+    return YAKSA_ERR__INTERNAL;
 }
 
 int yaksa_iov(const char *buf, uintptr_t count, yaksa_type_t type, uintptr_t iov_offset,
               struct iovec *iov, uintptr_t max_iov_len, uintptr_t * actual_iov_len)
 {
-    (void) buf;
-    (void) count;
-    (void) type;
-    (void) iov_offset;
-    (void) iov;
-    (void) max_iov_len;
     *actual_iov_len = 0;
-    return YAKSA_ERR__NOT_SUPPORTED;
+    yk_type *t = yk_type_get(type);
+    if (!t)
+        return YAKSA_ERR__INTERNAL;
+    if (max_iov_len == 0)
+        return YAKSA_SUCCESS;
+    iov_cur c = { iov, max_iov_len, iov_offset, 0 };
+    int rc = iov_walk(buf, count, t, &c);
+    *actual_iov_len = c.n;
+    return rc;
 }
 
-int yaksa_flatten_size(yaksa_type_t type, uintptr_t * flattened_type_size)
+/* ------------------------------------------------------------------------- */
+/* yaksa_iov_len_max: the longest leading part of the segment list whose bytes  */
+/* fit in max_iov_bytes, never splitting one builtin element.  The reference's  */
+/* recursion (src/frontend/iov/yaksa_iov_len_max.c:20-170) computes this for    */
+/* well-formed inputs, but reads the child's block length where it means the    */
+/* type's own (:59-69); this walk follows the segment list itself instead.      */
+/* ------------------------------------------------------------------------- */
+
+typedef struct {
+    uintptr_t room;             /* bytes left */
+    uintptr_t n, bytes;
+    int full;                   /* a piece did not fit: stop */
+} len_cur;
+
+static void len_walk(uintptr_t count, const yk_type * t, len_cur * c)
 {
-    (void) type;
-    *flattened_type_size = 0;
-    return YAKSA_ERR__NOT_SUPPORTED;
+    if (c->full)
+        return;
+    if (t->is_contig) {
+        uintptr_t b = count * t->size;
+        if (b > c->room) {
+            c->full = 1;
+            return;
+        }
+        c->room -= b;
+        c->bytes += b;
+        c->n++;
+        return;
+    }
+    /* whole elements first: each adds num_contig pieces */
+    uintptr_t whole = t->size ? YK_MIN(count, c->room / t->size) : count;
+    c->room -= whole * t->size;
+    c->bytes += whole * t->size;
+    c->n += whole * t->num_contig;
+    if (whole == count)
+        return;
+    /* the first element that does not fit, piece by piece */
+    switch (t->kind) {
+        case YK_K_BUILTIN:     /* a pair element is listed whole or not at all */
+            c->full = 1;
+            return;
+        case YK_K_CONTIG:
+            len_walk((uintptr_t) t->count, t->child, c);
+            break;
+        case YK_K_RESIZED:
+            len_walk(1, t->child, c);
+            break;
+        case YK_K_SUBARRAY:
+            len_walk(1, t->primary, c);
+            break;
+        case YK_K_HVECTOR:
+        case YK_K_BLKHINDX:
+        case YK_K_HINDEXED:
+        case YK_K_STRUCT:
+            for (intptr_t j = 0; j < t->count && !c->full; j++) {
+                uintptr_t n = (t->kind == YK_K_HVECTOR || t->kind == YK_K_BLKHINDX) ?
+                    (uintptr_t) t->blocklength : (uintptr_t) t->blens[j];
+                if (n == 0 && (t->kind == YK_K_HINDEXED || t->kind == YK_K_STRUCT))
+                    continue;
+                len_walk(n, t->kind == YK_K_STRUCT ? t->types[j] : t->child, c);
+            }
+            break;
+    }
+    c->full = 1;
 }
 
-int yaksa_flatten(yaksa_type_t type, void *flattened_type)
+int yaksa_iov_len_max(uintptr_t count, yaksa_type_t type, uintptr_t max_iov_bytes,
+                      uintptr_t * iov_len, uintptr_t * actual_iov_bytes)
 {
-    (void) type;
-    (void) flattened_type;
-    return YAKSA_ERR__NOT_SUPPORTED;
-}
-
-int yaksa_unflatten(yaksa_type_t * type, const void *flattened_type)
-{
-    (void) flattened_type;
-    *type = YAKSA_TYPE__NULL;
-    return YAKSA_ERR__NOT_SUPPORTED;
+    *iov_len = 0;
+    *actual_iov_bytes = 0;
+    yk_type *t = yk_type_get(type);
+    if (!t)
+        return YAKSA_ERR__INTERNAL;
+    len_cur c = { max_iov_bytes, 0, 0, 0 };
+    len_walk(count, t, &c);
+    *iov_len = c.n;
+    *actual_iov_bytes = c.bytes;
+    return YAKSA_SUCCESS;
 }

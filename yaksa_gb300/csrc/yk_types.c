@@ -950,3 +950,202 @@ int yaksa_type_free(yaksa_type_t type)
     yk_type_unref(t);
     return YAKSA_SUCCESS;
 }
+
+/* ------------------------------------------------------------------------- */
+/* flatten / unflatten (yaksa.h.in:618-634)                                  */
+/* ------------------------------------------------------------------------- */
+
+/* A flattened type is one record per node of the type tree, depth first: a fixed
+ * header with every derived field, then the node's block-length and displacement
+ * arrays, then its children.  Builtin nodes carry only their handle and unflatten to
+ * the builtin object itself.  Unlike the reference, which copies its in-memory type
+ * objects (pointers included) and so is readable only by the same build
+ * (src/frontend/flatten/yaksa_flatten.c:10-95), the records hold no pointers and are
+ * position independent; they keep host byte order, like every yaksa message. */
+#define YK_FLAT_MAGIC 0x59414b53u       /* "SKAY" */
+
+typedef struct {
+    uint32_t magic, kind;
+    int64_t builtin, count, blocklength, stride, ndims;
+    int64_t tree_depth, alignment;
+    uint64_t size, num_contig, builtin_size;
+    int64_t extent, lb, ub, true_lb, true_ub;
+    int64_t is_contig, base_type, needs_host_ops;
+} yk_flat_hdr;
+
+static int flat_has_blens(const yk_type * t)
+{
+    return t->kind == YK_K_HINDEXED || t->kind == YK_K_STRUCT;
+}
+
+static int flat_has_displs(const yk_type * t)
+{
+    return t->kind == YK_K_BLKHINDX || t->kind == YK_K_HINDEXED || t->kind == YK_K_STRUCT;
+}
+
+static uintptr_t flat_size(const yk_type * t)
+{
+    uintptr_t n = sizeof(yk_flat_hdr);
+    if (t->kind == YK_K_BUILTIN)
+        return n;
+    n += (flat_has_blens(t) + flat_has_displs(t)) * (uintptr_t) t->count * sizeof(int64_t);
+    if (t->kind == YK_K_STRUCT) {
+        for (intptr_t i = 0; i < t->count; i++)
+            n += flat_size(t->types[i]);
+    } else {
+        n += flat_size(t->kind == YK_K_SUBARRAY ? t->primary : t->child);
+    }
+    return n;
+}
+
+static char *flat_write(const yk_type * t, char *p)
+{
+    yk_flat_hdr h;
+    memset(&h, 0, sizeof(h));
+    h.magic = YK_FLAT_MAGIC;
+    h.kind = (uint32_t) t->kind;
+    h.builtin = (int64_t) t->builtin;
+    h.count = t->count;
+    h.blocklength = t->blocklength;
+    h.stride = t->stride;
+    h.ndims = t->ndims;
+    h.tree_depth = t->tree_depth;
+    h.alignment = t->alignment;
+    h.size = t->size;
+    h.num_contig = t->num_contig;
+    h.builtin_size = t->builtin_size;
+    h.extent = t->extent;
+    h.lb = t->lb;
+    h.ub = t->ub;
+    h.true_lb = t->true_lb;
+    h.true_ub = t->true_ub;
+    h.is_contig = t->is_contig;
+    h.base_type = t->base_type;
+    h.needs_host_ops = t->needs_host_ops;
+    memcpy(p, &h, sizeof(h));
+    p += sizeof(h);
+    if (t->kind == YK_K_BUILTIN)
+        return p;
+    for (intptr_t i = 0; flat_has_blens(t) && i < t->count; i++, p += sizeof(int64_t)) {
+        int64_t v = t->blens[i];
+        memcpy(p, &v, sizeof(v));
+    }
+    for (intptr_t i = 0; flat_has_displs(t) && i < t->count; i++, p += sizeof(int64_t)) {
+        int64_t v = t->displs[i];
+        memcpy(p, &v, sizeof(v));
+    }
+    if (t->kind == YK_K_STRUCT) {
+        for (intptr_t i = 0; i < t->count; i++)
+            p = flat_write(t->types[i], p);
+        return p;
+    }
+    return flat_write(t->kind == YK_K_SUBARRAY ? t->primary : t->child, p);
+}
+
+/* a new reference to the node at *pp; advances *pp past it */
+static int flat_read(const char **pp, yk_type ** out)
+{
+    yk_flat_hdr h;
+    memcpy(&h, *pp, sizeof(h));
+    *pp += sizeof(h);
+    *out = NULL;
+    if (h.magic != YK_FLAT_MAGIC || h.kind > YK_K_SUBARRAY)
+        return YAKSA_ERR__INTERNAL;
+    if (h.kind == YK_K_BUILTIN) {
+        yk_type *b = yk_type_get((yaksa_type_t) h.builtin);
+        if (!b || b->kind != YK_K_BUILTIN)
+            return YAKSA_ERR__INTERNAL;
+        yk_type_ref(b);
+        *out = b;
+        return YAKSA_SUCCESS;
+    }
+    yk_type *t = type_new((int) h.kind);
+    if (!t)
+        return YAKSA_ERR__OUT_OF_MEM;
+    t->count = h.count;
+    t->blocklength = h.blocklength;
+    t->stride = h.stride;
+    t->ndims = (int) h.ndims;
+    t->tree_depth = (int) h.tree_depth;
+    t->alignment = (int) h.alignment;
+    t->size = h.size;
+    t->num_contig = h.num_contig;
+    t->builtin_size = h.builtin_size;
+    t->extent = h.extent;
+    t->lb = h.lb;
+    t->ub = h.ub;
+    t->true_lb = h.true_lb;
+    t->true_ub = h.true_ub;
+    t->is_contig = h.is_contig != 0;
+    t->base_type = (int) h.base_type;
+    t->needs_host_ops = h.needs_host_ops != 0;
+    int rc = YAKSA_SUCCESS;
+    size_t arr = (size_t) (t->count > 0 ? t->count : 0) * sizeof(intptr_t);
+    if (flat_has_blens(t)) {
+        t->blens = malloc(arr ? arr : 1);
+        if (!t->blens)
+            rc = YAKSA_ERR__OUT_OF_MEM;
+        for (intptr_t i = 0; !rc && i < t->count; i++, *pp += sizeof(int64_t)) {
+            int64_t v;
+            memcpy(&v, *pp, sizeof(v));
+            t->blens[i] = (intptr_t) v;
+        }
+    }
+    if (!rc && flat_has_displs(t)) {
+        t->displs = malloc(arr ? arr : 1);
+        if (!t->displs)
+            rc = YAKSA_ERR__OUT_OF_MEM;
+        for (intptr_t i = 0; !rc && i < t->count; i++, *pp += sizeof(int64_t)) {
+            int64_t v;
+            memcpy(&v, *pp, sizeof(v));
+            t->displs[i] = (intptr_t) v;
+        }
+    }
+    if (!rc && t->kind == YK_K_STRUCT) {
+        t->types = calloc(t->count > 0 ? (size_t) t->count : 1, sizeof(yk_type *));
+        if (!t->types)
+            rc = YAKSA_ERR__OUT_OF_MEM;
+        for (intptr_t i = 0; !rc && i < t->count; i++)
+            rc = flat_read(pp, &t->types[i]);
+        if (rc && t->types) {
+            /* children read so far are released with the node below */
+            intptr_t got = 0;
+            while (got < t->count && t->types[got])
+                got++;
+            t->count = got;
+        }
+    } else if (!rc) {
+        rc = flat_read(pp, t->kind == YK_K_SUBARRAY ? &t->primary : &t->child);
+    }
+    if (rc) {
+        yk_type_unref(t);
+        return rc;
+    }
+    *out = t;
+    return YAKSA_SUCCESS;
+}
+
+int yaksa_flatten_size(yaksa_type_t type, uintptr_t * flattened_type_size)
+{
+    LOOKUP(type, t);
+    *flattened_type_size = flat_size(t);
+    return YAKSA_SUCCESS;
+}
+
+int yaksa_flatten(yaksa_type_t type, void *flattened_type)
+{
+    LOOKUP(type, t);
+    flat_write(t, (char *) flattened_type);
+    return YAKSA_SUCCESS;
+}
+
+int yaksa_unflatten(yaksa_type_t * type, const void *flattened_type)
+{
+    *type = YAKSA_TYPE__NULL;
+    const char *p = (const char *) flattened_type;
+    yk_type *t;
+    int rc = flat_read(&p, &t);
+    if (rc)
+        return rc;
+    return publish(t, type);
+}
