@@ -115,6 +115,11 @@ int yaksa_gb300_serve_trace(yaksa_gb300_pup_t * ops, const double *arrival_s, in
                             yaksa_gb300_server_t server, yaksa_info_t info, double *latency_s,
                             double *makespan_s);
 
+/* Launch-shape autotuner (no counterpart in the reference): shape classes seen, classes
+ * whose shape is decided, and launches timed so far.  YAKSA_GB300_AUTOTUNE=0 in the
+ * environment keeps the default shapes. */
+int yaksa_gb300_autotune_stats(uint32_t * classes, uint32_t * decided, uint64_t * probes);
+
 /* Runtime counters since load: kernel launches, calls served in place (device or
  * GPU-addressable host memory), calls that staged host data through device memory,
  * and contiguous calls served by one copy. */

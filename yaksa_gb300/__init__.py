@@ -139,6 +139,9 @@ def load_library(path):
     if hasattr(lib, "yaksa_gb300_stats"):
         lib.yaksa_gb300_stats.restype = ctypes.c_int
         lib.yaksa_gb300_stats.argtypes = [ctypes.POINTER(_u64)] * 4
+        lib.yaksa_gb300_autotune_stats.restype = ctypes.c_int
+        lib.yaksa_gb300_autotune_stats.argtypes = [ctypes.POINTER(ctypes.c_uint32),
+                                                   ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(_u64)]
         for name, extra in (("yaksa_gb300_pup_batch_stream", [_vp]), ("yaksa_gb300_pup_batch", []),
                             ("yaksa_gb300_ipup_batch", [ctypes.POINTER(_u64)])):
             f = getattr(lib, name)
@@ -474,6 +477,11 @@ class Yaksa:
 
     def graph_free(self, g):
         self._chk("yaksa_gb300_graph_free", self.lib.yaksa_gb300_graph_free(g))
+
+    def autotune_stats(self):
+        a, b, c = ctypes.c_uint32(), ctypes.c_uint32(), _u64()
+        self.lib.yaksa_gb300_autotune_stats(ctypes.byref(a), ctypes.byref(b), ctypes.byref(c))
+        return dict(classes=a.value, decided=b.value, probes=c.value)
 
     def stats(self):
         v = [_u64() for _ in range(4)]

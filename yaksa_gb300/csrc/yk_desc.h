@@ -124,7 +124,8 @@ typedef struct {
 /* Tiles of one batch request (units per tile depend on the batch's total size). */
 int yk_cuda_batch_units_per_thread(uint64_t total_units);
 uint64_t yk_cuda_tiles(uint64_t units, int units_per_thread);
-int yk_cuda_launch_batch(const yk_batch * b, int units_per_thread, int regular, void *stream);
+int yk_cuda_launch_batch(const yk_batch * b, int units_per_thread, int regular, int ctas_per_sm,
+                         void *stream);
 
 /* ---------------------------------------------------------------------------
  * Persistent request server: a device-visible work queue drained by resident CTAs.
@@ -159,6 +160,9 @@ void yk_level_set_magic(yk_level * l);
 
 /* Launch on `stream` (a cudaStream_t).  Returns 0 or a cudaError_t value. */
 int yk_cuda_launch_pup(const yk_launch * l, void *stream);
+/* the same with a launch shape for the REPLACE byte kernels (0, 0 = by size) */
+int yk_cuda_launch_pup_cfg(const yk_launch * l, void *stream, int units_per_thread,
+                           int ctas_per_sm);
 
 /* Ordered unpack for types whose targets may overlap: sorted-block owner-computes
  * kernel when the descriptor allows it, otherwise a single-warp ordered kernel. */

@@ -1435,9 +1435,9 @@ extern "C" uint64_t yk_cuda_tiles(uint64_t units, int units_per_thread)
 }
 
 template <typename IDX, int U>
-static void launch_bytes_u(const yk_launch * l, cudaStream_t s, uint64_t units)
+static void launch_bytes_u(const yk_launch * l, cudaStream_t s, uint64_t units, int cap)
 {
-    unsigned g = yk_grid(units, (uint64_t) YK_THREADS * U, U == 1 ? 64 : 8);
+    unsigned g = yk_grid(units, (uint64_t) YK_THREADS * U, cap ? cap : (U == 1 ? 64 : 8));
 #define YK_B(V) do { if (l->dir == 0) yk_bytes_kernel<IDX, V, 0, U><<<g, YK_THREADS, 0, s>>>(*l); \
                      else yk_bytes_kernel<IDX, V, 1, U><<<g, YK_THREADS, 0, s>>>(*l); } while (0)
     switch (l->vec) {
@@ -1451,9 +1451,9 @@ static void launch_bytes_u(const yk_launch * l, cudaStream_t s, uint64_t units)
 }
 
 template <int U>
-static void launch_regular_u(const yk_launch * l, cudaStream_t s, uint64_t units)
+static void launch_regular_u(const yk_launch * l, cudaStream_t s, uint64_t units, int cap)
 {
-    unsigned g = yk_grid(units, (uint64_t) YK_THREADS * U, U == 1 ? 64 : 8);
+    unsigned g = yk_grid(units, (uint64_t) YK_THREADS * U, cap ? cap : (U == 1 ? 64 : 8));
 #define YK_R(V) do { if (l->dir == 0) yk_regular_kernel<V, 0, U><<<g, YK_THREADS, 0, s>>>(*l); \
                      else yk_regular_kernel<V, 1, U><<<g, YK_THREADS, 0, s>>>(*l); } while (0)
     switch (l->vec) {
@@ -1466,31 +1466,34 @@ static void launch_regular_u(const yk_launch * l, cudaStream_t s, uint64_t units
 #undef YK_R
 }
 
+/* u: units per thread (1 or YK_UNROLL; 0 = by size); cap: CTAs per SM (0 = by u) */
 template <typename IDX>
-static void launch_bytes(const yk_launch * l, cudaStream_t s)
+static void launch_bytes(const yk_launch * l, cudaStream_t s, int u, int cap)
 {
     uint64_t units = l->nbytes / (uint64_t) l->vec;
-    int u = yk_cuda_batch_units_per_thread(units);
+    if (u != 1 && u != YK_UNROLL)
+        u = yk_cuda_batch_units_per_thread(units);
     if (l->regular >= 0 && sizeof(IDX) == 4) {
         if (u == 1)
-            launch_regular_u<1>(l, s, units);
+            launch_regular_u<1>(l, s, units, cap);
         else
-            launch_regular_u<YK_UNROLL>(l, s, units);
+            launch_regular_u<YK_UNROLL>(l, s, units, cap);
     } else if (u == 1) {
-        launch_bytes_u<IDX, 1>(l, s, units);
+        launch_bytes_u<IDX, 1>(l, s, units, cap);
     } else {
-        launch_bytes_u<IDX, YK_UNROLL>(l, s, units);
+        launch_bytes_u<IDX, YK_UNROLL>(l, s, units, cap);
     }
 }
 
 extern "C" int yk_cuda_launch_batch(const yk_batch * b, int units_per_thread, int regular,
-                                    void *stream)
+                                    int ctas_per_sm, void *stream)
 {
     cudaStream_t s = (cudaStream_t) stream;
     uint64_t tiles = b->tile_start[b->n];
     if (!tiles)
         return 0;
-    uint64_t cap = (uint64_t) yk_cuda_num_sms() * (units_per_thread == 1 ? 64u : 8u);
+    uint64_t cap = (uint64_t) yk_cuda_num_sms() *
+        (ctas_per_sm > 0 ? (unsigned) ctas_per_sm : (units_per_thread == 1 ? 64u : 8u));
     unsigned g = (unsigned) (tiles < cap ? tiles : cap);
     if (regular) {
         /* one unit per thread: the 40 inlined (vector width, direction, depth) variants
@@ -1506,6 +1509,12 @@ extern "C" int yk_cuda_launch_batch(const yk_batch * b, int units_per_thread, in
 }
 
 extern "C" int yk_cuda_launch_pup(const yk_launch * l, void *stream)
+{
+    return yk_cuda_launch_pup_cfg(l, stream, 0, 0);
+}
+
+extern "C" int yk_cuda_launch_pup_cfg(const yk_launch * l, void *stream, int units_per_thread,
+                                      int ctas_per_sm)
 {
     cudaStream_t s = (cudaStream_t) stream;
     if (l->nbytes == 0)
@@ -1531,9 +1540,9 @@ extern "C" int yk_cuda_launch_pup(const yk_launch * l, void *stream)
 #undef YK_H
     } else if (!l->typed_op) {
         if (l->use64)
-            launch_bytes<uint64_t>(l, s);
+            launch_bytes<uint64_t>(l, s, units_per_thread, ctas_per_sm);
         else
-            launch_bytes<uint32_t>(l, s);
+            launch_bytes<uint32_t>(l, s, units_per_thread, ctas_per_sm);
     } else {
         const yk_launch & c = *l;
         uint64_t units = c.nbytes / (uint64_t) c.vec;

@@ -27,6 +27,7 @@
 #include <time.h>
 #include <cuda_runtime_api.h>
 #include "yk_internal.h"
+#include "yk_tune.h"
 #include "yaksa_gb300.h"
 
 typedef struct {
@@ -112,6 +113,7 @@ static int runtime_ready(void)
 
 void yk_runtime_finalize(void)
 {
+    yk_tune_reset();
     pthread_mutex_lock(&R.mu);
     if (R.ready) {
         cudaStreamSynchronize(R.stream);
@@ -480,8 +482,10 @@ static int prepare(const yk_plan * p, char *typed, char *packed, yk_launch * L, 
     return prepare_with(p, typed, packed, L, kind, sorted, yk_desc_get);
 }
 
+/* tune: pick the launch shape of the REPLACE byte kernels with the autotuner (off for
+ * the no-allocation entry point, whose timing events would be a resource allocation) */
 static int launch_prepared(const yk_plan * p, const yk_launch * L, int kind, int sorted,
-                           cudaStream_t s)
+                           cudaStream_t s, int tune)
 {
     if (kind == YK_X_MEMCPY) {
         /* contiguous: the packed bytes are the memory bytes from true_lb */
@@ -492,8 +496,17 @@ static int launch_prepared(const yk_plan * p, const yk_launch * L, int kind, int
                                         cudaMemcpyDefault, s), "cudaMemcpyAsync");
     }
     __atomic_add_fetch(&R.launches, 1, __ATOMIC_RELAXED);
-    int e = (kind == YK_X_ORDERED) ? yk_cuda_launch_unpack_ordered(L, sorted, s) :
-        yk_cuda_launch_pup(L, s);
+    if (kind == YK_X_ORDERED)
+        return cuda_err((cudaError_t) yk_cuda_launch_unpack_ordered(L, sorted, s), "kernel launch");
+    yk_tune_cfg cfg = { 0, 0 };
+    int probe = -1;
+    if (tune && kind == YK_X_BYTES && !L->hidx) {
+        uint64_t units = L->nbytes / (uint64_t) L->vec;
+        probe = yk_tune_begin(yk_tune_key(YK_TUNE_SINGLE, L->regular, L->vec, L->dir, L->use64,
+                                          units), YK_TUNE_SINGLE, units, s, &cfg);
+    }
+    int e = yk_cuda_launch_pup_cfg(L, s, cfg.units_per_thread, cfg.ctas_per_sm);
+    yk_tune_end(probe, s);
     return cuda_err((cudaError_t) e, "kernel launch");
 }
 
@@ -504,7 +517,7 @@ static int enqueue(const yk_plan * p, char *typed, char *packed, cudaStream_t s)
     int rc = prepare(p, typed, packed, &L, &kind, &sorted);
     if (rc)
         return rc;
-    return launch_prepared(p, &L, kind, sorted, s);
+    return launch_prepared(p, &L, kind, sorted, s, 1);
 }
 
 /* The GPU cannot address a buffer: copy the touched span to device memory from the
@@ -717,13 +730,21 @@ static uint32_t tile_multiplier(uint64_t total)
  * (regular nests, everything else). */
 static int flush_class(yk_launch * ls, int n, int regular, cudaStream_t s)
 {
-    uint64_t units = 0;
-    for (int i = 0; i < n; i++)
-        units += ls[i].nbytes / (uint64_t) ls[i].vec;
-    int u = regular ? 1 : yk_cuda_batch_units_per_thread(units);
     static __thread yk_batch B;
     for (int i0 = 0; i0 < n; i0 += YK_BATCH_MAX) {
         int m = YK_MIN(YK_BATCH_MAX, n - i0);
+        uint64_t units = 0;
+        int wide = 0;
+        for (int i = 0; i < m; i++) {
+            units += ls[i0 + i].nbytes / (uint64_t) ls[i0 + i].vec;
+            wide |= ls[i0 + i].use64;
+        }
+        const int fam = regular ? YK_TUNE_BATCH_REGULAR : YK_TUNE_BATCH;
+        yk_tune_cfg cfg;
+        int probe = yk_tune_begin(yk_tune_key(fam, regular ? 0 : -1, 0, 0, wide, units), fam, units,
+                                  s, &cfg);
+        int u = regular ? 1 : cfg.units_per_thread ? cfg.units_per_thread :
+            yk_cuda_batch_units_per_thread(units);
         B.n = m;
         B.tile_start[0] = 0;
         for (int i = 0; i < m; i++) {
@@ -733,7 +754,9 @@ static int flush_class(yk_launch * ls, int n, int regular, cudaStream_t s)
         }
         B.tile_mul = m > 1 ? tile_multiplier(B.tile_start[m]) : 1;
         __atomic_add_fetch(&R.launches, 1, __ATOMIC_RELAXED);
-        int rc = cuda_err((cudaError_t) yk_cuda_launch_batch(&B, u, regular, s), "batch launch");
+        int rc = cuda_err((cudaError_t) yk_cuda_launch_batch(&B, u, regular, cfg.ctas_per_sm, s),
+                          "batch launch");
+        yk_tune_end(probe, s);
         if (rc)
             return rc;
     }
@@ -800,7 +823,7 @@ static int batch_run(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info, cudaStre
         if (kind == YK_X_BYTES && !ls[nb].use64 && !ls[nb].hidx)
             nb++;
         else
-            rc = launch_prepared(&p, &ls[nb], kind, sorted, s);
+            rc = launch_prepared(&p, &ls[nb], kind, sorted, s, 1);
     }
     if (!rc && nb)
         rc = flush_batch(ls, nb, s);
@@ -933,7 +956,7 @@ int yaksa_gb300_pup_noalloc(yaksa_gb300_pup_t * o, void *stream)
             desc_rebase(&L.desc, (const char *) src->dev_tables, (char *) scr);
         }
     }
-    rc = launch_prepared(&p, &L, kind, sorted, s);
+    rc = launch_prepared(&p, &L, kind, sorted, s, 0);
     if (!rc)
         o->actual = p.b1 - p.b0;
     return rc;

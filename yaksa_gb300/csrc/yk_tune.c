@@ -1,0 +1,257 @@
+/*
+ * yk_tune.c -- online autotuner for the launch shape of the byte-moving kernels.
+ *
+ * The REPLACE kernels (regular nests, generic descriptors, batches) can run with one
+ * work unit per thread over many CTAs, or four units per thread in a grid-stride loop
+ * over fewer, and the best grid size depends on the descriptor's shape and the request
+ * size.  Rather than fixing one rule, each shape class (kernel family, nesting depth,
+ * vector width, direction, log2 of the units) times a few candidate shapes on its first
+ * real launches: CUDA events around the launch, read back later without waiting
+ * (cudaEventQuery at the next tuning decision).  After every candidate has a few
+ * samples the class keeps the fastest.  All candidates run the same kernel over the
+ * same units, so results do not depend on which one runs.  Launches inside a stream
+ * capture, small launches and YAKSA_GB300_AUTOTUNE=0 use the decided (or default)
+ * shape without timing.  No reference counterpart: the reference fixes its launch
+ * shape (src/backend/cuda/pup/yaksuri_cudai_pup.c:20-48).
+ */
+#include <stdlib.h>
+#include <string.h>
+#include <pthread.h>
+#include <cuda_runtime.h>
+#include "yk_internal.h"
+#include "yk_tune.h"
+
+#define YK_TUNE_SLOTS 512
+#define YK_TUNE_PROBES 64
+#define YK_TUNE_REPS 4
+#define YK_TUNE_MARGIN 0.95f    /* a candidate replaces the default only if 5% faster */
+#define YK_TUNE_MIN_UNITS (1u << 15)
+
+/* candidate shapes per family: units per thread, CTAs per SM (0 = default) */
+/* candidate shapes per family: units per thread, CTAs per SM; the first is the default
+ * rule (units per thread by size, 64 or 8 CTAs per SM) */
+static const yk_tune_cfg cand_single[] = { {0, 0}, {1, 64}, {4, 8}, {4, 16}, {1, 16} };
+static const yk_tune_cfg cand_batch_regular[] = { {1, 0}, {1, 8}, {1, 4} };
+static const yk_tune_cfg cand_batch[] = { {0, 0}, {1, 64}, {4, 8}, {4, 16} };
+
+typedef struct {
+    uint64_t key;               /* 0: empty */
+    const yk_tune_cfg *cand;
+    int ncand;
+    float fastest[8];           /* best sample per candidate (ms) */
+    int done[8], issued[8];
+    int best;                   /* -1 while timing */
+} slot_t;
+
+typedef struct {
+    cudaEvent_t e0, e1;
+    int slot, cand;
+    int busy;                   /* taken by a launch */
+    int armed;                  /* e1 recorded after that launch: may be read */
+} probe_t;
+
+static struct {
+    pthread_mutex_t mu;
+    int init, enabled;
+    slot_t slots[YK_TUNE_SLOTS];
+    probe_t probes[YK_TUNE_PROBES];
+    uint64_t nprobes;
+} T = { PTHREAD_MUTEX_INITIALIZER, 0, 0, {{0}}, {{0}}, 0 };
+
+static int log2u(uint64_t v)
+{
+    int l = 0;
+    while (v >>= 1)
+        l++;
+    return l;
+}
+
+uint64_t yk_tune_key(int family, int depth, int vec, int dir, int wide, uint64_t units)
+{
+    /* nonzero by construction: family is 1..3 */
+    return ((uint64_t) family << 32) | ((uint64_t) (depth + 1) << 24) |
+        ((uint64_t) vec << 16) | ((uint64_t) dir << 12) | ((uint64_t) wide << 8) |
+        (uint64_t) log2u(units);
+}
+
+static void drain_locked(void)
+{
+    for (int i = 0; i < YK_TUNE_PROBES; i++) {
+        probe_t *p = &T.probes[i];
+        if (!p->busy || !p->armed)
+            continue;
+        cudaError_t e = cudaEventQuery(p->e1);
+        if (e == cudaErrorNotReady)
+            continue;
+        float ms = 0;
+        if (e == cudaSuccess && cudaEventElapsedTime(&ms, p->e0, p->e1) == cudaSuccess) {
+            slot_t *s = &T.slots[p->slot];
+            if (s->done[p->cand] == 0 || ms < s->fastest[p->cand])
+                s->fastest[p->cand] = ms;
+            s->done[p->cand]++;
+            int all = 1;
+            for (int c = 0; c < s->ncand; c++)
+                all &= s->done[c] >= YK_TUNE_REPS;
+            if (all && s->best < 0) {
+                /* candidate 0 is the default shape: keep it unless another one's fastest
+                 * sample beats it clearly (samples are noisy and taken with warm caches) */
+                int b = 0;
+                for (int c = 1; c < s->ncand; c++)
+                    if (s->fastest[c] < YK_TUNE_MARGIN * s->fastest[0] &&
+                        s->fastest[c] < s->fastest[b])
+                        b = c;
+                s->best = b;
+            }
+        } else {
+            cudaGetLastError();
+        }
+        p->busy = p->armed = 0;
+    }
+}
+
+static void init_locked(void)
+{
+    if (T.init)
+        return;
+    const char *e = getenv("YAKSA_GB300_AUTOTUNE");
+    T.enabled = !(e && e[0] == '0');
+    T.init = 1;
+}
+
+static slot_t *slot_locked(uint64_t key, int family)
+{
+    uint64_t h = key * 0x9e3779b97f4a7c15ull;
+    for (int k = 0; k < YK_TUNE_SLOTS; k++) {
+        slot_t *s = &T.slots[(h + (uint64_t) k) % YK_TUNE_SLOTS];
+        if (s->key == key)
+            return s;
+        if (s->key == 0) {
+            memset(s, 0, sizeof(*s));
+            s->key = key;
+            s->best = -1;
+            if (family == YK_TUNE_SINGLE) {
+                s->cand = cand_single;
+                s->ncand = (int) (sizeof(cand_single) / sizeof(cand_single[0]));
+            } else if (family == YK_TUNE_BATCH_REGULAR) {
+                s->cand = cand_batch_regular;
+                s->ncand = (int) (sizeof(cand_batch_regular) / sizeof(cand_batch_regular[0]));
+            } else {
+                s->cand = cand_batch;
+                s->ncand = (int) (sizeof(cand_batch) / sizeof(cand_batch[0]));
+            }
+            return s;
+        }
+    }
+    return NULL;        /* table full: default shapes */
+}
+
+int yk_tune_begin(uint64_t key, int family, uint64_t units, void *stream, yk_tune_cfg * cfg)
+{
+    cudaStream_t st = (cudaStream_t) stream;
+    cfg->units_per_thread = family == YK_TUNE_BATCH_REGULAR ? 1 : 0;
+    cfg->ctas_per_sm = 0;
+    pthread_mutex_lock(&T.mu);
+    init_locked();
+    if (!T.enabled || units < YK_TUNE_MIN_UNITS) {
+        pthread_mutex_unlock(&T.mu);
+        return -1;
+    }
+    drain_locked();
+    slot_t *s = slot_locked(key, family);
+    if (!s) {
+        pthread_mutex_unlock(&T.mu);
+        return -1;
+    }
+    if (s->best >= 0) {
+        *cfg = s->cand[s->best];
+        pthread_mutex_unlock(&T.mu);
+        return -1;
+    }
+    enum cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+        cudaGetLastError();
+        pthread_mutex_unlock(&T.mu);
+        return -1;      /* no timing inside a capture: default shape */
+    }
+    /* the candidate with the fewest samples issued */
+    int c = 0;
+    for (int k = 1; k < s->ncand; k++)
+        if (s->issued[k] < s->issued[c])
+            c = k;
+    int pi = -1;
+    for (int i = 0; i < YK_TUNE_PROBES && pi < 0; i++)
+        if (!T.probes[i].busy)
+            pi = i;
+    if (pi < 0) {
+        pthread_mutex_unlock(&T.mu);
+        return -1;      /* every probe in flight: launch untimed */
+    }
+    probe_t *p = &T.probes[pi];
+    if (!p->e0 && (cudaEventCreate(&p->e0) != cudaSuccess ||
+                   cudaEventCreate(&p->e1) != cudaSuccess)) {
+        cudaGetLastError();
+        pthread_mutex_unlock(&T.mu);
+        return -1;
+    }
+    if (cudaEventRecord(p->e0, st) != cudaSuccess) {
+        cudaGetLastError();
+        pthread_mutex_unlock(&T.mu);
+        return -1;
+    }
+    p->busy = 1;
+    p->armed = 0;
+    p->slot = (int) (s - T.slots);
+    p->cand = c;
+    s->issued[c]++;
+    T.nprobes++;
+    *cfg = s->cand[c];
+    pthread_mutex_unlock(&T.mu);
+    return pi;
+}
+
+void yk_tune_end(int probe, void *stream)
+{
+    if (probe < 0)
+        return;
+    pthread_mutex_lock(&T.mu);
+    if (cudaEventRecord(T.probes[probe].e1, (cudaStream_t) stream) != cudaSuccess) {
+        cudaGetLastError();
+        T.probes[probe].busy = 0;
+    } else {
+        T.probes[probe].armed = 1;
+    }
+    pthread_mutex_unlock(&T.mu);
+}
+
+void yk_tune_reset(void)
+{
+    pthread_mutex_lock(&T.mu);
+    for (int i = 0; i < YK_TUNE_PROBES; i++) {
+        if (T.probes[i].e0) {
+            cudaEventDestroy(T.probes[i].e0);
+            cudaEventDestroy(T.probes[i].e1);
+        }
+    }
+    memset(T.probes, 0, sizeof(T.probes));
+    memset(T.slots, 0, sizeof(T.slots));
+    T.nprobes = 0;
+    T.init = 0;
+    pthread_mutex_unlock(&T.mu);
+}
+
+int yaksa_gb300_autotune_stats(uint32_t * classes, uint32_t * decided, uint64_t * probes)
+{
+    pthread_mutex_lock(&T.mu);
+    drain_locked();
+    uint32_t n = 0, d = 0;
+    for (int i = 0; i < YK_TUNE_SLOTS; i++)
+        if (T.slots[i].key) {
+            n++;
+            d += T.slots[i].best >= 0;
+        }
+    *classes = n;
+    *decided = d;
+    *probes = T.nprobes;
+    pthread_mutex_unlock(&T.mu);
+    return YAKSA_SUCCESS;
+}

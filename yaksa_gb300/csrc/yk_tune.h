@@ -1,0 +1,22 @@
+/* yk_tune.h -- launch-shape autotuner of the byte-moving kernels (yk_tune.c) */
+#ifndef YK_TUNE_H
+#define YK_TUNE_H
+
+#include <stdint.h>
+
+enum { YK_TUNE_SINGLE = 1, YK_TUNE_BATCH_REGULAR = 2, YK_TUNE_BATCH = 3 };
+
+typedef struct {
+    int units_per_thread;       /* 1 or 4; 0 = chosen by size */
+    int ctas_per_sm;            /* grid cap; 0 = by units per thread */
+} yk_tune_cfg;
+
+/* shape class of a launch */
+uint64_t yk_tune_key(int family, int depth, int vec, int dir, int wide, uint64_t units);
+/* the shape to launch with; returns a probe id (>= 0) when this launch is timed, in
+ * which case the caller launches and then calls yk_tune_end on the same stream */
+int yk_tune_begin(uint64_t key, int family, uint64_t units, void *stream, yk_tune_cfg * cfg);
+void yk_tune_end(int probe, void *stream);
+void yk_tune_reset(void);
+
+#endif
