@@ -105,11 +105,14 @@ def test_sorted_overlapping_blocks_sum(cuda, prod, oracle):
         oracle.type_free(to)
 
 
+@pytest.mark.parametrize("cut", [1, 8])
 @pytest.mark.parametrize("bl", [4, 8, 16])
-def test_sorted_blocks_segmented(cuda, prod, oracle, bl):
+def test_sorted_blocks_segmented(cuda, prod, oracle, bl, cut):
     """Sorted overlapping fixed-length blocks unpacked in several calls whose ranges
-    start and end inside blocks: each call keeps the block order within its range."""
-    rng = np.random.default_rng(100 + bl)
+    start and end inside blocks: each call keeps the block order within its range.
+    cut 8 puts every range boundary on 8 bytes (the 8-byte chunk kernel of small
+    elements); cut 1 anywhere on an element boundary."""
+    rng = np.random.default_rng(100 + bl + cut)
     nblk = 3000
     for base, op in (("int8", "sum"), ("int16", "max"), ("float", "sum"), ("double", "prod"),
                      ("c_double_complex", "sum"), ("int32", "replace"), ("int64", "bxor")):
@@ -122,7 +125,8 @@ def test_sorted_blocks_segmented(cuda, prod, oracle, bl):
         target = fill(rng, (nblk * bl // 2 + bl) * es, base)
         d_o = target.copy()
         pk, dv = dev_copy(cuda, packed), dev_copy(cuda, target)
-        cuts = sorted(set(int(c) * es for c in rng.integers(1, total // es, 6)))
+        g = max(es, 8) if cut == 8 else es
+        cuts = sorted(set(int(c) * g for c in rng.integers(1, total // g, 6)))
         bounds = [0] + cuts + [total]
         for s0, s1 in zip(bounds[:-1], bounds[1:]):
             ao = oracle.unpack(packed.ctypes.data + s0, s1 - s0, d_o.ctypes.data, 1, to, s0,

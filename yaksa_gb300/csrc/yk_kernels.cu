@@ -954,6 +954,68 @@ yk_owner_lane_kernel(const __grid_constant__ yk_launch L, int rshift)
     }
 }
 
+/* The same for elements of 1, 2 or 4 bytes, one 8-byte packed chunk per lane: the
+ * chunk's elements share one block (blocks are a multiple of 8 bytes long and the range
+ * starts on 8 bytes, checked on the host), so its displacement words and the packed
+ * load serve 8/es elements. */
+template <int BT, int OP>
+__global__ void __launch_bounds__(YK_THREADS)
+yk_owner_chunk_kernel(const __grid_constant__ yk_launch L, int rshift)
+{
+    typedef typename yk_elem<BT>::T T;
+    constexpr uint32_t es = (uint32_t) sizeof(T);
+    constexpr int E = 8 / (int) es;
+    const uint32_t R = 1u << rshift;
+    const yk_level & lv = L.desc.lv[0];
+    const uint32_t p0 = (uint32_t) L.p0, p1 = (uint32_t) (L.p0 + L.nbytes);
+    const uint32_t nblk = (uint32_t) lv.count;
+    const uint32_t nchunks = (uint32_t) (L.nbytes / 8);
+    const uint64_t *packed8 = (const uint64_t *) L.packed;      /* chunk 0 is byte p0 */
+    const T *packed = (const T *) L.packed;
+    char *typed = L.typed + L.desc.base;
+    for (uint32_t u = blockIdx.x * YK_THREADS + threadIdx.x; u < nchunks; u += gridDim.x * YK_THREADS) {
+        const uint32_t p = p0 + u * 8;
+        const uint32_t b = p >> rshift;
+        const int64_t d = __ldg(lv.disp + b);
+        const int64_t dp = b > 0 ? __ldg(lv.disp + b - 1) : 0;
+        const int64_t dn = b + 1 < nblk ? __ldg(lv.disp + b + 1) : INT64_MAX;
+        union {
+            uint64_t w;
+            T e[E];
+        } in;
+        in.w = __ldg(packed8 + u);
+        const int64_t x0 = d + (int64_t) (p & (R - 1));
+        bool own[E];
+        T out[E];
+#pragma unroll
+        for (int k = 0; k < E; k++) {
+            const int64_t x = x0 + (int64_t) k * es;
+            /* an earlier in-range block owns this element */
+            own[k] = !(b > 0 && x < dp + (int64_t) R && (b - 1) * R + (uint32_t) (x - dp) >= p0);
+            if (own[k])
+                out[k] = *(const T *) (typed + x);
+        }
+#pragma unroll
+        for (int k = 0; k < E; k++) {
+            if (!own[k])
+                continue;
+            const int64_t x = x0 + (int64_t) k * es;
+            yk_elem<BT>::op(OP, in.e[k], out[k]);
+            /* the blocks after this one that start at or before x, in block order */
+            int64_t dd = dn;
+            for (uint32_t bb = b + 1; bb < nblk && dd <= x;) {
+                const uint64_t pp = ((uint64_t) bb << rshift) + (uint64_t) (x - dd);
+                if (pp >= p1)
+                    break;
+                yk_elem<BT>::op(OP, __ldg(packed + ((uint32_t) pp - p0) / es), out[k]);
+                bb++;
+                dd = bb < nblk ? __ldg(lv.disp + bb) : INT64_MAX;
+            }
+            *(T *) (typed + x) = out[k];
+        }
+    }
+}
+
 /* Sorted blocks: descriptor = IDX(nblk, disp sorted ascending, cps = R) over a run of
  * R bytes of one base type.  Every target element that receives data gets exactly one
  * owner: the thread of its first in-range contributor, which applies the
@@ -1562,13 +1624,29 @@ extern "C" int yk_cuda_launch_pup_cfg(const yk_launch * l, void *stream, int uni
     return (int) cudaGetLastError();
 }
 
+/* the 8-byte chunk form exists for elements smaller than 8 bytes only */
+template <int BT, int O>
+static bool yk_owner_chunk_launch(const yk_launch & c, int rshift, cudaStream_t s, unsigned g,
+                                  bool chunk)
+{
+    if constexpr (sizeof(typename yk_elem<BT>::T) < 8) {
+        if (chunk) {
+            yk_owner_chunk_kernel<BT, O><<<g, YK_THREADS, 0, s>>>(c, rshift);
+            return true;
+        }
+    }
+    return false;
+}
+
 /* yk_owner_lane_kernel for (base type, operator) pairs in the operator table; false
  * when the pair has no instance (the caller falls back to the runtime-op kernels) */
 template <int BT>
-static bool yk_owner_lane_int(const yk_launch & c, int rshift, cudaStream_t s, unsigned g)
+static bool yk_owner_lane_int(const yk_launch & c, int rshift, cudaStream_t s, unsigned g, bool chunk)
 {
     switch ((int) c.op) {
-#define YK_OL(O) case O: yk_owner_lane_kernel<BT, O><<<g, YK_THREADS, 0, s>>>(c, rshift); return true
+#define YK_OL(O) case O: if (!yk_owner_chunk_launch<BT, O>(c, rshift, s, g, chunk))           \
+                             yk_owner_lane_kernel<BT, O><<<g, YK_THREADS, 0, s>>>(c, rshift);  \
+                         return true
         YK_OL(OP_MAX); YK_OL(OP_MIN); YK_OL(OP_SUM); YK_OL(OP_PROD); YK_OL(OP_LAND); YK_OL(OP_BAND);
         YK_OL(OP_LOR); YK_OL(OP_BOR); YK_OL(OP_LXOR); YK_OL(OP_BXOR); YK_OL(OP_REPLACE);
     }
@@ -1576,7 +1654,7 @@ static bool yk_owner_lane_int(const yk_launch & c, int rshift, cudaStream_t s, u
 }
 
 template <int BT>
-static bool yk_owner_lane_flt(const yk_launch & c, int rshift, cudaStream_t s, unsigned g)
+static bool yk_owner_lane_flt(const yk_launch & c, int rshift, cudaStream_t s, unsigned g, bool chunk)
 {
     switch ((int) c.op) {
         YK_OL(OP_MAX); YK_OL(OP_MIN); YK_OL(OP_SUM); YK_OL(OP_PROD); YK_OL(OP_REPLACE);
@@ -1585,7 +1663,7 @@ static bool yk_owner_lane_flt(const yk_launch & c, int rshift, cudaStream_t s, u
 }
 
 template <int BT>
-static bool yk_owner_lane_cplx(const yk_launch & c, int rshift, cudaStream_t s, unsigned g)
+static bool yk_owner_lane_cplx(const yk_launch & c, int rshift, cudaStream_t s, unsigned g, bool chunk)
 {
     switch ((int) c.op) {
         YK_OL(OP_SUM); YK_OL(OP_PROD); YK_OL(OP_REPLACE);
@@ -1596,17 +1674,22 @@ static bool yk_owner_lane_cplx(const yk_launch & c, int rshift, cudaStream_t s, 
 
 static bool yk_owner_lane_launch(const yk_launch & c, int bt, int rshift, cudaStream_t s)
 {
-    const uint64_t units = c.nbytes / (uint64_t) yk_bt_size(bt);
+    const uint64_t es = (uint64_t) yk_bt_size(bt);
+    /* 8-byte chunks for small elements: blocks a multiple of 8 bytes, range and packed
+     * pointer on 8 bytes */
+    const bool chunk = es < 8 && rshift >= 3 && c.p0 % 8 == 0 && c.nbytes % 8 == 0 &&
+        (uintptr_t) c.packed % 8 == 0;
+    const uint64_t units = c.nbytes / (chunk ? 8 : es);
     const unsigned g = yk_grid(units, YK_THREADS, 16);
     switch (bt) {
-        case YK_BT_I8: return yk_owner_lane_int<YK_BT_I8>(c, rshift, s, g);
-        case YK_BT_I16: return yk_owner_lane_int<YK_BT_I16>(c, rshift, s, g);
-        case YK_BT_I32: return yk_owner_lane_int<YK_BT_I32>(c, rshift, s, g);
-        case YK_BT_I64: return yk_owner_lane_int<YK_BT_I64>(c, rshift, s, g);
-        case YK_BT_F32: return yk_owner_lane_flt<YK_BT_F32>(c, rshift, s, g);
-        case YK_BT_F64: return yk_owner_lane_flt<YK_BT_F64>(c, rshift, s, g);
-        case YK_BT_C32: return yk_owner_lane_cplx<YK_BT_C32>(c, rshift, s, g);
-        case YK_BT_C64: return yk_owner_lane_cplx<YK_BT_C64>(c, rshift, s, g);
+        case YK_BT_I8: return yk_owner_lane_int<YK_BT_I8>(c, rshift, s, g, chunk);
+        case YK_BT_I16: return yk_owner_lane_int<YK_BT_I16>(c, rshift, s, g, chunk);
+        case YK_BT_I32: return yk_owner_lane_int<YK_BT_I32>(c, rshift, s, g, chunk);
+        case YK_BT_I64: return yk_owner_lane_int<YK_BT_I64>(c, rshift, s, g, false);
+        case YK_BT_F32: return yk_owner_lane_flt<YK_BT_F32>(c, rshift, s, g, chunk);
+        case YK_BT_F64: return yk_owner_lane_flt<YK_BT_F64>(c, rshift, s, g, false);
+        case YK_BT_C32: return yk_owner_lane_cplx<YK_BT_C32>(c, rshift, s, g, false);
+        case YK_BT_C64: return yk_owner_lane_cplx<YK_BT_C64>(c, rshift, s, g, false);
     }
     return false;
 }
