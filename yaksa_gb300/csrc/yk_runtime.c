@@ -1388,6 +1388,7 @@ struct yaksa_gb300_graph_s {
     cudaGraphExec_t exec;
     yk_type **types;            /* held while the graph exists */
     int ntypes;
+    int nkernels;               /* kernel nodes: launches per replay */
 };
 
 int yaksa_gb300_graph_create(yaksa_gb300_pup_t * ops, const int *batch_ends, int nbatches,
@@ -1444,16 +1445,32 @@ int yaksa_gb300_graph_create(yaksa_gb300_pup_t * ops, const int *batch_ends, int
     if (!rc)
         rc = cuda_err(cudaStreamBeginCapture(cs, cudaStreamCaptureModeRelaxed), "capture");
     if (!rc) {
+        /* captured launches run at replay: counted there, not here */
+        uint64_t l0 = __atomic_load_n(&R.launches, __ATOMIC_RELAXED);
         int start = 0;
         for (int b = 0; b < nbatches && !rc; b++) {
             rc = batch_run(ops + start, batch_ends[b] - start, info, cs);
             start = batch_ends[b];
         }
+        __atomic_sub_fetch(&R.launches, __atomic_load_n(&R.launches, __ATOMIC_RELAXED) - l0,
+                           __ATOMIC_RELAXED);
         cudaError_t e = cudaStreamEndCapture(cs, &g->graph);
         if (!rc)
             rc = cuda_err(e, "capture");
         if (!rc)
             rc = cuda_err(cudaGraphInstantiate(&g->exec, g->graph, 0), "cudaGraphInstantiate");
+        size_t nn = 0;
+        if (!rc && cudaGraphGetNodes(g->graph, NULL, &nn) == cudaSuccess && nn) {
+            cudaGraphNode_t *nodes = malloc(nn * sizeof(cudaGraphNode_t));
+            if (nodes && cudaGraphGetNodes(g->graph, nodes, &nn) == cudaSuccess)
+                for (size_t i = 0; i < nn; i++) {
+                    enum cudaGraphNodeType ty;
+                    if (cudaGraphNodeGetType(nodes[i], &ty) == cudaSuccess &&
+                        ty == cudaGraphNodeTypeKernel)
+                        g->nkernels++;
+                }
+            free(nodes);
+        }
     }
     if (cs)
         cudaStreamDestroy(cs);
@@ -1470,7 +1487,7 @@ int yaksa_gb300_graph_launch(yaksa_gb300_graph_t g, void *stream)
     if (!g)
         return YAKSA_ERR__INTERNAL;
     cudaStream_t s = stream ? *(cudaStream_t *) stream : R.stream;
-    __atomic_add_fetch(&R.launches, 1, __ATOMIC_RELAXED);
+    __atomic_add_fetch(&R.launches, (uint64_t) g->nkernels, __ATOMIC_RELAXED);
     return cuda_err(cudaGraphLaunch(g->exec, s), "cudaGraphLaunch");
 }
 
