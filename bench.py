@@ -764,6 +764,28 @@ def main():
             e1.synchronize()
             per[d].append(e0.elapsed_time(e1) * 1e-3)
 
+    # a reference point: PyTorch's own strided-copy kernels moving the same six faces
+    # (one copy per face and direction, the same cold L2)
+    s3, d3 = src.view(N, N, N), dst.view(N, N, N)
+    views = [s3[:, :, :2], s3[:, :, N - 2:], s3[:, :2, :], s3[:, N - 2:, :], s3[:2], s3[N - 2:]]
+    dviews = [d3[:, :, :2], d3[:, :, N - 2:], d3[:, :2, :], d3[:, N - 2:, :], d3[:2], d3[N - 2:]]
+    pk_views = [pk.view(torch.float32).view(v.shape) for pk, v in zip(packed, views)]
+    torch_t = {"pack": [], "unpack": []}
+    for rep in range(5):
+        for d in ("pack", "unpack"):
+            flush()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            for i in range(len(faces)):
+                if d == "pack":
+                    pk_views[i].copy_(views[i])
+                else:
+                    dviews[i].copy_(pk_views[i])
+            e1.record()
+            e1.synchronize()
+            torch_t[d].append(e0.elapsed_time(e1) * 1e-3)
+    torch_ref = {d: statistics.median(v) * 1e6 for d, v in torch_t.items()}
+
     clocks = Clocks(os.path.join(ROOT, "gpurun_out", "clocks.csv")
                     if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/yk_clocks.csv")
     clocks.start()
@@ -880,6 +902,10 @@ def main():
             "clocks": clk,
             "e2e": e2e,
             "e2e_host_grid": e2e_host,
+            "torch_strided_copy": {"pack_us": torch_ref["pack"], "unpack_us": torch_ref["unpack"],
+                                   "note": "PyTorch copy_ of the same six face views, one kernel per "
+                                           "face and direction, cold L2 (a reference point for the "
+                                           "launch_us of the roofline kernel)"},
             "wall_s": wall}
     if not args.no_stream:
         # the metric's second half: batched (persistent server) vs plain p50/p99 on the
