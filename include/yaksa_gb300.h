@@ -120,6 +120,11 @@ int yaksa_gb300_serve_trace(yaksa_gb300_pup_t * ops, const double *arrival_s, in
  * environment keeps the default shapes. */
 int yaksa_gb300_autotune_stats(uint32_t * classes, uint32_t * decided, uint64_t * probes);
 
+/* Test hook (no counterpart in the reference): the library's next `n` device or pinned
+ * allocations fail as if memory were exhausted, without calling the allocator, so that
+ * error paths are exercised with no GPU fault.  0 clears it. */
+int yaksa_gb300_debug_fail_alloc(int n);
+
 /* Runtime counters since load: kernel launches, calls served in place (device or
  * GPU-addressable host memory), calls that staged host data through device memory,
  * and contiguous calls served by one copy. */

@@ -139,6 +139,8 @@ def load_library(path):
     if hasattr(lib, "yaksa_gb300_stats"):
         lib.yaksa_gb300_stats.restype = ctypes.c_int
         lib.yaksa_gb300_stats.argtypes = [ctypes.POINTER(_u64)] * 4
+        lib.yaksa_gb300_debug_fail_alloc.restype = ctypes.c_int
+        lib.yaksa_gb300_debug_fail_alloc.argtypes = [ctypes.c_int]
         lib.yaksa_gb300_autotune_stats.restype = ctypes.c_int
         lib.yaksa_gb300_autotune_stats.argtypes = [ctypes.POINTER(ctypes.c_uint32),
                                                    ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(_u64)]

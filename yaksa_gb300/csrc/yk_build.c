@@ -116,6 +116,27 @@ static void add_seg(hbuild * b, int64_t off, uint64_t len, int bt)
     b->nseg++;
 }
 
+/* Host-side failure injection for tests: the next `n` device allocations of the
+ * library report failure without calling the allocator (no GPU fault is involved). */
+static int yk_fail_next = 0;
+
+int yaksa_gb300_debug_fail_alloc(int n)
+{
+    __atomic_store_n(&yk_fail_next, n > 0 ? n : 0, __ATOMIC_RELEASE);
+    return YAKSA_SUCCESS;
+}
+
+int yk_fail_injected(void)
+{
+    int v = __atomic_load_n(&yk_fail_next, __ATOMIC_ACQUIRE);
+    while (v > 0) {
+        if (__atomic_compare_exchange_n(&yk_fail_next, &v, v - 1, 0, __ATOMIC_ACQ_REL,
+                                        __ATOMIC_ACQUIRE))
+            return 1;
+    }
+    return 0;
+}
+
 /* field layout of a pair builtin: (offset, size, base type) x 2 */
 int yk_pair_fields(yaksa_type_t h, size_t off[2], size_t sz[2], int bt[2])
 {
@@ -545,7 +566,7 @@ static int upload(hbuild * b, yk_devdesc * dd, int to_device)
             return YAKSA_ERR__OUT_OF_MEM;
         if (!to_device) {
             dev = host;
-        } else if (cudaMalloc((void **) &dev, bytes) != cudaSuccess) {
+        } else if (yk_fail_injected() || cudaMalloc((void **) &dev, bytes) != cudaSuccess) {
             free(host);
             return YAKSA_ERR__OUT_OF_MEM;
         }
@@ -712,17 +733,20 @@ static int build(yk_type * t, int typed, yk_devdesc * dd, int to_device)
     return rc;
 }
 
+/* Allocation failures are not cached: the next request for the type retries the
+ * build, so a transient shortage of device memory does not disable a type for good. */
 int yk_desc_get(yk_type * t, int typed, yk_devdesc ** out)
 {
     yk_devdesc *dd = typed ? &t->typed_desc : &t->bytes_desc;
     pthread_mutex_lock(&t->desc_mutex);
     if (!dd->built) {
         dd->status = build(t, typed, dd, 1);
-        dd->built = 1;
+        dd->built = dd->status != YAKSA_ERR__OUT_OF_MEM;
     }
+    int rc = dd->status;
     pthread_mutex_unlock(&t->desc_mutex);
     *out = dd;
-    return dd->status;
+    return rc;
 }
 
 /* The descriptor with its tables left on the host heap (built once, kept with the
@@ -734,11 +758,12 @@ int yk_desc_get_host(yk_type * t, int typed, yk_devdesc ** out)
     pthread_mutex_lock(&t->desc_mutex);
     if (!dd->built) {
         dd->status = build(t, typed, dd, 0);
-        dd->built = 1;
+        dd->built = dd->status != YAKSA_ERR__OUT_OF_MEM;
     }
+    int rc = dd->status;
     pthread_mutex_unlock(&t->desc_mutex);
     *out = dd;
-    return dd->status;
+    return rc;
 }
 
 /* the type's descriptor with the element level VEC(count, extent, size) in front

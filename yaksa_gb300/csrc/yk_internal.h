@@ -92,6 +92,8 @@ int yk_desc_get(yk_type * t, int typed, yk_devdesc ** out);
 int yk_desc_get_host(yk_type * t, int typed, yk_devdesc ** out);
 /* field layout of a pair builtin (float_int, short_int, ...): 1 if h is one */
 int yk_pair_fields(yaksa_type_t h, size_t off[2], size_t sz[2], int bt[2]);
+/* 1 when a test asked the next device allocation to fail (yaksa_gb300_debug_fail_alloc) */
+int yk_fail_injected(void);
 /* yk_noalloc.cu: the current device's address of the static descriptor scratch */
 int yk_noalloc_scratch(void **ptr, size_t * bytes);
 void yk_desc_release(yk_type * t);

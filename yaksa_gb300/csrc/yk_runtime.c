@@ -531,14 +531,16 @@ static int run_staged(const yk_plan * p, cudaStream_t s)
     size_t span = (size_t) (p->hi - p->lo);
     int rc = YAKSA_SUCCESS;
     if (p->staged & 1) {
-        rc = cuda_err(cudaMallocAsync(&scr_t, span, s), "cudaMallocAsync");
+        rc = yk_fail_injected() ? YAKSA_ERR__OUT_OF_MEM :
+            cuda_err(cudaMallocAsync(&scr_t, span, s), "cudaMallocAsync");
         if (!rc)
             rc = cuda_err(cudaMemcpyAsync(scr_t, p->typed + p->lo, span, cudaMemcpyHostToDevice, s),
                           "stage in");
         dtyped = (char *) scr_t - p->lo;
     }
     if (!rc && (p->staged & 2)) {
-        rc = cuda_err(cudaMallocAsync(&scr_p, n, s), "cudaMallocAsync");
+        rc = yk_fail_injected() ? YAKSA_ERR__OUT_OF_MEM :
+            cuda_err(cudaMallocAsync(&scr_p, n, s), "cudaMallocAsync");
         if (!rc && (p->dir == 1 || p->op != YAKSA_OP__REPLACE))
             rc = cuda_err(cudaMemcpyAsync(scr_p, p->packed, n, cudaMemcpyHostToDevice, s),
                           "stage in");
@@ -997,7 +999,8 @@ struct yaksa_gb300_server_s {
 static void *pinned(size_t n)
 {
     void *p = NULL;
-    if (cudaHostAlloc(&p, n, cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess)
+    if (yk_fail_injected() ||
+        cudaHostAlloc(&p, n, cudaHostAllocMapped | cudaHostAllocPortable) != cudaSuccess)
         return NULL;
     memset(p, 0, n);
     return p;
@@ -1023,6 +1026,7 @@ int yaksa_gb300_server_create(uint32_t ring_requests, uint64_t budget_bytes,
     S->ctl = pinned(64);
     S->slots = calloc(S->qr, sizeof(yk_srv_slot));
     if (!S->reqs || !S->items || !S->item_done || !S->ctl || !S->slots ||
+        yk_fail_injected() ||
         cudaMalloc((void **) &S->next_item, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMemset(S->next_item, 0, sizeof(unsigned long long)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking) != cudaSuccess) {
