@@ -28,6 +28,7 @@
 #include <cuda_runtime_api.h>
 #include "yk_internal.h"
 #include "yk_tune.h"
+#include <nvtx3/nvToolsExt.h>
 #include "yaksa_gb300.h"
 
 typedef struct {
@@ -593,9 +594,25 @@ static int complete(yk_type * t, int mode, cudaStream_t s, yaksa_request_t * req
     return rc;
 }
 
+static int pup(int dir, const void *packed_in, void *packed_out, char *typed, uintptr_t count,
+               yk_type * t, uintptr_t offset, uintptr_t maxbytes, uintptr_t * actual,
+               yk_info * info, yaksa_op_t op, int mode, void *stream, yaksa_request_t * request);
+
+/* every public pack/unpack call is one NVTX range (a no-op unless a tool is attached) */
 int yk_pup(int dir, const void *packed_in, void *packed_out, char *typed, uintptr_t count,
            yk_type * t, uintptr_t offset, uintptr_t maxbytes, uintptr_t * actual,
            yk_info * info, yaksa_op_t op, int mode, void *stream, yaksa_request_t * request)
+{
+    nvtxRangePushA(dir ? "yaksa unpack" : "yaksa pack");
+    int rc = pup(dir, packed_in, packed_out, typed, count, t, offset, maxbytes, actual, info, op,
+                 mode, stream, request);
+    nvtxRangePop();
+    return rc;
+}
+
+static int pup(int dir, const void *packed_in, void *packed_out, char *typed, uintptr_t count,
+               yk_type * t, uintptr_t offset, uintptr_t maxbytes, uintptr_t * actual,
+               yk_info * info, yaksa_op_t op, int mode, void *stream, yaksa_request_t * request)
 {
     if (request)
         *request = YAKSA_REQUEST__NULL;
@@ -787,7 +804,17 @@ static int flush_batch(yk_launch * ls, int n, cudaStream_t s)
     return rc;
 }
 
+static int batch_run_ranges(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info, cudaStream_t s);
+
 static int batch_run(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info, cudaStream_t s)
+{
+    nvtxRangePushA("yaksa batch");
+    int rc = batch_run_ranges(ops, n, info, s);
+    nvtxRangePop();
+    return rc;
+}
+
+static int batch_run_ranges(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info, cudaStream_t s)
 {
     yk_launch *ls = malloc(sizeof(yk_launch) * (n > 0 ? n : 1));
     if (!ls)
