@@ -609,10 +609,20 @@ def run_stream(nreq=10000, rate=50e3, seed=5, check=True, log=None):
         ops2 = make_ops()
         _, mk2 = yk.serve_trace(y, ops2, zero, server=s)
         torch.cuda.synchronize()
+        # latency by packed size: small (<= 64 KiB), medium (<= 4 MiB), large
+        sizes_req = np.array([k[1] for k in keys])
+        by_size = {}
+        for name, lo_, hi_ in (("small", 0, 64 << 10), ("medium", (64 << 10) + 1, 4 << 20),
+                               ("large", (4 << 20) + 1, 1 << 40)):
+            sel = lat_us[(sizes_req >= lo_) & (sizes_req <= hi_)]
+            if len(sel):
+                by_size[name] = {"n": int(len(sel)), "p50_us": float(np.percentile(sel, 50)),
+                                 "p99_us": float(np.percentile(sel, 99))}
         res[mode] = {"open_loop": {"GBps": total / mk / 1e9, "makespan_s": mk,
                                    "p50_us": float(np.percentile(lat_us, 50)),
                                    "p99_us": float(np.percentile(lat_us, 99)),
-                                   "mean_us": float(lat_us.mean()), "kernel_launches": launches},
+                                   "mean_us": float(lat_us.mean()), "kernel_launches": launches,
+                                   "by_size": by_size},
                      "closed_loop": {"GBps": total / mk2 / 1e9, "req_per_s": nreq / mk2, "makespan_s": mk2},
                      "bit_exact": not bad, "mismatched": bad[:10]}
         if log:
@@ -929,6 +939,9 @@ def main():
                         "GBps": r["server"]["open_loop"]["GBps"],
                         "capacity_GBps": r["server"]["closed_loop"]["GBps"],
                         "capacity_req_per_s": r["server"]["closed_loop"]["req_per_s"]},
+            "by_size": {"plain": r["plain"]["open_loop"]["by_size"],
+                        "batched": r["server"]["open_loop"]["by_size"],
+                        "classes": "small <= 64 KiB < medium <= 4 MiB < large"},
             "capacity_ratio": r["server_over_plain"]["closed_loop_throughput"],
             "p99_ratio": r["server_over_plain"]["open_loop_p99"],
             "bit_exact": r["plain"]["bit_exact"] and r["server"]["bit_exact"],

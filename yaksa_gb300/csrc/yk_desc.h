@@ -142,7 +142,8 @@ typedef struct {
 typedef struct {
     yk_launch *reqs;            /* request records (host-mapped, written by the host) */
     yk_item *items;             /* work items (host-mapped, written by the host) */
-    volatile uint64_t *item_done;       /* item sequence + 1 once done (written by the GPU) */
+    unsigned long long *req_done;       /* per request slot: items finished (host-mapped,
+                                         * reset by the host, counted by the GPU) */
     const volatile uint64_t *items_published;   /* items visible to the GPU (host) */
     const volatile int *stop;   /* host asks resident CTAs to leave */
     unsigned long long *next_item;      /* device memory: next item to claim */

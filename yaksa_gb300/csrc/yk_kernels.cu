@@ -1299,23 +1299,31 @@ __device__ __forceinline__ bool yk_item_ok(const yk_item & it, const yk_launch &
  * item, and publish its completion.  Every wait is bounded: a CTA that finds no new
  * item for max_idle_spins polls, or sees the stop flag, leaves; the host relaunches the
  * kernel when items are pending and no CTA is resident. */
-__global__ void __launch_bounds__(YK_THREADS)
+__global__ void __launch_bounds__(YK_THREADS, 6)
 yk_server_kernel(const __grid_constant__ yk_server_args A)
 {
     __shared__ yk_launch sL;
     __shared__ uint64_t s_item;
     __shared__ int s_cmd;
     __shared__ yk_item s_it;
+    uint64_t pub = 0;           /* thread 0: last published count read from the host */
     for (;;) {
         if (threadIdx.x == 0) {
             int cmd = 0;
+            /* idle polls of the host-mapped counter back off from 64 ns to 2 us: many
+             * resident CTAs polling at full rate would load the C2C link the host's own
+             * submissions cross */
+            unsigned nap = 64;
             for (uint32_t spins = 0;; spins++) {
                 if (*A.stop) {
                     cmd = 2;
                     break;
                 }
-                uint64_t pub = yk_ld_acquire_sys(A.items_published);
+                /* the published count only grows: re-read it from host memory only when
+                 * the claim counter has caught up with the copy held here */
                 unsigned long long nxt = *(volatile unsigned long long *) A.next_item;
+                if (nxt >= pub)
+                    pub = yk_ld_acquire_sys(A.items_published);
                 if (nxt < pub) {
                     if (atomicCAS(A.next_item, nxt, nxt + 1) == nxt) {
                         s_item = nxt;
@@ -1332,7 +1340,8 @@ yk_server_kernel(const __grid_constant__ yk_server_args A)
                     cmd = 3;
                     break;
                 }
-                __nanosleep(200);
+                __nanosleep(nap);
+                nap = nap < 2048 ? 2 * nap : 2048;
             }
             if (cmd == 1) {
                 /* the item carries its own sequence number: re-read (bounded) until the
@@ -1375,8 +1384,13 @@ yk_server_kernel(const __grid_constant__ yk_server_args A)
             /* unusable item: count it, mark it done, move on (never loop on it) */
             if (threadIdx.x == 0) {
                 atomicAdd((unsigned int *) &A.status[2], 1u);
-                __threadfence_system();
-                A.item_done[s_item % A.qi] = s_item + 1;
+                /* counted for its request only when the item record itself was current;
+                 * otherwise the request stays incomplete and the host's bounded wait
+                 * reports the error */
+                if (s_it.seq == s_item) {
+                    __threadfence_system();
+                    atomicAdd_system(&A.req_done[s_it.req % A.qr], 1ull);
+                }
             }
             __syncthreads();
             continue;
@@ -1434,8 +1448,9 @@ yk_server_kernel(const __grid_constant__ yk_server_args A)
         }
         __syncthreads();
         if (threadIdx.x == 0) {
+            /* the item's bytes become visible before its request's count moves */
             __threadfence_system();
-            A.item_done[s_item % A.qi] = s_item + 1;
+            atomicAdd_system(&A.req_done[it.req % A.qr], 1ull);
         }
     }
 }

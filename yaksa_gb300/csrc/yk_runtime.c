@@ -38,6 +38,8 @@ typedef struct {
     void *scratch[2];           /* staged buffers released at completion */
 } yk_req;
 
+#define YK_LIB_STREAMS 4
+
 static struct {
     pthread_mutex_t mu;
     int ready;
@@ -45,7 +47,11 @@ static struct {
     int device;
     int pageable_access;        /* the GPU reads/writes pageable host memory (ATS) */
     int host_ptr_ok;            /* registered host memory uses the host address */
-    cudaStream_t stream;
+    /* library streams: requests that are not stream-ordered go round robin over
+     * these, so independent requests (whose order the API leaves open) overlap on the
+     * GPU; streams[0] is also the default stream of graph replays */
+    cudaStream_t streams[YK_LIB_STREAMS];
+    unsigned next_stream;
     yk_req *reqs;
     size_t nreqs;
     size_t *freeidx;            /* stack of free request slots */
@@ -54,7 +60,15 @@ static struct {
     size_t nev, capev;
     /* counters (yaksa_gb300_stats) */
     uint64_t launches, staged_calls, direct_calls, memcpy_calls;
-} R = { PTHREAD_MUTEX_INITIALIZER, 0, 0, 0, 0, 0, NULL, NULL, 0, NULL, 0, NULL, 0, 0, 0, 0, 0, 0 };
+} R = { .mu = PTHREAD_MUTEX_INITIALIZER };
+
+/* a library stream for a request that is not stream-ordered (round robin) */
+static cudaStream_t lib_stream(void)
+{
+    unsigned k = __atomic_fetch_add(&R.next_stream, 1, __ATOMIC_RELAXED);
+    return R.streams[k % YK_LIB_STREAMS];
+}
+
 
 static int cuda_err(cudaError_t e, const char *what)
 {
@@ -97,7 +111,8 @@ static int runtime_ready(void)
             const char *l2 = getenv("YAKSA_GB300_L2_FETCH_BYTES");
             if (l2 && atoi(l2) > 0)
                 cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t) atoi(l2));
-            e = cudaStreamCreateWithFlags(&R.stream, cudaStreamNonBlocking);
+            for (int k = 0; k < YK_LIB_STREAMS && e == cudaSuccess; k++)
+                e = cudaStreamCreateWithFlags(&R.streams[k], cudaStreamNonBlocking);
             if (e != cudaSuccess) {
                 cuda_err(e, "cudaStreamCreate");
                 R.failed = 1;
@@ -117,7 +132,8 @@ void yk_runtime_finalize(void)
     yk_tune_reset();
     pthread_mutex_lock(&R.mu);
     if (R.ready) {
-        cudaStreamSynchronize(R.stream);
+        for (int k = 0; k < YK_LIB_STREAMS; k++)
+            cudaStreamSynchronize(R.streams[k]);
         for (size_t i = 0; i < R.nreqs; i++)
             if (R.reqs[i].in_use) {
                 cudaEventDestroy(R.reqs[i].ev);
@@ -126,7 +142,8 @@ void yk_runtime_finalize(void)
         for (size_t i = 0; i < R.nev; i++)
             cudaEventDestroy(R.evpool[i]);
         R.nev = 0;
-        cudaStreamDestroy(R.stream);
+        for (int k = 0; k < YK_LIB_STREAMS; k++)
+            cudaStreamDestroy(R.streams[k]);
         R.ready = 0;
     }
     free(R.reqs);
@@ -621,7 +638,7 @@ static int pup(int dir, const void *packed_in, void *packed_out, char *typed, ui
     int rc = plan(dir, packed_in, packed_out, typed, count, t, offset, maxbytes, info, op, &p);
     if (rc || p.b1 == p.b0)
         return rc;
-    cudaStream_t s = (mode == YK_MODE_STREAM && stream) ? *(cudaStream_t *) stream : R.stream;
+    cudaStream_t s = (mode == YK_MODE_STREAM && stream) ? *(cudaStream_t *) stream : lib_stream();
     if (p.staged) {
         rc = run_staged(&p, s);
         if (!rc)
@@ -865,7 +882,7 @@ int yaksa_gb300_pup_batch_stream(yaksa_gb300_pup_t * ops, int n, yaksa_info_t in
     int rc = runtime_ready();
     if (rc)
         return rc;
-    cudaStream_t s = stream ? *(cudaStream_t *) stream : R.stream;
+    cudaStream_t s = stream ? *(cudaStream_t *) stream : lib_stream();
     return batch_run(ops, n, info, s);
 }
 
@@ -874,10 +891,11 @@ int yaksa_gb300_pup_batch(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info)
     int rc = runtime_ready();
     if (rc)
         return rc;
-    rc = batch_run(ops, n, info, R.stream);
+    cudaStream_t s = lib_stream();
+    rc = batch_run(ops, n, info, s);
     if (rc)
         return rc;
-    return complete(NULL, YK_MODE_BLOCKING, R.stream, NULL);
+    return complete(NULL, YK_MODE_BLOCKING, s, NULL);
 }
 
 int yaksa_gb300_ipup_batch(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info,
@@ -887,10 +905,11 @@ int yaksa_gb300_ipup_batch(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info,
     int rc = runtime_ready();
     if (rc)
         return rc;
-    rc = batch_run(ops, n, info, R.stream);
+    cudaStream_t s = lib_stream();
+    rc = batch_run(ops, n, info, s);
     if (rc)
         return rc;
-    return complete(NULL, YK_MODE_NONBLOCKING, R.stream, request);
+    return complete(NULL, YK_MODE_NONBLOCKING, s, request);
 }
 
 /* ------------------------------------------------------------------------- */
@@ -1000,7 +1019,6 @@ int yaksa_gb300_pup_noalloc(yaksa_gb300_pup_t * o, void *stream)
 typedef struct {
     uint64_t seq;               /* request sequence number (ticket) */
     uint64_t item0, nitems;
-    uint64_t checked;           /* leading items already seen done */
     uint64_t bytes;
     yk_type *t;
     int busy;
@@ -1013,7 +1031,7 @@ struct yaksa_gb300_server_s {
     uint32_t qr, qi;
     yk_launch *reqs;            /* pinned, mapped */
     yk_item *items;             /* pinned, mapped */
-    uint64_t *item_done;        /* pinned, mapped */
+    unsigned long long *req_done;       /* pinned, mapped: items finished per request slot */
     uint64_t *ctl;              /* pinned, mapped: [0] items published, [1] stop, [2] status */
     unsigned long long *next_item;      /* device */
     yk_srv_slot *slots;
@@ -1049,10 +1067,10 @@ int yaksa_gb300_server_create(uint32_t ring_requests, uint64_t budget_bytes,
     S->budget = budget_bytes ? budget_bytes : (64ull << 30);
     S->reqs = pinned(sizeof(yk_launch) * S->qr);
     S->items = pinned(sizeof(yk_item) * S->qi);
-    S->item_done = pinned(sizeof(uint64_t) * S->qi);
+    S->req_done = pinned(sizeof(unsigned long long) * S->qr);
     S->ctl = pinned(64);
     S->slots = calloc(S->qr, sizeof(yk_srv_slot));
-    if (!S->reqs || !S->items || !S->item_done || !S->ctl || !S->slots ||
+    if (!S->reqs || !S->items || !S->req_done || !S->ctl || !S->slots ||
         yk_fail_injected() ||
         cudaMalloc((void **) &S->next_item, sizeof(unsigned long long)) != cudaSuccess ||
         cudaMemset(S->next_item, 0, sizeof(unsigned long long)) != cudaSuccess ||
@@ -1064,14 +1082,14 @@ int yaksa_gb300_server_create(uint32_t ring_requests, uint64_t budget_bytes,
     S->ctas = yk_cuda_server_ctas();
     S->args.reqs = S->reqs;
     S->args.items = S->items;
-    S->args.item_done = S->item_done;
+    S->args.req_done = S->req_done;
     S->args.items_published = &S->ctl[0];
     S->args.stop = (const volatile int *) &S->ctl[1];
     S->args.next_item = S->next_item;
     S->args.status = (volatile uint32_t *) &S->ctl[2];
     S->args.qi = S->qi;
     S->args.qr = S->qr;
-    S->args.max_idle_spins = 20000;     /* a few milliseconds without work */
+    S->args.max_idle_spins = 4000;      /* ~8 ms without work at the 2 us poll interval */
     *server = S;
     return YAKSA_SUCCESS;
 }
@@ -1085,13 +1103,9 @@ static int server_progress_locked(struct yaksa_gb300_server_s *S)
         yk_srv_slot *sl = &S->slots[s % S->qr];
         if (!sl->busy)
             continue;
-        while (sl->checked < sl->nitems) {
-            uint64_t i = sl->item0 + sl->checked;
-            if (__atomic_load_n(&S->item_done[i % S->qi], __ATOMIC_ACQUIRE) != i + 1)
-                break;
-            sl->checked++;
-        }
-        if (sl->checked < sl->nitems)
+        /* one word per request: the GPU counts the request's finished items */
+        if (sl->nitems &&
+            __atomic_load_n(&S->req_done[s % S->qr], __ATOMIC_ACQUIRE) < sl->nitems)
             continue;
         sl->busy = 0;
         S->inflight_bytes -= sl->bytes;
@@ -1199,13 +1213,13 @@ int yaksa_gb300_server_submit(yaksa_gb300_server_t S, yaksa_gb300_pup_t * o, yak
     sl->seq = seq;
     sl->item0 = S->item_seq;
     sl->nitems = nitems;
-    sl->checked = 0;
     sl->bytes = n;
     sl->busy = 1;
     sl->t = t;
     yk_type_ref(t);
     S->inflight_bytes += n;
     if (nitems) {
+        __atomic_store_n(&S->req_done[slot], 0ull, __ATOMIC_RELAXED);
         memcpy(&S->reqs[slot], &L, sizeof(L));
         for (uint64_t i = 0; i < nitems; i++) {
             yk_item *it = &S->items[(S->item_seq + i) % S->qi];
@@ -1304,8 +1318,8 @@ int yaksa_gb300_server_destroy(yaksa_gb300_server_t S)
             cudaFreeHost(S->reqs);
         if (S->items)
             cudaFreeHost(S->items);
-        if (S->item_done)
-            cudaFreeHost(S->item_done);
+        if (S->req_done)
+            cudaFreeHost(S->req_done);
         if (S->ctl)
             cudaFreeHost(S->ctl);
     }
@@ -1517,7 +1531,7 @@ int yaksa_gb300_graph_launch(yaksa_gb300_graph_t g, void *stream)
 {
     if (!g)
         return YAKSA_ERR__INTERNAL;
-    cudaStream_t s = stream ? *(cudaStream_t *) stream : R.stream;
+    cudaStream_t s = stream ? *(cudaStream_t *) stream : R.streams[0];
     __atomic_add_fetch(&R.launches, (uint64_t) g->nkernels, __ATOMIC_RELAXED);
     return cuda_err(cudaGraphLaunch(g->exec, s), "cudaGraphLaunch");
 }
