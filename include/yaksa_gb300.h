@@ -58,7 +58,7 @@ int yaksa_gb300_graph_free(yaksa_gb300_graph_t graph);
 
 /* Request server (no counterpart in the reference, whose progress engine launches
  * one kernel per request chunk, src/backend/src/yaksuri_progress.c:2862-3088).  A
- * persistent kernel keeps one CTA group resident per SM and drains a work queue in
+ * persistent kernel keeps six CTAs resident per SM and drains a work queue in
  * pinned, device-mapped host memory; requests are split into work items of up to
  * 512 KiB of packed bytes, so requests of any size and type share the GPU as they
  * arrive (continuous batching).
