@@ -66,8 +66,14 @@ def build(verbose=False, extra_nvcc=()):
     if verbose:
         for r in results:
             sys.stderr.write(r.stderr)
+    # export the yaksa_* API only: internal yk_* symbols and the static CUDA runtime stay
+    # private, so the library can sit in any application without symbol clashes
+    vscript = os.path.join(BUILD, "exports.map")
+    with open(vscript, "w") as f:
+        f.write("{ global: yaksa_*; local: *; };\n")
     _run([nvcc, *ARCH, "-shared", "-o", LIB, *objs, "-Xlinker", "-Bsymbolic",
-          "-Xlinker", "--no-undefined", "-lpthread", "-lrt", "-ldl"])
+          "-Xlinker", "--no-undefined", "-Xlinker", "--version-script=" + vscript,
+          "-lpthread", "-lrt", "-ldl"])
     return LIB
 
 
