@@ -358,7 +358,7 @@ yk_hidx_kernel(const __grid_constant__ yk_launch L)
  * the typed offset of relative position 0 in that block, so a unit's typed offset is one
  * shuffle and one add. */
 template <int V, int DIR>
-__global__ void __launch_bounds__(YK_THREADS)
+__global__ void __launch_bounds__(YK_THREADS, 6)
 yk_hidx32_kernel(const __grid_constant__ yk_launch L)
 {
     typedef typename yk_vec<V>::T VT;
