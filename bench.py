@@ -796,8 +796,8 @@ def main():
             torch_t[d].append(e0.elapsed_time(e1) * 1e-3)
     torch_ref = {d: statistics.median(v) * 1e6 for d, v in torch_t.items()}
 
-    clocks = Clocks(os.path.join(ROOT, "gpurun_out", "clocks.csv")
-                    if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "/tmp/yk_clocks.csv")
+    import tempfile
+    clocks = Clocks(os.path.join(tempfile.gettempdir(), f"yk_clocks_{os.getpid()}.csv"))
     clocks.start()
     time.sleep(0.3)
     launches0 = y.stats()["launches"]

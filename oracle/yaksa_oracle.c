@@ -1,7 +1,7 @@
 /*
  * yaksa_oracle.c -- CPU oracle for the pack/unpack path.  TEST INFRASTRUCTURE ONLY.
  *
- * This file is the checker, never the product: only tests/, the smoke check and the
+ * This file is the test oracle, never the product: only tests/, the smoke check and the
  * bench's CPU-baseline leg load the library built from it (liboracle_yaksa.so).  It
  * exports the same C ABI as libyaksa.so (include/yaksa.h) so that the reference's own
  * test programs (test/pack/pack.c with dtpools, the programs in test/simple) compile unchanged
