@@ -120,6 +120,13 @@ int yaksa_gb300_serve_trace(yaksa_gb300_pup_t * ops, const double *arrival_s, in
  * environment keeps the default shapes. */
 int yaksa_gb300_autotune_stats(uint32_t * classes, uint32_t * decided, uint64_t * probes);
 
+/* Sharding (no counterpart in the reference): the part of the packed range of `count`
+ * elements of `type` that rank `rank` of `nranks` moves, as (inoffset, max bytes) of
+ * yaksa_pack / yaksa_unpack.  Both ends sit on builtin boundaries and the parts tile the
+ * range, so N GPUs or processes each move their part with no exchange.  Host only. */
+int yaksa_gb300_shard(yaksa_type_t type, uintptr_t count, int rank, int nranks,
+                      uintptr_t * offset, uintptr_t * bytes);
+
 /* Test hook (no counterpart in the reference): the library's next `n` device or pinned
  * allocations fail as if memory were exhausted, without calling the allocator, so that
  * error paths are exercised with no GPU fault.  0 clears it. */

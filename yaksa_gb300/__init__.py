@@ -139,6 +139,9 @@ def load_library(path):
     if hasattr(lib, "yaksa_gb300_stats"):
         lib.yaksa_gb300_stats.restype = ctypes.c_int
         lib.yaksa_gb300_stats.argtypes = [ctypes.POINTER(_u64)] * 4
+        lib.yaksa_gb300_shard.restype = ctypes.c_int
+        lib.yaksa_gb300_shard.argtypes = [_u64, _up, ctypes.c_int, ctypes.c_int, ctypes.POINTER(_up),
+                                          ctypes.POINTER(_up)]
         lib.yaksa_gb300_debug_fail_alloc.restype = ctypes.c_int
         lib.yaksa_gb300_debug_fail_alloc.argtypes = [ctypes.c_int]
         lib.yaksa_gb300_autotune_stats.restype = ctypes.c_int
@@ -479,6 +482,13 @@ class Yaksa:
 
     def graph_free(self, g):
         self._chk("yaksa_gb300_graph_free", self.lib.yaksa_gb300_graph_free(g))
+
+    def shard(self, t, count, rank, nranks):
+        """yaksa_gb300_shard: (inoffset, bytes) of rank's part of the packed range."""
+        o, n = _up(), _up()
+        self._chk("yaksa_gb300_shard", self.lib.yaksa_gb300_shard(t, count, rank, nranks,
+                                                                   ctypes.byref(o), ctypes.byref(n)))
+        return o.value, n.value
 
     def autotune_stats(self):
         a, b, c = ctypes.c_uint32(), ctypes.c_uint32(), _u64()

@@ -915,3 +915,29 @@ uintptr_t yk_builtin_floor(yk_type * t, uintptr_t count, uintptr_t pos)
     uintptr_t e = pos / t->size;
     return e * t->size + floor_in(t, pos - e * t->size);
 }
+
+/* Sharding (no counterpart in the reference): rank `rank` of `nranks` takes packed bytes
+ * [offset, offset + bytes) of `count` elements of `type`, the n-th part of the packed
+ * range with both ends moved down to a builtin boundary.  The parts tile the range
+ * exactly, and each is a valid (inoffset, max_pack_bytes) of yaksa_pack / yaksa_unpack,
+ * so ranks or GPUs can each move their part with no exchange between them. */
+int yaksa_gb300_shard(yaksa_type_t type, uintptr_t count, int rank, int nranks,
+                      uintptr_t * offset, uintptr_t * bytes)
+{
+    *offset = *bytes = 0;
+    yk_type *t = yk_type_get(type);
+    if (!t || nranks <= 0 || rank < 0 || rank >= nranks)
+        return YAKSA_ERR__INTERNAL;
+    uintptr_t total = count * t->size;
+    if (!total)
+        return YAKSA_SUCCESS;
+    /* rank * total / nranks without overflow: total < 2^64 and nranks < 2^31 */
+    uintptr_t q = total / (uintptr_t) nranks, r = total % (uintptr_t) nranks;
+    uintptr_t a = q * (uintptr_t) rank + r * (uintptr_t) rank / (uintptr_t) nranks;
+    uintptr_t b = q * (uintptr_t) (rank + 1) + r * (uintptr_t) (rank + 1) / (uintptr_t) nranks;
+    a = yk_builtin_floor(t, count, a);
+    b = rank + 1 == nranks ? total : yk_builtin_floor(t, count, b);
+    *offset = a;
+    *bytes = b - a;
+    return YAKSA_SUCCESS;
+}
