@@ -138,6 +138,43 @@ def test_sorted_blocks_segmented(cuda, prod, oracle, bl, cut):
         oracle.type_free(to)
 
 
+@pytest.mark.parametrize("bl", [8, 256, 2048, 4096])
+def test_sorted_blocks_clustered(cuda, prod, oracle, bl):
+    """Sorted blocks of 64 B to 32 KiB where runs of up to 60 blocks share one offset, so
+    that one target element folds in contributions from up to 60 blocks, in block order,
+    and ranges that start and end inside blocks."""
+    rng = np.random.default_rng(300 + bl)
+    nblk = max(64, (1 << 21) // (bl * 8))
+    span = nblk * bl // 2
+    offs = np.sort(rng.integers(0, span, nblk)).astype(np.int64)
+    i = 0
+    while i < nblk:                     # clusters of equal offsets
+        k = int(rng.integers(1, 61))
+        offs[i:i + k] = offs[i]
+        i += k + int(rng.integers(0, 40))
+    for base, op in (("double", "sum"), ("int32", "bxor")):
+        h, es = BASE[base][0], BASE[base][1]
+        n = bl * 8 // es                # the same block bytes for either base
+        eoffs = offs * 8 // es          # kept alive while the constructors read it
+        tp = prod.type_create_indexed_block_array(nblk, n, eoffs.ctypes.data, h)
+        to = oracle.type_create_indexed_block_array(nblk, n, eoffs.ctypes.data, h)
+        total = nblk * bl * 8
+        packed = fill(rng, total, base)
+        target = fill(rng, (span + bl) * 8, base)
+        d_o = target.copy()
+        pk, dv = dev_copy(cuda, packed), dev_copy(cuda, target)
+        cuts = sorted(set(int(c) * 8 for c in rng.integers(1, total // 8, 4)))
+        bounds = [0] + cuts + [total]
+        for s0, s1 in zip(bounds[:-1], bounds[1:]):
+            ao = oracle.unpack(packed.ctypes.data + s0, s1 - s0, d_o.ctypes.data, 1, to, s0,
+                               op=yk.OP_NAMES[op])
+            ap = prod.unpack(pk.data_ptr() + s0, s1 - s0, dv.data_ptr(), 1, tp, s0, op=yk.OP_NAMES[op])
+            assert ao == ap
+        assert_same_bytes(host_of(cuda, dv), d_o, f"bl {bl} {base} {op}", base)
+        prod.type_free(tp)
+        oracle.type_free(to)
+
+
 def test_nonblocking_and_stream(cuda, prod, oracle):
     t = prod.type_create_hvector(1024, 4, 128, yk.TYPE_DOUBLE)
     src = cuda.randn(1024 * 16, dtype=cuda.float64, device="cuda")
