@@ -105,17 +105,18 @@ def test_sorted_overlapping_blocks_sum(cuda, prod, oracle):
         oracle.type_free(to)
 
 
-@pytest.mark.parametrize("cut", [1, 8])
+@pytest.mark.parametrize("cut", [1, 8, 16])
 @pytest.mark.parametrize("bl", [4, 8, 16])
 def test_sorted_blocks_segmented(cuda, prod, oracle, bl, cut):
     """Sorted overlapping fixed-length blocks unpacked in several calls whose ranges
     start and end inside blocks: each call keeps the block order within its range.
-    cut 8 puts every range boundary on 8 bytes (the 8-byte chunk kernel of small
-    elements); cut 1 anywhere on an element boundary."""
+    cut 8 and 16 put every range boundary on 8 or 16 bytes (the 8- and 16-byte chunk
+    kernels of small elements); cut 1 anywhere on an element boundary."""
     rng = np.random.default_rng(100 + bl + cut)
     nblk = 3000
     for base, op in (("int8", "sum"), ("int16", "max"), ("float", "sum"), ("double", "prod"),
-                     ("c_double_complex", "sum"), ("int32", "replace"), ("int64", "bxor")):
+                     ("c_double_complex", "sum"), ("int32", "replace"), ("int64", "bxor"),
+                     ("uint32", "bxor"), ("float", "min")):
         offs = np.sort(rng.integers(0, nblk * bl // 2, nblk)).astype(np.int64)
         h, es = BASE[base][0], BASE[base][1]
         tp = prod.type_create_indexed_block_array(nblk, bl, offs.ctypes.data, h)
@@ -125,7 +126,7 @@ def test_sorted_blocks_segmented(cuda, prod, oracle, bl, cut):
         target = fill(rng, (nblk * bl // 2 + bl) * es, base)
         d_o = target.copy()
         pk, dv = dev_copy(cuda, packed), dev_copy(cuda, target)
-        g = max(es, 8) if cut == 8 else es
+        g = max(es, cut)
         cuts = sorted(set(int(c) * g for c in rng.integers(1, total // g, 6)))
         bounds = [0] + cuts + [total]
         for s0, s1 in zip(bounds[:-1], bounds[1:]):

@@ -954,36 +954,37 @@ yk_owner_lane_kernel(const __grid_constant__ yk_launch L, int rshift)
     }
 }
 
-/* The same for elements of 1, 2 or 4 bytes, one 8-byte packed chunk per lane: the
- * chunk's elements share one block (blocks are a multiple of 8 bytes long and the range
- * starts on 8 bytes, checked on the host), so its displacement words and the packed
- * load serve 8/es elements. */
-template <int BT, int OP>
+/* The same for elements of 1, 2 or 4 bytes, one CW-byte packed chunk per lane (CW 8 or
+ * 16): the chunk's elements share one block (blocks are a multiple of CW bytes long and
+ * the range and the packed pointer sit on CW bytes, checked on the host), so its
+ * displacement words and the packed load serve CW/es elements. */
+template <int BT, int OP, int CW>
 __global__ void __launch_bounds__(YK_THREADS)
 yk_owner_chunk_kernel(const __grid_constant__ yk_launch L, int rshift)
 {
     typedef typename yk_elem<BT>::T T;
+    typedef typename yk_vec<CW>::T CT;
     constexpr uint32_t es = (uint32_t) sizeof(T);
-    constexpr int E = 8 / (int) es;
+    constexpr int E = CW / (int) es;
     const uint32_t R = 1u << rshift;
     const yk_level & lv = L.desc.lv[0];
     const uint32_t p0 = (uint32_t) L.p0, p1 = (uint32_t) (L.p0 + L.nbytes);
     const uint32_t nblk = (uint32_t) lv.count;
-    const uint32_t nchunks = (uint32_t) (L.nbytes / 8);
-    const uint64_t *packed8 = (const uint64_t *) L.packed;      /* chunk 0 is byte p0 */
+    const uint32_t nchunks = (uint32_t) (L.nbytes / CW);
+    const CT *packedc = (const CT *) L.packed;  /* chunk 0 is byte p0 */
     const T *packed = (const T *) L.packed;
     char *typed = L.typed + L.desc.base;
     for (uint32_t u = blockIdx.x * YK_THREADS + threadIdx.x; u < nchunks; u += gridDim.x * YK_THREADS) {
-        const uint32_t p = p0 + u * 8;
+        const uint32_t p = p0 + u * CW;
         const uint32_t b = p >> rshift;
         const int64_t d = __ldg(lv.disp + b);
         const int64_t dp = b > 0 ? __ldg(lv.disp + b - 1) : 0;
         const int64_t dn = b + 1 < nblk ? __ldg(lv.disp + b + 1) : INT64_MAX;
         union {
-            uint64_t w;
+            CT w;
             T e[E];
         } in;
-        in.w = __ldg(packed8 + u);
+        in.w = __ldg(packedc + u);
         const int64_t x0 = d + (int64_t) (p & (R - 1));
         bool own[E];
         T out[E];
@@ -1639,24 +1640,32 @@ extern "C" int yk_cuda_launch_pup_cfg(const yk_launch * l, void *stream, int uni
     return (int) cudaGetLastError();
 }
 
-/* the 8-byte chunk form exists for elements smaller than 8 bytes only */
+/* the chunk forms exist for elements smaller than 8 bytes only, 16-byte chunks for
+ * 4-byte elements only; chunk = bytes per lane (0: one element per lane) */
 template <int BT, int O>
 static bool yk_owner_chunk_launch(const yk_launch & c, int rshift, cudaStream_t s, unsigned g,
-                                  bool chunk)
+                                  int chunk)
 {
+    if constexpr (sizeof(typename yk_elem<BT>::T) == 4) {
+        if (chunk == 16) {
+            yk_owner_chunk_kernel<BT, O, 16><<<g, YK_THREADS, 0, s>>>(c, rshift);
+            return true;
+        }
+    }
     if constexpr (sizeof(typename yk_elem<BT>::T) < 8) {
-        if (chunk) {
-            yk_owner_chunk_kernel<BT, O><<<g, YK_THREADS, 0, s>>>(c, rshift);
+        if (chunk == 8) {
+            yk_owner_chunk_kernel<BT, O, 8><<<g, YK_THREADS, 0, s>>>(c, rshift);
             return true;
         }
     }
     return false;
 }
 
+
 /* yk_owner_lane_kernel for (base type, operator) pairs in the operator table; false
  * when the pair has no instance (the caller falls back to the runtime-op kernels) */
 template <int BT>
-static bool yk_owner_lane_int(const yk_launch & c, int rshift, cudaStream_t s, unsigned g, bool chunk)
+static bool yk_owner_lane_int(const yk_launch & c, int rshift, cudaStream_t s, unsigned g, int chunk)
 {
     switch ((int) c.op) {
 #define YK_OL(O) case O: if (!yk_owner_chunk_launch<BT, O>(c, rshift, s, g, chunk))           \
@@ -1669,7 +1678,7 @@ static bool yk_owner_lane_int(const yk_launch & c, int rshift, cudaStream_t s, u
 }
 
 template <int BT>
-static bool yk_owner_lane_flt(const yk_launch & c, int rshift, cudaStream_t s, unsigned g, bool chunk)
+static bool yk_owner_lane_flt(const yk_launch & c, int rshift, cudaStream_t s, unsigned g, int chunk)
 {
     switch ((int) c.op) {
         YK_OL(OP_MAX); YK_OL(OP_MIN); YK_OL(OP_SUM); YK_OL(OP_PROD); YK_OL(OP_REPLACE);
@@ -1678,7 +1687,7 @@ static bool yk_owner_lane_flt(const yk_launch & c, int rshift, cudaStream_t s, u
 }
 
 template <int BT>
-static bool yk_owner_lane_cplx(const yk_launch & c, int rshift, cudaStream_t s, unsigned g, bool chunk)
+static bool yk_owner_lane_cplx(const yk_launch & c, int rshift, cudaStream_t s, unsigned g, int chunk)
 {
     switch ((int) c.op) {
         YK_OL(OP_SUM); YK_OL(OP_PROD); YK_OL(OP_REPLACE);
@@ -1690,21 +1699,25 @@ static bool yk_owner_lane_cplx(const yk_launch & c, int rshift, cudaStream_t s, 
 static bool yk_owner_lane_launch(const yk_launch & c, int bt, int rshift, cudaStream_t s)
 {
     const uint64_t es = (uint64_t) yk_bt_size(bt);
-    /* 8-byte chunks for small elements: blocks a multiple of 8 bytes, range and packed
-     * pointer on 8 bytes */
-    const bool chunk = es < 8 && rshift >= 3 && c.p0 % 8 == 0 && c.nbytes % 8 == 0 &&
-        (uintptr_t) c.packed % 8 == 0;
-    const uint64_t units = c.nbytes / (chunk ? 8 : es);
+    /* chunks of CW bytes for small elements: blocks a multiple of CW bytes, range and
+     * packed pointer on CW bytes; 16-byte chunks for 4-byte elements (within the
+     * register budget of full occupancy), else 8-byte chunks */
+    int chunk = 0;
+    for (int cw = es == 4 ? 16 : 8; cw >= 8 && !chunk && es < 8; cw /= 2)
+        if (rshift >= (cw == 16 ? 4 : 3) && c.p0 % cw == 0 && c.nbytes % cw == 0 &&
+            (uintptr_t) c.packed % cw == 0)
+            chunk = cw;
+    const uint64_t units = c.nbytes / (chunk ? (uint64_t) chunk : es);
     const unsigned g = yk_grid(units, YK_THREADS, 16);
     switch (bt) {
         case YK_BT_I8: return yk_owner_lane_int<YK_BT_I8>(c, rshift, s, g, chunk);
         case YK_BT_I16: return yk_owner_lane_int<YK_BT_I16>(c, rshift, s, g, chunk);
         case YK_BT_I32: return yk_owner_lane_int<YK_BT_I32>(c, rshift, s, g, chunk);
-        case YK_BT_I64: return yk_owner_lane_int<YK_BT_I64>(c, rshift, s, g, false);
+        case YK_BT_I64: return yk_owner_lane_int<YK_BT_I64>(c, rshift, s, g, 0);
         case YK_BT_F32: return yk_owner_lane_flt<YK_BT_F32>(c, rshift, s, g, chunk);
-        case YK_BT_F64: return yk_owner_lane_flt<YK_BT_F64>(c, rshift, s, g, false);
-        case YK_BT_C32: return yk_owner_lane_cplx<YK_BT_C32>(c, rshift, s, g, false);
-        case YK_BT_C64: return yk_owner_lane_cplx<YK_BT_C64>(c, rshift, s, g, false);
+        case YK_BT_F64: return yk_owner_lane_flt<YK_BT_F64>(c, rshift, s, g, 0);
+        case YK_BT_C32: return yk_owner_lane_cplx<YK_BT_C32>(c, rshift, s, g, 0);
+        case YK_BT_C64: return yk_owner_lane_cplx<YK_BT_C64>(c, rshift, s, g, 0);
     }
     return false;
 }
