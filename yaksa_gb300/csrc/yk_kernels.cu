@@ -1640,13 +1640,14 @@ extern "C" int yk_cuda_launch_pup_cfg(const yk_launch * l, void *stream, int uni
     return (int) cudaGetLastError();
 }
 
-/* the chunk forms exist for elements smaller than 8 bytes only, 16-byte chunks for
- * 4-byte elements only; chunk = bytes per lane (0: one element per lane) */
+/* the 8-byte chunk form exists for elements under 8 bytes, the 16-byte form for 4- and
+ * 8-byte elements other than double; chunk = bytes per lane (0: the per-lane kernel) */
 template <int BT, int O>
 static bool yk_owner_chunk_launch(const yk_launch & c, int rshift, cudaStream_t s, unsigned g,
                                   int chunk)
 {
-    if constexpr (sizeof(typename yk_elem<BT>::T) == 4) {
+    if constexpr (sizeof(typename yk_elem<BT>::T) == 4 ||
+                  (sizeof(typename yk_elem<BT>::T) == 8 && BT != YK_BT_F64)) {
         if (chunk == 16) {
             yk_owner_chunk_kernel<BT, O, 16><<<g, YK_THREADS, 0, s>>>(c, rshift);
             return true;
@@ -1699,24 +1700,30 @@ static bool yk_owner_lane_cplx(const yk_launch & c, int rshift, cudaStream_t s, 
 static bool yk_owner_lane_launch(const yk_launch & c, int bt, int rshift, cudaStream_t s)
 {
     const uint64_t es = (uint64_t) yk_bt_size(bt);
-    /* chunks of CW bytes for small elements: blocks a multiple of CW bytes, range and
-     * packed pointer on CW bytes; 16-byte chunks for 4-byte elements (within the
-     * register budget of full occupancy), else 8-byte chunks */
+    /* chunks of CW bytes: blocks a multiple of CW bytes, range and packed pointer on CW
+     * bytes.  16-byte chunks for 4- and 8-byte elements (within the register budget of
+     * full occupancy), else 8-byte chunks for elements under 8 bytes.  double keeps one
+     * element per lane: its arithmetic runs on the FP64 pipe, a small share of the SM's
+     * issue rate on GB300, and measured slower with its two operations per lane
+     * back to back (double SUM, 2^25 elements: 213 us per lane, 234 us chunked) */
     int chunk = 0;
-    for (int cw = es == 4 ? 16 : 8; cw >= 8 && !chunk && es < 8; cw /= 2)
-        if (rshift >= (cw == 16 ? 4 : 3) && c.p0 % cw == 0 && c.nbytes % cw == 0 &&
-            (uintptr_t) c.packed % cw == 0)
-            chunk = cw;
+    if (es <= 8 && bt != YK_BT_F64) {
+        const int first = es >= 4 ? 16 : 8, last = es < 8 ? 8 : 16;
+        for (int cw = first; cw >= last && !chunk; cw /= 2)
+            if (rshift >= (cw == 16 ? 4 : 3) && c.p0 % cw == 0 && c.nbytes % cw == 0 &&
+                (uintptr_t) c.packed % cw == 0)
+                chunk = cw;
+    }
     const uint64_t units = c.nbytes / (chunk ? (uint64_t) chunk : es);
     const unsigned g = yk_grid(units, YK_THREADS, 16);
     switch (bt) {
         case YK_BT_I8: return yk_owner_lane_int<YK_BT_I8>(c, rshift, s, g, chunk);
         case YK_BT_I16: return yk_owner_lane_int<YK_BT_I16>(c, rshift, s, g, chunk);
         case YK_BT_I32: return yk_owner_lane_int<YK_BT_I32>(c, rshift, s, g, chunk);
-        case YK_BT_I64: return yk_owner_lane_int<YK_BT_I64>(c, rshift, s, g, 0);
+        case YK_BT_I64: return yk_owner_lane_int<YK_BT_I64>(c, rshift, s, g, chunk);
         case YK_BT_F32: return yk_owner_lane_flt<YK_BT_F32>(c, rshift, s, g, chunk);
-        case YK_BT_F64: return yk_owner_lane_flt<YK_BT_F64>(c, rshift, s, g, 0);
-        case YK_BT_C32: return yk_owner_lane_cplx<YK_BT_C32>(c, rshift, s, g, 0);
+        case YK_BT_F64: return yk_owner_lane_flt<YK_BT_F64>(c, rshift, s, g, chunk);
+        case YK_BT_C32: return yk_owner_lane_cplx<YK_BT_C32>(c, rshift, s, g, chunk);
         case YK_BT_C64: return yk_owner_lane_cplx<YK_BT_C64>(c, rshift, s, g, 0);
     }
     return false;
