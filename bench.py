@@ -941,7 +941,7 @@ def main():
         # mixed request stream; the grids of the halo step are released first
         y.graph_free(graph)
         torch.cuda.synchronize()
-        del src, dst, packed, flush, hsrc, hdst, hpk
+        del src, dst, packed, flush, hsrc, hdst, send, recv
         torch.cuda.empty_cache()
         r = run_stream(nreq=args.stream_requests, check=True)
         line["stream"] = {
