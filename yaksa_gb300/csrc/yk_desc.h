@@ -139,6 +139,11 @@ typedef struct {
     uint64_t pb, pe;            /* packed byte range of this item */
 } yk_item;
 
+/* Claim lanes of the request server: item t belongs to lane t mod YK_SRV_LANES, and each
+ * lane has its own claim counter, so resident CTAs contend on 16 addresses, not one. */
+#define YK_SRV_LANES 16
+#define YK_SRV_LANE_STRIDE 16
+
 typedef struct {
     yk_launch *reqs;            /* request records (host-mapped, written by the host) */
     yk_item *items;             /* work items (host-mapped, written by the host) */
@@ -146,7 +151,10 @@ typedef struct {
                                          * reset by the host, counted by the GPU) */
     const volatile uint64_t *items_published;   /* items visible to the GPU (host) */
     const volatile int *stop;   /* host asks resident CTAs to leave */
-    unsigned long long *next_item;      /* device memory: next item to claim */
+    unsigned long long *next_item;      /* device memory: YK_SRV_LANES claim counters, one
+                                         * per 128-byte line (YK_SRV_LANE_STRIDE words
+                                         * apart); lane k's counter c means its next item
+                                         * is c * YK_SRV_LANES + k */
     volatile uint32_t *status;  /* [0] idle exits, [1] stop exits, [2] rejected items */
     uint32_t qi, qr;            /* ring sizes */
     uint32_t max_idle_spins;    /* bounded wait for new items */

@@ -1295,10 +1295,11 @@ __device__ __forceinline__ bool yk_item_ok(const yk_item & it, const yk_launch &
     return L.dir == 0 || L.dir == 1;
 }
 
-/* Resident CTAs claim work items one at a time (a compare-and-swap that never runs past
- * the published count), stage the item's request record in shared memory, process the
- * item, and publish its completion.  Every wait is bounded: a CTA that finds no new
- * item for max_idle_spins polls, or sees the stop flag, leaves; the host relaunches the
+/* Resident CTAs claim work items one at a time (a compare-and-swap on a lane's counter
+ * that never runs past the published count), stage the item's request record in shared
+ * memory, process the item, and publish its completion.  A CTA tries its home lane
+ * first, then the others in turn.  Every wait is bounded: a CTA that finds no new item
+ * for max_idle_spins polls, or sees the stop flag, leaves; the host relaunches the
  * kernel when items are pending and no CTA is resident. */
 __global__ void __launch_bounds__(YK_THREADS, 6)
 yk_server_kernel(const __grid_constant__ yk_server_args A)
@@ -1321,16 +1322,28 @@ yk_server_kernel(const __grid_constant__ yk_server_args A)
                     break;
                 }
                 /* the published count only grows: re-read it from host memory only when
-                 * the claim counter has caught up with the copy held here */
-                unsigned long long nxt = *(volatile unsigned long long *) A.next_item;
-                if (nxt >= pub)
-                    pub = yk_ld_acquire_sys(A.items_published);
-                if (nxt < pub) {
-                    if (atomicCAS(A.next_item, nxt, nxt + 1) == nxt) {
-                        s_item = nxt;
-                        cmd = 1;
-                        break;
+                 * every lane has caught up with the copy held here */
+                bool pending = false;
+                for (int pass = 0; pass < 2 && !pending; pass++) {
+                    if (pass == 1)
+                        pub = yk_ld_acquire_sys(A.items_published);
+                    for (uint32_t i = 0; i < YK_SRV_LANES && cmd == 0; i++) {
+                        const uint32_t lane = (blockIdx.x + i) % YK_SRV_LANES;
+                        unsigned long long *ctr = A.next_item + lane * YK_SRV_LANE_STRIDE;
+                        const unsigned long long c = *(volatile unsigned long long *) ctr;
+                        const unsigned long long t = c * YK_SRV_LANES + lane;
+                        if (t >= pub)
+                            continue;
+                        pending = true;
+                        if (atomicCAS(ctr, c, c + 1) == c) {
+                            s_item = t;
+                            cmd = 1;
+                        }
                     }
+                }
+                if (cmd == 1)
+                    break;
+                if (pending) {
                     if (spins >= 64u * A.max_idle_spins) {
                         cmd = 3;        /* hard bound: leave; the host relaunches */
                         break;

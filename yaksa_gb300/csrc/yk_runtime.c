@@ -1014,7 +1014,10 @@ int yaksa_gb300_pup_noalloc(yaksa_gb300_pup_t * o, void *stream)
 /* persistent request server                                                 */
 /* ------------------------------------------------------------------------- */
 
-#define YK_ITEM_BYTES (512u << 10)
+/* packed bytes per work item; YAKSA_GB300_SERVER_ITEM_KIB in the environment overrides
+ * it (a power of two from 16 KiB to 16 MiB).  On the mixed request stream 256 KiB gave
+ * the lowest p99 at 97% of the 512 KiB capacity; 128 KiB raised small-request p99. */
+#define YK_ITEM_BYTES (256u << 10)
 
 typedef struct {
     uint64_t seq;               /* request sequence number (ticket) */
@@ -1033,11 +1036,12 @@ struct yaksa_gb300_server_s {
     yk_item *items;             /* pinned, mapped */
     unsigned long long *req_done;       /* pinned, mapped: items finished per request slot */
     uint64_t *ctl;              /* pinned, mapped: [0] items published, [1] stop, [2] status */
-    unsigned long long *next_item;      /* device */
+    unsigned long long *next_item;      /* device: the lanes' claim counters */
     yk_srv_slot *slots;
     uint64_t req_seq, item_seq, oldest_req;
     uint64_t inflight_bytes, budget;
     uint64_t relaunches;
+    uint64_t item_bytes;
     yk_server_args args;
 };
 
@@ -1065,6 +1069,13 @@ int yaksa_gb300_server_create(uint32_t ring_requests, uint64_t budget_bytes,
     S->qr = ring_requests ? ring_requests : 4096;
     S->qi = 16 * S->qr;
     S->budget = budget_bytes ? budget_bytes : (64ull << 30);
+    S->item_bytes = YK_ITEM_BYTES;
+    const char *ik = getenv("YAKSA_GB300_SERVER_ITEM_KIB");
+    if (ik) {
+        unsigned long v = strtoul(ik, NULL, 10);
+        if (v >= 16 && v <= 16384 && !(v & (v - 1)))
+            S->item_bytes = (uint64_t) v << 10;
+    }
     S->reqs = pinned(sizeof(yk_launch) * S->qr);
     S->items = pinned(sizeof(yk_item) * S->qi);
     S->req_done = pinned(sizeof(unsigned long long) * S->qr);
@@ -1072,8 +1083,10 @@ int yaksa_gb300_server_create(uint32_t ring_requests, uint64_t budget_bytes,
     S->slots = calloc(S->qr, sizeof(yk_srv_slot));
     if (!S->reqs || !S->items || !S->req_done || !S->ctl || !S->slots ||
         yk_fail_injected() ||
-        cudaMalloc((void **) &S->next_item, sizeof(unsigned long long)) != cudaSuccess ||
-        cudaMemset(S->next_item, 0, sizeof(unsigned long long)) != cudaSuccess ||
+        cudaMalloc((void **) &S->next_item, sizeof(unsigned long long) * YK_SRV_LANES *
+                   YK_SRV_LANE_STRIDE) != cudaSuccess ||
+        cudaMemset(S->next_item, 0, sizeof(unsigned long long) * YK_SRV_LANES *
+                   YK_SRV_LANE_STRIDE) != cudaSuccess ||
         cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking) != cudaSuccess) {
         yaksa_gb300_server_destroy(S);
         return YAKSA_ERR__OUT_OF_MEM;
@@ -1193,7 +1206,7 @@ int yaksa_gb300_server_submit(yaksa_gb300_server_t S, yaksa_gb300_pup_t * o, yak
         gran = sorted ? (uint64_t) yk_base_type_size(L.desc.leaf_type) : (uint64_t) L.vec;
     }
     uint64_t n = p.b1 - p.b0;
-    uint64_t chunk = skind == YK_SRV_ORDERED ? (n ? n : 1) : (YK_ITEM_BYTES / gran) * gran;
+    uint64_t chunk = skind == YK_SRV_ORDERED ? (n ? n : 1) : (S->item_bytes / gran) * gran;
     uint64_t nitems = n ? (n + chunk - 1) / chunk : 0;
     if (nitems > S->qi)
         return YAKSA_ERR__NOT_SUPPORTED;        /* larger than the whole item ring */
