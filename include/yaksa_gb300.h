@@ -60,8 +60,9 @@ int yaksa_gb300_graph_free(yaksa_gb300_graph_t graph);
  * one kernel per request chunk, src/backend/src/yaksuri_progress.c:2862-3088).  A
  * persistent kernel keeps six CTAs resident per SM and drains a work queue in
  * pinned, device-mapped host memory; requests are split into work items of up to
- * 256 KiB of packed bytes (YAKSA_GB300_SERVER_ITEM_KIB overrides it), so requests of
- * any size and type share the GPU as they arrive (continuous batching).
+ * 256 KiB of packed bytes (YAKSA_GB300_SERVER_ITEM_KIB overrides it), and into at least
+ * 128 items down to 32 KiB each (YAKSA_GB300_SERVER_MIN_ITEMS), so requests of any size
+ * and type share the GPU as they arrive (continuous batching).
  *   create: ring_requests request slots (0: 4096), budget_bytes of packed bytes in
  *           flight (0: 64 GiB);
  *   submit: admits one request or returns YAKSA_ERR__OUT_OF_MEM when the rings or the

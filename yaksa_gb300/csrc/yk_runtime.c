@@ -1042,6 +1042,7 @@ struct yaksa_gb300_server_s {
     uint64_t inflight_bytes, budget;
     uint64_t relaunches;
     uint64_t item_bytes;
+    uint32_t min_items;         /* split requests into at least this many items (>= 32 KiB) */
     yk_server_args args;
 };
 
@@ -1076,6 +1077,15 @@ int yaksa_gb300_server_create(uint32_t ring_requests, uint64_t budget_bytes,
         if (v >= 16 && v <= 16384 && !(v & (v - 1)))
             S->item_bytes = (uint64_t) v << 10;
     }
+    /* a request is split into at least min_items items (down to 32 KiB each), so that a
+     * mid-size request is walked by that many CTAs at once; YAKSA_GB300_SERVER_MIN_ITEMS
+     * overrides it (0: items of item_bytes only).  On the mixed request stream 128 cut
+     * the p50 of 64 KiB..4 MiB requests from 183 to 53 us and of larger ones from 272 to
+     * 189 us, at 98% of the capacity; 256 cost 7% of the capacity. */
+    const char *mi = getenv("YAKSA_GB300_SERVER_MIN_ITEMS");
+    S->min_items = mi ? (uint32_t) strtoul(mi, NULL, 10) : 128;
+    if (S->min_items > 1024)
+        S->min_items = 1024;
     S->reqs = pinned(sizeof(yk_launch) * S->qr);
     S->items = pinned(sizeof(yk_item) * S->qi);
     S->req_done = pinned(sizeof(unsigned long long) * S->qr);
@@ -1206,7 +1216,10 @@ int yaksa_gb300_server_submit(yaksa_gb300_server_t S, yaksa_gb300_pup_t * o, yak
         gran = sorted ? (uint64_t) yk_base_type_size(L.desc.leaf_type) : (uint64_t) L.vec;
     }
     uint64_t n = p.b1 - p.b0;
-    uint64_t chunk = skind == YK_SRV_ORDERED ? (n ? n : 1) : (S->item_bytes / gran) * gran;
+    uint64_t ib = S->item_bytes;
+    while (S->min_items && ib > (32u << 10) && n < (uint64_t) S->min_items * ib)
+        ib >>= 1;       /* mid-size requests: more, smaller items, so more CTAs share them */
+    uint64_t chunk = skind == YK_SRV_ORDERED ? (n ? n : 1) : YK_MAX(ib / gran, 1) * gran;
     uint64_t nitems = n ? (n + chunk - 1) / chunk : 0;
     if (nitems > S->qi)
         return YAKSA_ERR__NOT_SUPPORTED;        /* larger than the whole item ring */
