@@ -159,3 +159,71 @@ def test_server_admission_budget(cuda, prod, oracle):
     srv2.destroy()
     srv.destroy()
     prod.type_free(t)
+
+
+def test_server_large_requests_split(cuda, prod, oracle):
+    """Requests of 2-4 MiB from four families (hvector, lognormal hindexed, struct,
+    sorted overlapping blocks unpacked with MAX) submitted together: each is split into
+    many work items claimed across the lanes, and every byte matches the oracle."""
+    rng = np.random.default_rng(21)
+    nb = 20000
+    blens = np.clip(np.round(np.exp(np.log(16) + rng.standard_normal(nb))), 1, 4096).astype(np.int64)
+    gaps = rng.integers(0, 64, nb)
+    order = rng.permutation(nb)
+    starts = np.cumsum(blens[order] + gaps) - blens[order]
+    displs = np.empty(nb, dtype=np.int64)
+    displs[order] = starts * 4
+    offs = np.sort(rng.integers(0, (1 << 16) * 8, 1 << 16)).astype(np.int64)
+    specs = [
+        ("double", 1, lambda y: y.type_create_hvector(1 << 17, 4, 128, yk.TYPE_DOUBLE), 0, yk.OP_REPLACE),
+        ("int32", 1, lambda y: y.type_create_hindexed_arrays(nb, blens.ctypes.data, displs.ctypes.data,
+                                                             yk.TYPE_INT32_T), 1, yk.OP_REPLACE),
+        ("float", 200000, lambda y: y.type_create_resized(
+            y.type_create_struct([1, 3], [0, 8], [yk.TYPE_INT64_T, yk.TYPE_FLOAT]), 0, 32), 0, yk.OP_REPLACE),
+        ("int64", 1, lambda y: y.type_create_indexed_block_array(1 << 16, 8, offs.ctypes.data,
+                                                                 yk.TYPE_INT64_T), 1, yk.OP_MAX),
+    ]
+    srv = yk.Server(prod)
+    reqs, ops = [], []
+    for base, count, mk, kind, op in specs:
+        tp, to = mk(prod), mk(oracle)
+        lo, hi, size = footprint(oracle, to, count)
+        r = dict(tp=tp, to=to, lo=lo, count=count, n=size * count, kind=kind, op=op, base=base,
+                 typed=fill(rng, hi - lo + 64, base), packed=fill(rng, size * count + 64, base))
+        r["t_g"], r["p_g"] = dev_copy(cuda, r["typed"]), dev_copy(cuda, r["packed"])
+        tpp = r["t_g"].data_ptr() + 32 - lo
+        ops.append(yk.pack_op(tpp, count, tp, 0, r["p_g"].data_ptr(), r["n"], op=op) if kind == 0 else
+                   yk.unpack_op(r["p_g"].data_ptr(), r["n"], tpp, count, tp, 0, op=op))
+        reqs.append(r)
+    assert min(r["n"] for r in reqs) >= 2 << 20
+    for t in submit_all(srv, ops):
+        srv.wait(t)
+    cuda.cuda.synchronize()
+    for r, o in zip(reqs, ops):
+        th, ph = r["typed"].copy(), r["packed"].copy()
+        tpo = th.ctypes.data + 32 - r["lo"]
+        if r["kind"] == 0:
+            a = oracle.pack(tpo, r["count"], r["to"], 0, ph.ctypes.data, r["n"], op=r["op"])
+        else:
+            a = oracle.unpack(ph.ctypes.data, r["n"], tpo, r["count"], r["to"], 0, op=r["op"])
+        assert o.actual == a == r["n"]
+        assert_same_bytes(host_of(cuda, r["p_g"]), ph, "server packed", r["base"])
+        assert_same_bytes(host_of(cuda, r["t_g"]), th, "server typed", r["base"])
+        prod.type_free(r["tp"])
+        oracle.type_free(r["to"])
+    srv.destroy()
+
+
+@pytest.mark.parametrize("env", [{"YAKSA_GB300_SERVER_ITEM_KIB": "16", "YAKSA_GB300_SERVER_MIN_ITEMS": "0"},
+                                 {"YAKSA_GB300_SERVER_MIN_ITEMS": "1024"}])
+def test_server_item_sizes(cuda, env):
+    """The server tests again, in a child process, with 16 KiB items or at least 1024
+    items per request: many items per request spread over every claim lane."""
+    import os
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    r = subprocess.run([sys.executable, "-m", "pytest", "-x", "-q", "-p", "no:cacheprovider",
+                        os.path.join(here, "test_gpu_server.py"), "-k", "not item_sizes"],
+                       env=dict(os.environ, **env), capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
