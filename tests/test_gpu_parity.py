@@ -12,7 +12,7 @@ import pytest
 
 import yaksa_gb300 as yk
 from helpers import Pair, assert_same_bytes, dev_copy, fill, host_of, roundtrip
-from typegen import BASE, VALID_OPS, Gen
+from typegen import BASE, VALID_OPS, Gen, footprint
 
 pytestmark = pytest.mark.gpu
 
@@ -174,6 +174,53 @@ def test_sorted_blocks_clustered(cuda, prod, oracle, bl):
         assert_same_bytes(host_of(cuda, dv), d_o, f"bl {bl} {base} {op}", base)
         prod.type_free(tp)
         oracle.type_free(to)
+
+
+DENSE_STRUCTS = [
+    # (blocklengths, displacements, types, resized extent or None)
+    ([1, 3], [0, 8], [yk.TYPE_INT64_T, yk.TYPE_FLOAT], 32),        # 20 B run in 32 B
+    ([1, 1], [0, 12], [yk.TYPE_INT64_T, yk.TYPE_FLOAT], 24),       # two segments with a gap
+    ([3, 1, 2], [0, 6, 12], [yk.TYPE_INT16_T, yk.TYPE_INT8_T, yk.TYPE_INT16_T], 16),
+    ([5], [4], [yk.TYPE_INT32_T], 28),                             # run starting at 4
+    ([1, 2], [0, 8], [yk.TYPE_DOUBLE, yk.TYPE_FLOAT], None),       # natural extent 16
+    ([7], [0], [yk.TYPE_INT8_T], 12),                              # 1-byte units
+    ([60, 1], [0, 248], [yk.TYPE_INT32_T, yk.TYPE_INT32_T], 256),  # 244 B over 256 B
+]
+
+
+@pytest.mark.parametrize("k", range(len(DENSE_STRUCTS)))
+def test_dense_struct_pack(cuda, prod, oracle, k):
+    """Packs of many elements of dense structs (runs of 7 to 244 bytes in extents of 12
+    to 256, one or several segments, 1- to 4-byte units): whole and partial ranges on
+    builtin boundaries, packed pointers on and off 16 bytes."""
+    bl, dp, ty, ext = DENSE_STRUCTS[k]
+    rng = np.random.default_rng(500 + k)
+
+    def mk(y):
+        t = y.type_create_struct(bl, dp, ty)
+        if ext is None:
+            return t
+        r = y.type_create_resized(t, 0, ext)
+        y.type_free(t)
+        return r
+    tp, to = mk(prod), mk(oracle)
+    size = prod.size(tp)
+    for count in (2, 7, 411, 5000):
+        lo, hi, _ = footprint(oracle, to, count)
+        total = size * count
+        typed = fill(rng, hi - lo + 64, "int8")
+        tg = dev_copy(cuda, typed)
+        cases = [(0, total), (size, total - 2 * size), (0, total // 3)]
+        for shift in (0, 4):
+            for off, n in cases:
+                exp = np.zeros(total + 64, dtype=np.uint8)
+                a = oracle.pack(typed.ctypes.data + 32 - lo, count, to, off, exp.ctypes.data, n)
+                pk = cuda.zeros(total + 64, dtype=cuda.uint8, device="cuda")
+                got = prod.pack(tg.data_ptr() + 32 - lo, count, tp, off, pk.data_ptr() + shift, n)
+                assert got == a
+                assert np.array_equal(host_of(cuda, pk)[shift:shift + a], exp[:a]), (count, off, n, shift)
+    prod.type_free(tp)
+    oracle.type_free(to)
 
 
 def test_nonblocking_and_stream(cuda, prod, oracle):
