@@ -38,7 +38,7 @@ typedef struct {
     void *scratch[2];           /* staged buffers released at completion */
 } yk_req;
 
-#define YK_LIB_STREAMS 4
+#define YK_LIB_STREAMS 16     /* at most; YAKSA_GB300_LIB_STREAMS sets how many (4) */
 
 static struct {
     pthread_mutex_t mu;
@@ -51,6 +51,7 @@ static struct {
      * these, so independent requests (whose order the API leaves open) overlap on the
      * GPU; streams[0] is also the default stream of graph replays */
     cudaStream_t streams[YK_LIB_STREAMS];
+    int nstreams;
     unsigned next_stream;
     yk_req *reqs;
     size_t nreqs;
@@ -66,7 +67,7 @@ static struct {
 static cudaStream_t lib_stream(void)
 {
     unsigned k = __atomic_fetch_add(&R.next_stream, 1, __ATOMIC_RELAXED);
-    return R.streams[k % YK_LIB_STREAMS];
+    return R.streams[k % (unsigned) R.nstreams];
 }
 
 
@@ -111,7 +112,11 @@ static int runtime_ready(void)
             const char *l2 = getenv("YAKSA_GB300_L2_FETCH_BYTES");
             if (l2 && atoi(l2) > 0)
                 cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t) atoi(l2));
-            for (int k = 0; k < YK_LIB_STREAMS && e == cudaSuccess; k++)
+            const char *ns = getenv("YAKSA_GB300_LIB_STREAMS");
+            R.nstreams = ns ? atoi(ns) : 4;
+            if (R.nstreams < 1 || R.nstreams > YK_LIB_STREAMS)
+                R.nstreams = 4;
+            for (int k = 0; k < R.nstreams && e == cudaSuccess; k++)
                 e = cudaStreamCreateWithFlags(&R.streams[k], cudaStreamNonBlocking);
             if (e != cudaSuccess) {
                 cuda_err(e, "cudaStreamCreate");
@@ -132,7 +137,7 @@ void yk_runtime_finalize(void)
     yk_tune_reset();
     pthread_mutex_lock(&R.mu);
     if (R.ready) {
-        for (int k = 0; k < YK_LIB_STREAMS; k++)
+        for (int k = 0; k < R.nstreams; k++)
             cudaStreamSynchronize(R.streams[k]);
         for (size_t i = 0; i < R.nreqs; i++)
             if (R.reqs[i].in_use) {
@@ -142,7 +147,7 @@ void yk_runtime_finalize(void)
         for (size_t i = 0; i < R.nev; i++)
             cudaEventDestroy(R.evpool[i]);
         R.nev = 0;
-        for (int k = 0; k < YK_LIB_STREAMS; k++)
+        for (int k = 0; k < R.nstreams; k++)
             cudaStreamDestroy(R.streams[k]);
         R.ready = 0;
     }
