@@ -86,3 +86,19 @@ def test_concurrent_threads_match_oracle(cuda, prod, oracle):
         th.join(timeout=300)
     assert not any(th.is_alive() for th in threads)
     assert not errors, errors[:4]
+
+
+@pytest.mark.parametrize("nstreams", ["1", "16"])
+def test_library_stream_counts(cuda, nstreams):
+    """The threaded test and the nonblocking parity tests again, in a child process, with
+    one library stream (every request in one order) and with sixteen."""
+    import os
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    r = subprocess.run([sys.executable, "-m", "pytest", "-x", "-q", "-p", "no:cacheprovider",
+                        os.path.join(here, "test_gpu_threads.py"), os.path.join(here, "test_gpu_parity.py"),
+                        "-k", "concurrent_threads or nonblocking or host_buffers"],
+                       env=dict(os.environ, YAKSA_GB300_LIB_STREAMS=nstreams),
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
