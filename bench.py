@@ -180,9 +180,12 @@ def run_reference(args):
     threads = os.cpu_count() or 1
     seconds = max(2.0, min(30.0, 1.0 * args.steps))
     b = cpu_baseline(oracle_path, seconds, threads)
+    step_bytes = 2 * (2 * N * N * 4) * 6      # six 2 MiB faces, packed and unpacked
     line = {"impl": "reference", "metric": METRIC, "value": b["value"], "unit": "GB/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "higher_is_better": True, "dtype": "f32", "data": "synthetic",
+            "ms_per_step": step_bytes / (b["value"] * 1e9) * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "bit_exact": bool(b["ok"]),
             "config": {"workload": WORKLOAD, "parallelism": "host threads", "l2": "host caches"},
             "cpu_baseline": {"value": b["value"], "unit": "GB/s", "cores": threads, "kind": "port",
                              "sample": b["sample"], "faces_equal": bool(b["ok"])},
