@@ -12,7 +12,9 @@ job), next to the HBM roofline of the pack/unpack kernel whose algorithmic traff
 2 bytes per packed byte per direction (read strided + write contiguous, or the mirror).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload halo3d|hvector|hindexed|struct|reduce]
+                    [--no-cpu] [--no-stream] [--cpu-seconds S]
+    python bench.py --suite out.jsonl [--suite-only hindexed,struct,...] [--suite-scale K]
+    python bench.py --stream out.json [--stream-requests R]
 """
 import argparse
 import ctypes
