@@ -59,8 +59,9 @@ template <> struct yk_vec<4> { typedef uint32_t T; };
 template <> struct yk_vec<8> { typedef uint2 T; };
 template <> struct yk_vec<16> { typedef uint4 T; };
 
-/* Loads cached in L2 only and with no L2 prefetch-size qualifier, so an isolated
- * 8-byte run costs one 32-byte sector request instead of a 128-byte line. */
+/* Loads cached in L2 only: the strided side is read once, so it does not displace L1.
+ * (An isolated 8-byte run still costs a whole 128-byte line from L2 on GB300, whatever
+ * the cache operator or prefetch-size qualifier; measured for every documented form.) */
 __device__ __forceinline__ uint8_t yk_ldcg(const uint8_t * p)
 {
     uint16_t v;
