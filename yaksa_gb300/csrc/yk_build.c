@@ -296,22 +296,34 @@ static void chain(hbuild * b, const yk_type * t)
                 break;
             }
         case YK_K_HINDEXED:{
-                hlev *l = push_level(b, YK_LV_HIDX, t->count, t->child->extent, t->child->size);
+                /* empty blocks hold no bytes: left out, so every block of the level is
+                 * at least one child long and block starts strictly increase */
+                intptr_t nb = 0;
+                for (intptr_t j = 0; j < t->count; j++)
+                    nb += t->blens[j] != 0;
+                const int keep_all = nb == 0;
+                if (keep_all)
+                    nb = t->count;
+                hlev *l = push_level(b, YK_LV_HIDX, (uint64_t) nb, t->child->extent, t->child->size);
                 if (!l)
                     return;
-                l->disp = malloc(t->count * sizeof(int64_t));
-                l->pfx = malloc((t->count + 1) * sizeof(uint64_t));
+                l->disp = malloc((size_t) nb * sizeof(int64_t));
+                l->pfx = malloc(((size_t) nb + 1) * sizeof(uint64_t));
                 if (!l->disp || !l->pfx) {
                     b->err = YAKSA_ERR__OUT_OF_MEM;
                     return;
                 }
                 uint64_t acc = 0;
+                intptr_t k = 0;
                 for (intptr_t j = 0; j < t->count; j++) {
-                    l->disp[j] = t->displs[j];
-                    l->pfx[j] = acc;
+                    if (!t->blens[j] && !keep_all)
+                        continue;
+                    l->disp[k] = t->displs[j];
+                    l->pfx[k] = acc;
                     acc += (uint64_t) t->blens[j] * t->child->size;
+                    k++;
                 }
-                l->pfx[t->count] = acc;
+                l->pfx[nb] = acc;
                 chain(b, t->child);
                 break;
             }
