@@ -87,3 +87,49 @@ def test_zero_length_blocks_and_negative_layouts(cuda, prod, oracle, direction):
                 run_pair(cuda, prod, oracle, tp, to, count, base, off, n, direction, hi - lo, lo)
         prod.type_free(tp)
         oracle.type_free(to)
+
+
+@pytest.mark.parametrize("nranks", [2, 3, 8])
+def test_shard_parts_on_gpu(cuda, prod, oracle, nranks):
+    """The parts yaksa_gb300_shard gives, each packed by the product on its own, make up
+    the oracle's one-call pack; unpacked part by part they give its one-call unpack."""
+    from helpers import Pair
+    from typegen import Gen
+    g = Gen(oracle, 15000 + nranks, max_depth=3)
+    rng = np.random.default_rng(nranks)
+    for i in range(8):
+        base = ["int32", "double", "int8", "float"][i % 4]
+        pair = Pair(prod, oracle, g.gen(base))
+        count = int(rng.integers(1, 7))
+        lo, hi, size = footprint(oracle, pair.ho, count)
+        total = size * count
+        typed = fill(rng, hi - lo + 64, base)
+        tg = dev_copy(cuda, typed)
+        exp = np.zeros(total + 16, dtype=np.uint8)
+        oracle.pack(typed.ctypes.data + 32 - lo, count, pair.ho, 0, exp.ctypes.data, total)
+        pg = cuda.zeros(total + 16, dtype=cuda.uint8, device="cuda")
+        parts = [prod.shard(pair.hp, count, r, nranks) for r in range(nranks)]
+        assert sum(n for _, n in parts) == total
+        for off, n in parts:
+            assert prod.pack(tg.data_ptr() + 32 - lo, count, pair.hp, off, pg.data_ptr() + off, n) == n
+        cuda.cuda.synchronize()
+        assert np.array_equal(host_of(cuda, pg)[:total], exp[:total])
+        # unpack the parts into a fresh buffer, in reverse order (no order between parts)
+        dst = fill(rng, hi - lo + 64, base)
+        dg, d_o = dev_copy(cuda, dst), dst.copy()
+        oracle.unpack(exp.ctypes.data, total, d_o.ctypes.data + 32 - lo, count, pair.ho, 0)
+        pe = dev_copy(cuda, exp)
+        for off, n in reversed(parts):
+            assert prod.unpack(pe.data_ptr() + off, n, dg.data_ptr() + 32 - lo, count, pair.hp, off) == n
+        cuda.cuda.synchronize()
+        ok = np.array_equal(host_of(cuda, dg), d_o)
+        offs = np.empty(total, dtype=np.int64)
+        f = oracle.lib.yaksa_oracle_byte_offsets
+        import ctypes
+        f.restype = ctypes.c_int
+        f.argtypes = [ctypes.c_uint64, ctypes.c_size_t, ctypes.c_void_p]
+        assert f(pair.ho, count, offs.ctypes.data) == 0
+        if len(np.unique(offs)) == total:       # no byte reached twice: order is free
+            assert ok
+        pair.free()
+    g.free()
