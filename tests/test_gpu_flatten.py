@@ -7,7 +7,6 @@ Tolerance: byte-identical (REPLACE only moves bytes).
 import numpy as np
 import pytest
 
-import yaksa_gb300 as yk
 from helpers import Pair, assert_same_bytes, dev_copy, fill, host_of
 from typegen import Gen, footprint
 

@@ -11,7 +11,6 @@ import threading
 import numpy as np
 import pytest
 
-import yaksa_gb300 as yk
 from helpers import fill
 from typegen import Gen, build, footprint
 
