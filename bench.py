@@ -110,6 +110,19 @@ def make_faces(y, yk):
             for name, sub, st in FACES]
 
 
+def cpu_model():
+    """The host CPU's model name (lscpu), for the baseline records."""
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
 def cpu_baseline(oracle_path, seconds, threads):
     """The oracle (CPU restatement of the reference's seq path) on the host cores."""
     import numpy as np
@@ -166,6 +179,7 @@ def cpu_baseline(oracle_path, seconds, threads):
     o.finalize()
     moved = 2 * P * len(faces) * n
     return {"value": moved / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
+            "cpu": cpu_model(),
             "sample": f"{n} steps of the 6-face pack+unpack on the host (host buffers), "
                       f"{dt:.2f} s", "ok": ok}
 
@@ -190,6 +204,7 @@ def run_reference(args):
             "bit_exact": bool(b["ok"]),
             "config": {"workload": WORKLOAD, "parallelism": "host threads", "l2": "host caches"},
             "cpu_baseline": {"value": b["value"], "unit": "GB/s", "cores": threads, "kind": "port",
+                             "cpu": b["cpu"],
                              "sample": b["sample"], "faces_equal": bool(b["ok"])},
             "e2e": {"value": b["value"], "unit": "GB/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
@@ -977,7 +992,7 @@ def main():
         if not os.path.exists(oracle_path):
             subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
         b = cpu_baseline(oracle_path, args.cpu_seconds, 1)
-        line["cpu_baseline"] = {k: b[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        line["cpu_baseline"] = {k: b[k] for k in ("value", "unit", "cores", "kind", "cpu", "sample")}
         line["cpu_baseline"]["faces_equal"] = bool(b["ok"])
     if rank == 0:
         print(json.dumps(line))
