@@ -185,6 +185,8 @@ DENSE_STRUCTS = [
     ([1, 2], [0, 8], [yk.TYPE_DOUBLE, yk.TYPE_FLOAT], None),       # natural extent 16
     ([7], [0], [yk.TYPE_INT8_T], 12),                              # 1-byte units
     ([60, 1], [0, 248], [yk.TYPE_INT32_T, yk.TYPE_INT32_T], 256),  # 244 B over 256 B
+    ([4, 1], [0, 32], [yk.TYPE_INT64_T, yk.TYPE_INT32_T], 48),     # 36 B run in 48 B
+    ([3], [0], [yk.TYPE_DOUBLE], 32),                              # 24 B run, 8-byte units
 ]
 
 

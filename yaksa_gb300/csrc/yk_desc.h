@@ -162,6 +162,10 @@ typedef struct {
 } yk_server_args;
 
 int yk_cuda_server_launch(const yk_server_args * a, int ctas, void *stream);
+
+/* REPLACE pack of whole elements of one VEC level over a run of 17..47 bytes (not a
+ * multiple of 16) that starts on 16 bytes in every element; units of 4 or 8 bytes */
+int yk_cuda_launch_runs_pack(const yk_launch * l, uint32_t run, void *stream);
 int yk_cuda_server_ctas(void);
 
 /* Granlund-Montgomery constants for dividing by l->cps (host side). */

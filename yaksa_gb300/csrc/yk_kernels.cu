@@ -427,6 +427,43 @@ yk_hidx32_kernel(const __grid_constant__ yk_launch L)
 }
 
 
+/* Pack of whole elements whose one run (16 < R <= 48 bytes, not a multiple of 16)
+ * starts on 16 bytes in every element (extent a multiple of 16): one element per
+ * thread, read with ceil(R/16) 16-byte loads and written as R/G pieces of G bytes (the
+ * packed side of element i sits at i*R, on G bytes only).  A 16-byte load may cover
+ * bytes past the run, but never past the 16-byte block that holds the run's last byte,
+ * so it stays inside the caller's page.  Five 4-byte loads per element become two for a
+ * 20-byte struct run. */
+template <int G>
+__global__ void __launch_bounds__(YK_THREADS, 8)
+yk_runs_pack_kernel(const __grid_constant__ yk_launch L, uint32_t R)
+{
+    typedef typename yk_vec<G>::T GT;
+    const yk_level & l0 = L.desc.lv[0];
+    const int64_t E = l0.stride;
+    const uint32_t nel = (uint32_t) (L.nbytes / R), e0 = (uint32_t) (L.p0 / R);
+    const char *tb = L.typed + L.desc.base;
+    const uint32_t nv = (R + 15) / 16, np = R / G;
+    for (uint32_t i = blockIdx.x * YK_THREADS + threadIdx.x; i < nel; i += gridDim.x * YK_THREADS) {
+        const char *src = tb + (int64_t) (e0 + i) * E;
+        union {
+            uint4 w[3];
+            GT g[48 / G];
+        } v;
+#pragma unroll
+        for (int k = 0; k < 3; k++)
+            if ((uint32_t) k < nv)
+                v.w[k] = yk_ldcg((const uint4 *) (src + 16 * k));
+        char *dst = L.packed + (uint64_t) i * R;
+#pragma unroll
+        for (int j = 0; j < 48 / G; j++)
+            if ((uint32_t) j < np)
+                *(GT *) (dst + j * G) = v.g[j];
+    }
+}
+
+extern "C" int yk_cuda_launch_runs_pack(const yk_launch * l, uint32_t run, void *stream);
+
 template <typename IDX, int V, int DIR, int U>
 __global__ void __launch_bounds__(YK_THREADS)
 yk_bytes_kernel(const __grid_constant__ yk_launch L)
@@ -1741,6 +1778,18 @@ static bool yk_owner_lane_launch(const yk_launch & c, int bt, int rshift, cudaSt
         case YK_BT_C64: return yk_owner_lane_cplx<YK_BT_C64>(c, rshift, s, g, 0);
     }
     return false;
+}
+
+extern "C" int yk_cuda_launch_runs_pack(const yk_launch * l, uint32_t run, void *stream)
+{
+    const uint64_t nel = l->nbytes / run;
+    const unsigned g = yk_grid(nel, YK_THREADS, 8);
+    cudaStream_t s = (cudaStream_t) stream;
+    if (l->vec == 8)
+        yk_runs_pack_kernel<8><<<g, YK_THREADS, 0, s>>>(*l, run);
+    else
+        yk_runs_pack_kernel<4><<<g, YK_THREADS, 0, s>>>(*l, run);
+    return (int) cudaGetLastError();
 }
 
 extern "C" int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blocks, void *stream)

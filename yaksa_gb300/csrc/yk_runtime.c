@@ -505,6 +505,26 @@ static int prepare(const yk_plan * p, char *typed, char *packed, yk_launch * L, 
     return prepare_with(p, typed, packed, L, kind, sorted, yk_desc_get);
 }
 
+/* A pack of whole elements of one VEC level over a run of 17..47 bytes (not a multiple
+ * of 16, so the byte kernels would take 4- or 8-byte units) that starts on 16 bytes in
+ * every element: one thread per element, 16-byte loads (yk_cuda_launch_runs_pack).
+ * YAKSA_GB300_RUNS_PACK=0 in the environment keeps such packs on the byte kernels. */
+static int runs_pack_ok(const yk_launch * L)
+{
+    static int on = -1;
+    if (on < 0) {
+        const char *e = getenv("YAKSA_GB300_RUNS_PACK");
+        on = !(e && e[0] == '0');
+    }
+    const uint64_t r = L->desc.run;
+    return on && L->dir == 0 && !L->typed_op && !L->use64 && L->regular == 1 &&
+        L->desc.leaf == YK_LEAF_RUN && L->desc.lv[0].kind == YK_LV_VEC && L->desc.lv[0].cps == r &&
+        r > 16 && r < 48 && r % 16 && (L->vec == 4 || L->vec == 8) && r % (uint64_t) L->vec == 0 &&
+        L->desc.lv[0].stride > 0 && L->desc.lv[0].stride % 16 == 0 &&
+        ((uintptr_t) L->typed + (uintptr_t) L->desc.base) % 16 == 0 &&
+        L->p0 % r == 0 && L->nbytes % r == 0 && L->nbytes / r > 0;
+}
+
 /* tune: pick the launch shape of the REPLACE byte kernels with the autotuner (off for
  * the no-allocation entry point, whose timing events would be a resource allocation) */
 static int launch_prepared(const yk_plan * p, const yk_launch * L, int kind, int sorted,
@@ -521,6 +541,9 @@ static int launch_prepared(const yk_plan * p, const yk_launch * L, int kind, int
     __atomic_add_fetch(&R.launches, 1, __ATOMIC_RELAXED);
     if (kind == YK_X_ORDERED)
         return cuda_err((cudaError_t) yk_cuda_launch_unpack_ordered(L, sorted, s), "kernel launch");
+    if (kind == YK_X_BYTES && runs_pack_ok(L))
+        return cuda_err((cudaError_t) yk_cuda_launch_runs_pack(L, (uint32_t) L->desc.run, s),
+                        "kernel launch");
     yk_tune_cfg cfg = { 0, 0 };
     int probe = -1;
     if (tune && kind == YK_X_BYTES && !L->hidx) {
