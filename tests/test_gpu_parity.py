@@ -225,6 +225,21 @@ def test_dense_struct_pack(cuda, prod, oracle, k):
     oracle.type_free(to)
 
 
+def test_dense_struct_pack_byte_kernels(cuda):
+    """The dense-struct packs again in a child process with YAKSA_GB300_RUNS_PACK=0, so
+    the byte kernels take the struct-like runs too."""
+    import os
+    import subprocess
+    import sys
+    here = os.path.dirname(os.path.abspath(__file__))
+    r = subprocess.run([sys.executable, "-m", "pytest", "-x", "-q", "-p", "no:cacheprovider",
+                        os.path.join(here, "test_gpu_parity.py"), "-k",
+                        "dense_struct_pack and not byte_kernels"],
+                       env=dict(os.environ, YAKSA_GB300_RUNS_PACK="0"),
+                       capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
+
+
 def test_nonblocking_and_stream(cuda, prod, oracle):
     t = prod.type_create_hvector(1024, 4, 128, yk.TYPE_DOUBLE)
     src = cuda.randn(1024 * 16, dtype=cuda.float64, device="cuda")
