@@ -1,18 +1,31 @@
 #!/usr/bin/env python3
-"""Benchmark of the GB300 pack/unpack engine.
+"""Benchmark of the GB300 pack/unpack engine: every configuration of the metric, on one GPU.
 
-Default workload ("halo3d"): a 512^3 float32 grid (uniform [-1, 1) from a seed) and
-its six depth-2 halo faces described as subarray types (x-faces {512,512,2}: 8-byte runs
-at a 2 KiB row stride; y-faces {512,2,512}: 4 KiB runs per plane; z-faces {2,512,512}:
-one 2 MiB run).  One step = pack all six faces into contiguous device buffers, then
-unpack them with REPLACE into a second grid.  Inputs are synthetic and seeded.
+Headline ("halo3d", the 3-level nested halo faces): a 512^3 float32 grid (uniform
+[-1, 1) from a seed) and its six depth-2 halo faces described as subarray types (x-faces
+{512,512,2}: 8-byte runs at a 2 KiB row stride; y-faces {512,2,512}: 4 KiB runs per
+plane; z-faces {2,512,512}: one 2 MiB run).  One step = pack every face into its own
+contiguous device buffer, then unpack every face with REPLACE into a second grid, on the
+plain path: one yaksa_pack_stream / yaksa_unpack_stream call per face, each face on its
+own stream (as a halo exchange posts one message per neighbour), the twelve calls
+captured once into a CUDA graph and replayed per step.  Reported per face as well.
 
-Metric: packed GB/s of pack+unpack (bytes packed + bytes unpacked per second, whole
-job), next to the HBM roofline of the pack/unpack kernel whose algorithmic traffic is
-2 bytes per packed byte per direction (read strided + write contiguous, or the mirror).
+The same run measures, each as its own record with a full-size byte comparison against
+the oracle and the oracle's own time on the host cores:
+  hvector     4-column block of a 1024x16 double matrix (hvector 1024 x 4 doubles, stride 128 B)
+  hindexed    int32, 2^20 lognormal blocks at shuffled non-overlapping places in 1 GiB
+  struct      {int64, float x3} resized to 32 B, count 8M
+  reduce_*    indexed_block 2^22 x 8 at sorted random offsets over 256 MiB targets, unpacked
+              with SUM (double), MAX (int64), BXOR (uint32), PROD (complex float)
+and the mixed request stream (10,000 requests, Poisson 50k/s) through the plain
+per-request path and the persistent-kernel server, p50/p99 latency and capacity.
+
+Metric: packed GB/s (bytes packed + bytes unpacked per second), next to the HBM
+roofline: REPLACE moves 2 bytes per packed byte (read strided + write contiguous, or the
+mirror), an operator 3 (read packed, read target, write target).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--no-cpu] [--no-stream] [--cpu-seconds S]
+                    [--no-cpu] [--no-stream] [--no-suite] [--cpu-seconds S]
     python bench.py --suite out.jsonl [--suite-only hindexed,struct,...] [--suite-scale K]
     python bench.py --stream out.json [--stream-requests R]
 """
@@ -23,13 +36,15 @@ import os
 import statistics
 import subprocess
 import sys
-import threading
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N = int(os.environ.get("YK_BENCH_N", "512"))   # grid edge; smaller only for ncu captures
+ORACLE_LIB = os.path.join(ROOT, "oracle", "_ref", "liboracle_yaksa.so")
+PROFILES = os.path.join(ROOT, "profiles")
 
 
 def face_specs(n):
@@ -42,6 +57,9 @@ def face_specs(n):
 FACES = face_specs(N)
 L2_FLUSH_BYTES = 512 << 20
 TUNE_CALLS = 28     # calls per shape class before the autotuner has chosen (5 shapes x 4 + slack)
+METRIC = "pack+unpack GB/s vs HBM peak (bit-exact); batched p50/p99 us vs plain path"
+WORKLOAD = (f"halo3d: {N}^3 float32 grid, 6 depth-2 subarray faces ({2 * N * N * 4 >> 20} MiB "
+            "packed each), pack + unpack REPLACE per step, plain path (one call per face)")
 
 
 def peaks():
@@ -50,6 +68,26 @@ def peaks():
         d = json.load(open(p))
         return d["hbm_gbs"], "measured"
     return 6800.0, "fallback"
+
+
+def ensure_oracle():
+    if not os.path.exists(ORACLE_LIB):
+        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    return ORACLE_LIB
+
+
+def ncu_traffic(name):
+    """dram__bytes_read.sum + dram__bytes_write.sum per launch, from the committed ncu
+    summary of a kernel and workload (the `traffic:` lines of profiles/<name>.md), or
+    None when no capture exists."""
+    p = os.path.join(PROFILES, name + ".md")
+    out = {}
+    if os.path.exists(p):
+        for line in open(p):
+            if line.startswith("traffic:"):
+                k, v = line[len("traffic:"):].split("=")
+                out[k.strip()] = float(v)
+    return out
 
 
 class Clocks:
@@ -105,9 +143,18 @@ class ColdL2:
         self.sink = self.r.sum()
 
 
-def make_faces(y, yk):
-    return [(name, y.type_create_subarray([N, N, N], sub, st, yk.SUBARRAY_ORDER_C, yk.TYPE_FLOAT))
-            for name, sub, st in FACES]
+def event_time(torch, fn, reps, flush, stat=statistics.median):
+    """CUDA-event time of fn() on torch's current stream, a cold L2 before each rep."""
+    ts = []
+    for _ in range(reps):
+        flush()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1) * 1e-3)
+    return stat(ts)
 
 
 def cpu_model():
@@ -123,11 +170,68 @@ def cpu_model():
     return platform.processor() or platform.machine()
 
 
-def cpu_baseline(oracle_path, seconds, threads):
-    """The oracle (CPU restatement of the reference's seq path) on the host cores."""
+# ---------------------------------------------------------------------------
+# the oracle on the host cores: one thread, or every core through its thread pool
+# ---------------------------------------------------------------------------
+
+class OracleJob(ctypes.Structure):
+    """oracle_job (oracle/oracle_pool.c)"""
+    _fields_ = [("dir", ctypes.c_int), ("typed_in", ctypes.c_void_p), ("typed_out", ctypes.c_void_p),
+                ("count", ctypes.c_size_t), ("type", ctypes.c_uint64), ("packed", ctypes.c_void_p),
+                ("total", ctypes.c_size_t), ("granule", ctypes.c_size_t), ("op", ctypes.c_uint64)]
+
+
+class OraclePool:
+    """The oracle's persistent thread pool: each job's packed range split on builtin
+    boundaries over `threads` host threads created once (oracle/oracle_pool.c)."""
+
+    def __init__(self, oracle, threads):
+        self.lib = oracle.lib
+        self.lib.oracle_pool_start.argtypes = [ctypes.c_int]
+        self.lib.oracle_pool_run.argtypes = [ctypes.POINTER(OracleJob), ctypes.c_int, ctypes.c_int]
+        self.lib.oracle_pool_run.restype = ctypes.c_double
+        self.threads = threads
+        assert self.lib.oracle_pool_start(threads) == 0, "oracle pool start failed"
+
+    def run(self, jobs, reps=1):
+        arr = (OracleJob * len(jobs))(*jobs)
+        s = self.lib.oracle_pool_run(arr, len(jobs), reps)
+        assert s >= 0, "an oracle call of the pool failed"
+        return s
+
+    def stop(self):
+        self.lib.oracle_pool_stop()
+
+
+def halo_jobs(faces, src, dst, bufs, P):
+    """pack every face (granule 4: float), then unpack every face; a thread's unpack part
+    reads the packed bytes its own pack part wrote"""
+    jobs = [OracleJob(0, src.ctypes.data, None, 1, t, b.ctypes.data, P, 4, 10)
+            for (_, t), b in zip(faces, bufs)]
+    jobs += [OracleJob(1, None, dst.ctypes.data, 1, t, b.ctypes.data, P, 4, 10)
+             for (_, t), b in zip(faces, bufs)]
+    return jobs
+
+
+def make_faces(y, yk, n=N):
+    return [(name, y.type_create_subarray([n, n, n], sub, st, yk.SUBARRAY_ORDER_C, yk.TYPE_FLOAT))
+            for name, sub, st in face_specs(n)]
+
+
+def faces_equal_np(np, src, dst, n=N):
+    s3, d3 = src.reshape(n, n, n), dst.reshape(n, n, n)
+    return all(np.array_equal(s3[sl], d3[sl]) for sl in
+               ((slice(None), slice(None), slice(0, 2)), (slice(None), slice(None), slice(n - 2, n)),
+                (slice(None), slice(0, 2)), (slice(None), slice(n - 2, n)), (slice(0, 2),),
+                (slice(n - 2, n),)))
+
+
+def cpu_halo(seconds, threads):
+    """The oracle (CPU restatement of the reference's seq path) over the halo step on the
+    host cores; threads > 1 runs through the oracle's persistent pool."""
     import numpy as np
     import yaksa_gb300 as yk
-    o = yk.Yaksa(oracle_path)
+    o = yk.Yaksa(ensure_oracle())
     o.init()
     faces = make_faces(o, yk)
     rng = np.random.default_rng(1)
@@ -135,89 +239,50 @@ def cpu_baseline(oracle_path, seconds, threads):
     dst = np.zeros_like(src)
     P = 2 * N * N * 4
     bufs = [np.zeros(P // 4, dtype=np.float32) for _ in faces]
-
-    def one_face_range(i, off, ln, direction):
-        t = faces[i][1]
-        if direction == 0:
-            o.pack(src.ctypes.data, 1, t, off, bufs[i].ctypes.data + off, ln)
-        else:
-            o.unpack(bufs[i].ctypes.data + off, ln, dst.ctypes.data, 1, t, off)
-
-    def step():
-        for direction in (0, 1):
-            if threads == 1:
-                for i in range(len(faces)):
-                    one_face_range(i, 0, P, direction)
-            else:
-                chunk = P // threads
-                work = [(i, k * chunk, chunk) for i in range(len(faces)) for k in range(threads)]
-                ths = []
-                for tid in range(threads):
-                    mine = work[tid::threads]
-                    th = threading.Thread(target=lambda m=mine: [one_face_range(i, off, ln, direction)
-                                                                 for (i, off, ln) in m])
-                    th.start()
-                    ths.append(th)
-                for th in ths:
-                    th.join()
-
-    step()  # warm
-    t0 = time.perf_counter()
-    n = 0
-    while True:
-        step()
-        n += 1
-        if time.perf_counter() - t0 > seconds:
-            break
-    dt = time.perf_counter() - t0
-    # correctness of the sample: every face of dst equals that face of src
-    s3, d3 = src.reshape(N, N, N), dst.reshape(N, N, N)
-    ok = all(np.array_equal(s3[sl], d3[sl]) for sl in
-             ((slice(None), slice(None), slice(0, 2)), (slice(None), slice(None), slice(N - 2, N)),
-              (slice(None), slice(0, 2)), (slice(None), slice(N - 2, N)), (slice(0, 2),),
-              (slice(N - 2, N),)))
+    pool = OraclePool(o, threads)
+    jobs = halo_jobs(faces, src, dst, bufs, P)
+    one = pool.run(jobs, 1)     # warm
+    reps = max(1, int(seconds / max(one, 1e-4)))
+    t = pool.run(jobs, reps)
+    pool.stop()
+    ok = faces_equal_np(np, src, dst)
+    for _, tt in faces:
+        o.type_free(tt)
     o.finalize()
-    moved = 2 * P * len(faces) * n
-    return {"value": moved / dt / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
+    moved = 2 * P * len(faces)
+    return {"value": moved / t / 1e9, "unit": "GB/s", "cores": threads, "kind": "port",
             "cpu": cpu_model(),
-            "sample": f"{n} steps of the 6-face pack+unpack on the host (host buffers), "
-                      f"{dt:.2f} s", "ok": ok}
+            "sample": f"{reps} steps of the 6-face pack+unpack on the host (host buffers, "
+                      f"{threads} thread{'s' if threads > 1 else ''}), {reps * t:.2f} s",
+            "ok": ok, "s_per_step": t}
 
 
 def run_reference(args):
-    """--impl reference: the CPU implementation of the path on the host cores."""
+    """--impl reference: the CPU implementation of the path (the oracle, restated from the
+    reference's seq backend) on every host core, through its persistent thread pool."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    from __graft_entry__ import build  # noqa: F401
-    oracle_path = os.path.join(ROOT, "oracle", "_ref", "liboracle_yaksa.so")
-    if not os.path.exists(oracle_path):
-        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
     threads = os.cpu_count() or 1
     seconds = max(2.0, min(30.0, 1.0 * args.steps))
-    b = cpu_baseline(oracle_path, seconds, threads)
+    b = cpu_halo(seconds, threads)
     step_bytes = 2 * (2 * N * N * 4) * 6      # six 2 MiB faces, packed and unpacked
     line = {"impl": "reference", "metric": METRIC, "value": b["value"], "unit": "GB/s",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": step_bytes / (b["value"] * 1e9) * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "bit_exact": bool(b["ok"]),
-            "config": {"workload": WORKLOAD, "parallelism": "host threads", "l2": "host caches"},
+            "config": {"workload": WORKLOAD, "parallelism": f"host threads x{threads}",
+                       "l2": "host caches"},
             "cpu_baseline": {"value": b["value"], "unit": "GB/s", "cores": threads, "kind": "port",
-                             "cpu": b["cpu"],
-                             "sample": b["sample"], "faces_equal": bool(b["ok"])},
+                             "cpu": b["cpu"], "sample": b["sample"], "faces_equal": bool(b["ok"])},
             "e2e": {"value": b["value"], "unit": "GB/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 
 
-METRIC = "pack+unpack GB/s vs HBM peak (bit-exact); batched p50/p99 us vs plain path"
-WORKLOAD = (f"halo3d: {N}^3 float32 grid, 6 depth-2 subarray faces ({2 * N * N * 4 >> 20} MiB "
-            "packed each), pack + unpack REPLACE per step")
-
-
 # ---------------------------------------------------------------------------
-# the other configurations: one JSON line per (config, direction) with a full-size
+# the other configurations: one record per (config, direction) with a full-size
 # byte comparison against the oracle and the oracle's own time on the host
 # ---------------------------------------------------------------------------
 
@@ -229,12 +294,6 @@ def suite_types(y, yk, np, rng_seed=7, scale=1):
     # hvector of double: 4-column block of a 1024x16 row-major matrix
     out["hvector"] = dict(mk=lambda L: L.type_create_hvector(1024, 4, 128, yk.TYPE_DOUBLE),
                           base="double", count=1, extent=1024 * 16 * 8, gran=8)
-    # halo faces of the 512^3 float grid, one per orientation (the +/- faces mirror them)
-    for name, sub, st in face_specs(512)[0::2]:
-        out["halo_" + name[0]] = dict(
-            mk=lambda L, sub=sub, st=st: L.type_create_subarray([512, 512, 512], sub, st,
-                                                                yk.SUBARRAY_ORDER_C, yk.TYPE_FLOAT),
-            base="float", count=1, extent=512 ** 3 * 4, gran=4)
     # hindexed int32: 2^20 blocks, lognormal lengths (median 16, sigma 1, clipped 1..4096),
     # non-overlapping blocks in shuffled order with random gaps inside 1 GiB
     nb = (1 << 20) // scale
@@ -292,14 +351,24 @@ def suite_fill(np, rng, base, nbytes):
     return rng.uniform(-1, 1, nbytes // 4).astype(np.float32).view(np.uint8)
 
 
-def run_suite(out_path, steps, cpu_seconds, only=None, scale=1):
+# the committed ncu summary (profiles/<name>.md) whose `traffic: <key> = bytes` line gives
+# the DRAM bytes of a config's launch, and the full config's size over the captured case's
+SUITE_PROFILE = {("hindexed", "pack"): ("yk_hidx32_kernel_hindexed", "pack", 2),
+                 ("struct", "pack"): ("yk_runs_pack_kernel_struct", "pack", 2),
+                 ("struct", "unpack"): ("yk_regular_kernel_struct", "unpack", 2),
+                 ("reduce_double", "unpack"): ("yk_owner_lane_kernel_reduce", "double_sum", 2),
+                 ("reduce_uint32", "unpack"): ("yk_owner_chunk_kernel_reduce_uint32", "uint32_bxor", 2),
+                 ("reduce_int64", "unpack"): ("yk_owner_chunk_kernel_reduce_uint32", "int64_max", 2)}
+
+
+def run_suite(steps, only=None, scale=1, threads=None, log=None):
+    """One record per (config, direction): CUDA-event kernel time (median, cold L2), the
+    HBM roofline of algorithmic bytes, the full-size byte comparison with the oracle,
+    and the oracle's time on 1 thread and on every host core."""
     import numpy as np
     import torch
     import yaksa_gb300 as yk
-    oracle_path = os.path.join(ROOT, "oracle", "_ref", "liboracle_yaksa.so")
-    if not os.path.exists(oracle_path):
-        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
-    y, o = yk.Yaksa(), yk.Yaksa(oracle_path)
+    y, o = yk.Yaksa(), yk.Yaksa(ensure_oracle())
     y.init()
     o.init()
     hbm, peak_kind = peaks()
@@ -308,7 +377,8 @@ def run_suite(out_path, steps, cpu_seconds, only=None, scale=1):
     sh = ctypes.c_void_p(stream.cuda_stream)
     shp = ctypes.addressof(sh)
     rng = np.random.default_rng(11)
-    threads = os.cpu_count() or 1
+    threads = threads or os.cpu_count() or 1
+    pool = OraclePool(o, threads)
     lines = []
     for name, w in suite_types(y, yk, np, scale=scale).items():
         if only and name not in only:
@@ -317,14 +387,16 @@ def run_suite(out_path, steps, cpu_seconds, only=None, scale=1):
         size = y.size(tp)
         count = w["count"]
         P = size * count
-        ext = w["extent"] * (1 if count == 1 else 1)
-        typed_h = suite_fill(np, rng, w["base"], ext)
+        typed_h = suite_fill(np, rng, w["base"], w["extent"])
         packed0 = suite_fill(np, rng, w["base"], P)
         typed_d = torch.from_numpy(typed_h).cuda()
         packed_d = torch.from_numpy(packed0).cuda()
         op = w.get("op", yk.OP_REPLACE)
         dirs = ["unpack"] if op != yk.OP_REPLACE else ["pack", "unpack"]
         for d in dirs:
+            prof = SUITE_PROFILE.get((name, d))
+            tr = ncu_traffic(prof[0]).get(prof[1]) if prof else None
+            tr = tr * prof[2] / scale if tr else None
             def call():
                 if d == "pack":
                     y.pack_stream(typed_d.data_ptr(), count, tp, 0, packed_d.data_ptr(), P, shp, op=op)
@@ -342,64 +414,51 @@ def run_suite(out_path, steps, cpu_seconds, only=None, scale=1):
             else:
                 o.unpack(ph.ctypes.data, P, th.ctypes.data, count, to, 0, op=op)
             cpu_t = time.perf_counter() - t0
-            exact = (np.array_equal(typed_d.cpu().numpy(), th) and np.array_equal(packed_d.cpu().numpy(), ph))
-            # the oracle on every host core: the packed range split at multiples of the
-            # granule (builtin boundaries) through the API's offset/max-bytes arguments;
-            # not for overlapping targets, whose order only one thread keeps
+            exact = bool(np.array_equal(typed_d.cpu().numpy(), th) and
+                         np.array_equal(packed_d.cpu().numpy(), ph))
+            # every host core: the packed range split at multiples of the granule
+            # (builtin boundaries) through the API's offset/max-bytes arguments, on the
+            # oracle's persistent pool; not for overlapping targets, whose order only
+            # one thread keeps
             cpu_nt, nt_exact = None, None
             if w["gran"]:
                 th2, ph2 = typed_h.copy(), packed0.copy()
-                chunk = max(w["gran"], P // threads // w["gran"] * w["gran"])
-                ranges = [(a, min(chunk, P - a)) for a in range(0, P, chunk)]
-
-                def part(rs, th2=th2, ph2=ph2):
-                    for a, n in rs:
-                        if d == "pack":
-                            o.pack(th2.ctypes.data, count, to, a, ph2.ctypes.data + a, n, op=op)
-                        else:
-                            o.unpack(ph2.ctypes.data + a, n, th2.ctypes.data, count, to, a, op=op)
-                ths = [threading.Thread(target=part, args=(ranges[k::threads],)) for k in range(threads)]
-                t0 = time.perf_counter()
-                for x in ths:
-                    x.start()
-                for x in ths:
-                    x.join()
-                cpu_nt = time.perf_counter() - t0
+                job = (OracleJob(0, th2.ctypes.data, None, count, to, ph2.ctypes.data, P, w["gran"], op)
+                       if d == "pack" else
+                       OracleJob(1, None, th2.ctypes.data, count, to, ph2.ctypes.data, P, w["gran"], op))
+                cpu_nt = pool.run([job], 1)
                 nt_exact = bool(np.array_equal(th2, th) and np.array_equal(ph2, ph))
+                del th2, ph2
+            del th, ph
             # untimed calls while the launch-shape autotuner settles, then timing: fresh L2
             # each launch, CUDA events on the launching stream
             for _ in range(TUNE_CALLS):
                 call()
-            ts = []
-            for rep in range(max(3, steps)):
-                flush()
-                e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-                e0.record()
-                call()
-                e1.record()
-                e1.synchronize()
-                ts.append(e0.elapsed_time(e1) * 1e-3)
-            t = statistics.median(ts[1:])
+            t = event_time(torch, call, max(3, steps), flush)
             alg = (2 if op == yk.OP_REPLACE else 3) * P
             line = {"workload": name, "direction": d, "op": int(op), "packed_bytes": P,
-                    "algorithmic_bytes": alg, "time_us": t * 1e6, "packed_GBps": P / t / 1e9,
-                    "achieved_GBps": alg / t / 1e9, "hbm_frac": alg / t / 1e9 / hbm,
-                    "peak": hbm, "peak_source": peak_kind, "bit_exact": bool(exact),
-                    "cpu_oracle_s": cpu_t, "cpu_oracle_packed_GBps": P / cpu_t / 1e9,
-                    "gpu_over_cpu": cpu_t / t,
-                    "cpu_oracle_threads": threads if cpu_nt else None,
-                    "cpu_oracle_nthr_packed_GBps": P / cpu_nt / 1e9 if cpu_nt else None,
-                    "cpu_nthr_same_bytes": nt_exact}
+                    "time_us": t * 1e6, "packed_GBps": P / t / 1e9,
+                    "roofline": {"bound": "hbm", "achieved": alg / t / 1e9, "peak": hbm, "unit": "GB/s",
+                                 "frac": alg / t / 1e9 / hbm, "peak_source": peak_kind,
+                                 "algorithmic_bytes": alg,
+                                 "traffic": tr, "traffic_frac": tr / t / 1e9 / hbm if tr else None},
+                    "bit_exact": exact,
+                    "cpu_oracle": {"threads": 1, "s": cpu_t, "packed_GBps": P / cpu_t / 1e9},
+                    "cpu_oracle_all_cores": ({"threads": threads, "s": cpu_nt, "packed_GBps": P / cpu_nt / 1e9,
+                                              "same_bytes": nt_exact} if cpu_nt else
+                                             {"note": "overlapping targets: one thread keeps the order"}),
+                    "gpu_over_cpu_1thr": cpu_t / t}
             lines.append(line)
-            print(json.dumps(line), file=sys.stderr, flush=True)
+            if log:
+                print(json.dumps(line), file=log, flush=True)
         y.type_free(tp)
         o.type_free(to)
-        del typed_d, packed_d
+        del typed_d, packed_d, typed_h, packed0
         torch.cuda.empty_cache()
-    if out_path:
-        with open(out_path, "w") as f:
-            for l in lines:
-                f.write(json.dumps(l) + "\n")
+    pool.stop()
+    o.finalize()
+    del flush
+    torch.cuda.empty_cache()
     return lines
 
 
@@ -428,7 +487,7 @@ def stream_family_types(yk, np, seed):
         x0 = int(rng.choice([0, 510]))
         out[("halo", S)] = dict(mk=lambda L, Z=Z, Y=Y, x0=x0: L.type_create_subarray(
             [Z, Y, 512], [Z, Y, 2], [0, 0, x0], yk.SUBARRAY_ORDER_C, yk.TYPE_FLOAT),
-            base="float", count=1, extent=Z * Y * 2048, op=yk.OP_REPLACE)
+            base="float", count=1, extent=Z * Y * 2048, op=yk.OP_REPLACE, xface=(Z, Y, x0))
         # hindexed int32: lognormal block lengths (median 16, sigma 1, clipped 1..4096),
         # non-overlapping blocks in shuffled order inside a resized extent of 4 S
         nel = S // 4
@@ -496,19 +555,21 @@ def dev_fill(torch, base, nbytes, gen):
     return out
 
 
-def run_stream(nreq=10000, rate=50e3, seed=5, check=True, log=None):
+def run_stream(nreq=10000, rate=50e3, seed=5, check=True, log=None, floor=True):
     """10,000 pack/unpack requests with Poisson arrivals at `rate` req/s: families drawn
     uniformly from hvector/halo/hindexed/struct/reduce, packed sizes log-uniform over
     19 power-of-two classes 256 B .. 64 MiB, 20% with the packed buffer in pinned host
     memory.  Each request uses its (family, class) arena: one typed buffer per family
-    and one packed buffer per (family, class, host); checked requests own private
-    buffers and are compared with the oracle after each path.  Returns a dict."""
+    and one packed buffer per (family, class, host).  Checked requests own private
+    buffers and are compared with the oracle after each path: 120 small ones and, for
+    every size class, at least one whose typed footprint is at most 256 MiB (the halo
+    family's footprint is 256 times its packed size, so its largest classes are checked
+    through the other families).  Returns a dict."""
     import numpy as np
     import torch
     import yaksa_gb300 as yk
-    oracle_path = os.path.join(ROOT, "oracle", "_ref", "liboracle_yaksa.so")
-    if check and not os.path.exists(oracle_path):
-        subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
+    if check:
+        ensure_oracle()
     y = yk.Yaksa()
     y.init()
     specs = stream_family_types(yk, np, seed)
@@ -542,9 +603,15 @@ def run_stream(nreq=10000, rate=50e3, seed=5, check=True, log=None):
     for i in range(nreq):
         if host_of[i] and keys[i] not in packed_h:
             packed_h[keys[i]] = packed_d[keys[i]].cpu().pin_memory()
-    # checked requests: small ones, private buffers
-    small = [i for i in range(nreq) if keys[i][1] <= (256 << 10)]
-    chk = set(rng.choice(small, size=min(len(small), 120), replace=False).tolist()) if check else set()
+    # checked requests: 120 small ones, and every size class
+    chk = set()
+    if check:
+        small = [i for i in range(nreq) if keys[i][1] <= (256 << 10)]
+        chk = set(rng.choice(small, size=min(len(small), 120), replace=False).tolist())
+        for S in STREAM_CLASSES:
+            cand = [i for i in range(nreq) if keys[i][1] == S and specs[keys[i]]["extent"] <= (256 << 20)]
+            if cand:
+                chk.update(rng.choice(cand, size=min(2, len(cand)), replace=False).tolist())
     priv = {}
     for i in sorted(chk):
         k = keys[i]
@@ -580,7 +647,7 @@ def run_stream(nreq=10000, rate=50e3, seed=5, check=True, log=None):
     o = None
     expect = {}
     if check:
-        o = yk.Yaksa(oracle_path)
+        o = yk.Yaksa(ORACLE_LIB)
         o.init()
         for i in sorted(priv):
             k = keys[i]
@@ -604,9 +671,11 @@ def run_stream(nreq=10000, rate=50e3, seed=5, check=True, log=None):
         return bad
 
     total = float(sum(sizes[k] for k in keys))
+    checked_classes = sorted(set(keys[i][1] for i in chk))
     res = {"requests": nreq, "rate_per_s": rate, "packed_bytes": total,
-           "checked_requests": len(chk), "families": fams,
-           "size_classes": [STREAM_CLASSES[0], STREAM_CLASSES[-1]],
+           "checked_requests": len(chk), "checked_size_classes": len(checked_classes),
+           "largest_checked_bytes": max(checked_classes) if checked_classes else 0,
+           "families": fams, "size_classes": [STREAM_CLASSES[0], STREAM_CLASSES[-1]],
            "host_fraction": float(host_of.mean()),
            "arena_bytes": int(sum(arena.values()))}
     zero = np.zeros(nreq)
@@ -652,6 +721,9 @@ def run_stream(nreq=10000, rate=50e3, seed=5, check=True, log=None):
     res["server_over_plain"] = {
         "closed_loop_throughput": res["server"]["closed_loop"]["GBps"] / res["plain"]["closed_loop"]["GBps"],
         "open_loop_p99": res["server"]["open_loop"]["p99_us"] / res["plain"]["open_loop"]["p99_us"]}
+    if floor:
+        res["xface_floor"] = stream_xface_floor(torch, np, y, yk, keys, dir_of, specs, typed, total,
+                                                res["plain"]["closed_loop"]["GBps"])
     for k in used:
         y.type_free(types[k])
     if o:
@@ -661,60 +733,63 @@ def run_stream(nreq=10000, rate=50e3, seed=5, check=True, log=None):
     return res
 
 
-def main():
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
-    ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--cpu-seconds", type=float, default=5.0)
-    ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--suite", default=None,
-                    help="also run the hvector/hindexed/struct/reduction configs and write their "
-                         "JSON lines to this file")
-    ap.add_argument("--suite-only", default=None, help="comma-separated suite workloads")
-    ap.add_argument("--suite-scale", type=int, default=1,
-                    help="divide the suite's block/element counts (profiler captures)")
-    ap.add_argument("--stream", default=None,
-                    help="run only the mixed request stream (plain vs server) and write its JSON")
-    ap.add_argument("--stream-requests", type=int, default=10000)
-    ap.add_argument("--no-stream", action="store_true")
-    args = ap.parse_args()
-    if args.impl == "reference":
-        return run_reference(args)
-    if args.suite:
-        import torch
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        run_suite(args.suite, args.steps, args.cpu_seconds,
-                  only=args.suite_only.split(",") if args.suite_only else None, scale=args.suite_scale)
-        return
-    if args.stream:
-        import torch
-        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        r = run_stream(nreq=args.stream_requests, log=sys.stderr)
-        with open(args.stream, "w") as f:
-            f.write(json.dumps(r) + "\n")
-        print(json.dumps(r))
-        return
+def stream_xface_floor(torch, np, y, yk, keys, dir_of, specs, typed, total, plain_gbps):
+    """The halo x-face fifth of the stream alone, as plain 8-byte loads (packs) and
+    stores (unpacks) of its rows with the row-touch instrument, 16 requests per launch,
+    all launches back to back: a lower bound on the time of any path that serves the
+    stream, and so an upper bound on any path's capacity."""
+    reads, writes = [], []
+    arena = typed["halo"].data_ptr()     # the stream has finished with it: stores may land there
+    for i, k in enumerate(keys):
+        if k[0] != "halo":
+            continue
+        Z, Y, x0 = specs[k]["xface"]
+        (writes if dir_of[i] == 1 else reads).append(yk.Rows(arena + 4 * x0, Z, Y * 2048, Y, 2048, 8, 0))
+    torch.cuda.synchronize()
+    flush = ColdL2(torch)
+    stream = torch.cuda.current_stream()
+    sh = ctypes.c_void_p(stream.cuda_stream)
+    shp = ctypes.addressof(sh)
 
-    import numpy as np
-    import torch
-    import yaksa_gb300 as yk
+    def run():
+        for pats, w in ((reads, 0), (writes, 1)):
+            for j in range(0, len(pats), 16):
+                y.probe_rows(pats[j:j + 16], w, shp)
+    run()
+    t = event_time(torch, run, 3, flush, stat=min)
+    xbytes = float(sum(k[1] for k in keys if k[0] == "halo"))
+    del flush
+    cap = total / t / 1e9
+    return {"requests": len(reads) + len(writes), "packed_bytes": xbytes, "rows": int(xbytes // 8),
+            "touch_s": t, "capacity_bound_GBps": cap, "capacity_ratio_bound": cap / plain_gbps,
+            "note": "plain 8-byte loads/stores of the x-face fifth's rows alone (row-touch instrument, "
+                    "16 requests per launch); no path can serve the stream faster than this fifth's "
+                    "rows can be touched"}
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    if not os.path.exists(yk.LIB_PATH):
-        from yaksa_gb300 import build
-        build.build()
-    y = yk.Yaksa()
-    y.init()
+# ---------------------------------------------------------------------------
+# the headline: halo faces, plain path per face, batched graph as a second form
+# ---------------------------------------------------------------------------
+
+def face_rows(yk, base, name, n=N):
+    """Row-touch patterns covering exactly one face's typed bytes (16-byte runs for the
+    contiguous faces)."""
+    plane, row = n * n * 4, n * 4
+    if name[0] == "x":
+        return yk.Rows(base + (0 if name == "x-" else (n - 2) * 4), n, plane, n, row, 8, 0)
+    if name[0] == "y":
+        return yk.Rows(base + (0 if name == "y-" else (n - 2) * row), n, plane, 2 * row // 16, 16, 16, 0)
+    return yk.Rows(base + (0 if name == "z-" else (n - 2) * plane), 1, 0, 2 * plane // 16, 16, 16, 0)
+
+
+def capture(torch, fn):
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        fn()
+    return g
+
+
+def run_halo(args, y, yk, torch, np, world, rank, dist):
     faces = make_faces(y, yk)
     P = 2 * N * N * 4                      # packed bytes per face
     g = torch.Generator(device="cuda").manual_seed(1234 + rank)
@@ -722,46 +797,90 @@ def main():
     dst = torch.zeros_like(src)
     packed = [torch.empty(P, dtype=torch.uint8, device="cuda") for _ in faces]
     flush = ColdL2(torch)
-    stream = torch.cuda.current_stream()
-    sh = ctypes.c_void_p(stream.cuda_stream)
-    shp = ctypes.addressof(sh)
+    hbm, peak_kind = peaks()
 
-    # the step through the batched C-ABI: one launch packs all six faces, one unpacks them
+    def cur():
+        return torch.cuda.current_stream()
+
+    def pack_face(i, s):
+        h = ctypes.c_void_p(s.cuda_stream)      # alive for the call: the API reads *stream
+        y.pack_stream(src.data_ptr(), 1, faces[i][1], 0, packed[i].data_ptr(), P, ctypes.addressof(h))
+
+    def unpack_face(i, s):
+        h = ctypes.c_void_p(s.cuda_stream)
+        y.unpack_stream(packed[i].data_ptr(), P, dst.data_ptr(), 1, faces[i][1], 0, ctypes.addressof(h))
+
+    def on_stream(fn, s):
+        h = ctypes.c_void_p(s.cuda_stream)
+        return fn(ctypes.addressof(h))
+
+    # the launch-shape autotuner settles over the first calls of each shape class (a few
+    # timed candidates each): make those calls before capturing and timing anything
     pack_batch = y.batch_array([yk.pack_op(src.data_ptr(), 1, t, 0, pk.data_ptr(), P)
                                 for (name, t), pk in zip(faces, packed)])
     unpack_batch = y.batch_array([yk.unpack_op(pk.data_ptr(), P, dst.data_ptr(), 1, t, 0)
                                   for (name, t), pk in zip(faces, packed)])
-
-    # the launch-shape autotuner settles over the first calls of each shape class (a few
-    # timed candidates each): run those calls before capturing and timing anything
     for _ in range(TUNE_CALLS):
-        y.pup_batch_stream(pack_batch, shp)
-        y.pup_batch_stream(unpack_batch, shp)
-        for (name, t), pk in zip(faces, packed):
-            y.pack_stream(src.data_ptr(), 1, t, 0, pk.data_ptr(), P, shp)
-        for (name, t), pk in zip(faces, packed):
-            y.unpack_stream(pk.data_ptr(), P, dst.data_ptr(), 1, t, 0, shp)
+        on_stream(lambda p: y.pup_batch_stream(pack_batch, p), cur())
+        on_stream(lambda p: y.pup_batch_stream(unpack_batch, p), cur())
+        for i in range(len(faces)):
+            pack_face(i, cur())
+        for i in range(len(faces)):
+            unpack_face(i, cur())
     torch.cuda.synchronize()
 
-    # the exchange repeats with the same buffers every step: capture it once
+    # the plain step: one stream per face (the message to one neighbour), pack then
+    # unpack on it; the twelve calls captured once into a CUDA graph
+    face_streams = [torch.cuda.Stream() for _ in faces]
+
+    def plain_step_streams():
+        main = torch.cuda.current_stream()
+        for i, s in enumerate(face_streams):
+            s.wait_stream(main)
+            with torch.cuda.stream(s):
+                pack_face(i, s)
+                unpack_face(i, s)
+        for s in face_streams:
+            main.wait_stream(s)
+
+    def plain_step_one_stream():
+        for i in range(len(faces)):
+            pack_face(i, cur())
+        for i in range(len(faces)):
+            unpack_face(i, cur())
+
+    st0 = y.stats()
+    g_plain = capture(torch, plain_step_streams)
+    st1 = y.stats()
+    kernels_per_step = st1["launches"] - st0["launches"]          # counted when captured
+    copies_per_step = st1["memcpy_calls"] - st0["memcpy_calls"]   # contiguous faces
+    # per face and direction: one plain call captured alone
+    g_face, face_kind = {}, {}
+    for i, (name, _) in enumerate(faces):
+        for d, fn in (("pack", pack_face), ("unpack", unpack_face)):
+            l0 = y.stats()["launches"]
+            g_face[(name, d)] = capture(torch, lambda i=i, fn=fn: fn(i, cur()))
+            face_kind[(name, d)] = ("yk_regular_kernel" if y.stats()["launches"] > l0 else
+                                    "cudaMemcpyAsync (contiguous face)")
+    # the batched form: one launch per direction for all six faces, a library-captured graph
     graph, _ = y.graph_create([[yk.pack_op(src.data_ptr(), 1, t, 0, pk.data_ptr(), P)
                                 for (name, t), pk in zip(faces, packed)],
                                [yk.unpack_op(pk.data_ptr(), P, dst.data_ptr(), 1, t, 0)
                                 for (name, t), pk in zip(faces, packed)]])
+    g_pack_b, _ = y.graph_create([[yk.pack_op(src.data_ptr(), 1, t, 0, pk.data_ptr(), P)
+                                   for (name, t), pk in zip(faces, packed)]])
+    g_unpack_b, _ = y.graph_create([[yk.unpack_op(pk.data_ptr(), P, dst.data_ptr(), 1, t, 0)
+                                     for (name, t), pk in zip(faces, packed)]])
 
     def step_batched():
-        y.graph_launch(graph, shp)
+        on_stream(lambda p: y.graph_launch(graph, p), cur())
 
-    def step_batched_uncaptured():
-        y.pup_batch_stream(pack_batch, shp)
-        y.pup_batch_stream(unpack_batch, shp)
-
-    # the same step through the reference's API: one stream-ordered call per face
-    def step_plain():
-        for (name, t), pk in zip(faces, packed):
-            y.pack_stream(src.data_ptr(), 1, t, 0, pk.data_ptr(), P, shp)
-        for (name, t), pk in zip(faces, packed):
-            y.unpack_stream(pk.data_ptr(), P, dst.data_ptr(), 1, t, 0, shp)
+    for _ in range(args.warmup):
+        flush()
+        g_plain.replay()
+        flush()
+        step_batched()
+    torch.cuda.synchronize()
 
     def timed(fn, steps):
         tot = 0.0
@@ -775,48 +894,7 @@ def main():
             tot += e0.elapsed_time(e1) * 1e-3
         return tot
 
-    for _ in range(args.warmup):
-        flush()
-        step_batched()
-        flush()
-        step_plain()
-    torch.cuda.synchronize()
-
-    # per-launch durations of the dominant kernel (one batched launch per direction)
-    per = {"pack": [], "unpack": []}
-    for rep in range(5):
-        for d, arr in (("pack", pack_batch), ("unpack", unpack_batch)):
-            flush()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            y.pup_batch_stream(arr, shp)
-            e1.record()
-            e1.synchronize()
-            per[d].append(e0.elapsed_time(e1) * 1e-3)
-
-    # a reference point: PyTorch's own strided-copy kernels moving the same six faces
-    # (one copy per face and direction, the same cold L2)
-    s3, d3 = src.view(N, N, N), dst.view(N, N, N)
-    views = [s3[:, :, :2], s3[:, :, N - 2:], s3[:, :2, :], s3[:, N - 2:, :], s3[:2], s3[N - 2:]]
-    dviews = [d3[:, :, :2], d3[:, :, N - 2:], d3[:, :2, :], d3[:, N - 2:, :], d3[:2], d3[N - 2:]]
-    pk_views = [pk.view(torch.float32).view(v.shape) for pk, v in zip(packed, views)]
-    torch_t = {"pack": [], "unpack": []}
-    for rep in range(5):
-        for d in ("pack", "unpack"):
-            flush()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record()
-            for i in range(len(faces)):
-                if d == "pack":
-                    pk_views[i].copy_(views[i])
-                else:
-                    dviews[i].copy_(pk_views[i])
-            e1.record()
-            e1.synchronize()
-            torch_t[d].append(e0.elapsed_time(e1) * 1e-3)
-    torch_ref = {d: statistics.median(v) * 1e6 for d, v in torch_t.items()}
-
-    import tempfile
+    # the timed region: the plain step, graph replay
     clocks = Clocks(os.path.join(tempfile.gettempdir(), f"yk_clocks_{os.getpid()}.csv"))
     clocks.start()
     time.sleep(0.3)
@@ -825,42 +903,137 @@ def main():
         dist.barrier()
     torch.cuda.synchronize()
     wall0 = time.perf_counter()
-    tot = timed(step_batched, args.steps)
+    tot = timed(g_plain.replay, args.steps)
     torch.cuda.synchronize()
     if dist:
         dist.barrier()
     wall = time.perf_counter() - wall0
-    launches = y.stats()["launches"] - launches0
     clk = clocks.stop()
+    # the library counts launches when the calls are made (here: at capture), so the
+    # timed region's launches are the graph's kernel nodes times the steps
+    launches = kernels_per_step * args.steps
+    assert y.stats()["launches"] == launches0
     if dist:
         tt = torch.tensor([tot], device="cuda", dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         tot = tt.item()
-    tot_plain = timed(step_plain, args.steps)
-    tot_uncap = timed(step_batched_uncaptured, args.steps)
+    step_bytes = 2 * P * len(faces)       # packed bytes moved per step (pack + unpack)
+    ms = tot / args.steps * 1e3
+    value = step_bytes * world / (tot / args.steps) / 1e9
 
-    # correctness of the timed work: every face of dst equals the face of src
+    # the other forms of the same step
+    tot_one = timed(lambda: plain_step_one_stream(), args.steps)
+    tot_b = timed(step_batched, args.steps)
+    tot_unc = timed(lambda: (on_stream(lambda p: y.pup_batch_stream(pack_batch, p), cur()),
+                             on_stream(lambda p: y.pup_batch_stream(unpack_batch, p), cur())), args.steps)
+
+    # per face: each plain call alone (graph replay, cold L2)
+    reps = max(5, args.steps)
+    per_face = []
+    for (name, d), gg in g_face.items():
+        t = event_time(torch, gg.replay, reps, flush)
+        per_face.append({"face": name, "direction": d, "time_us": t * 1e6, "packed_GBps": P / t / 1e9,
+                         "hbm_frac": 2 * P / t / 1e9 / hbm, "launch": face_kind[(name, d)]})
+    # the batched launches alone (graph replay): the dominant kernel of the batched form
+    t_bp = event_time(torch, lambda: on_stream(lambda p: y.graph_launch(g_pack_b, p), cur()), reps, flush)
+    t_bu = event_time(torch, lambda: on_stream(lambda p: y.graph_launch(g_unpack_b, p), cur()), reps, flush)
+
+    # the floor: plain loads of every face's typed bytes in src (what a pack must read)
+    # and plain stores into every face of dst (what an unpack must write), one launch
+    # each, cold L2; the x-faces alone as well
+    def probe(base, which, write):
+        pats = [face_rows(yk, base, name) for name, _ in faces if name in which]
+        on_stream(lambda p: y.probe_rows(pats, write, p), cur())
+    fl = {}
+    for key, which in (("all", ("x-", "x+", "y-", "y+", "z-", "z+")), ("x", ("x-", "x+")), ("x1", ("x-",))):
+        fl[key] = (event_time(torch, lambda: probe(src.data_ptr(), which, 0), reps, flush),
+                   event_time(torch, lambda: probe(dst.data_ptr(), which, 1), reps, flush))
+    floor_us = (fl["all"][0] + fl["all"][1]) * 1e6
+
+    # the measured step ran last in dst order: refresh dst with one plain step, then check
+    dst.zero_()
+    torch.cuda.synchronize()
+    g_plain.replay()
+    torch.cuda.synchronize()
+
     def faces_equal(a, b):
         s3, d3 = a.view(N, N, N), b.view(N, N, N)
         return (torch.equal(s3[:, :, :2], d3[:, :, :2]) and torch.equal(s3[:, :, -2:], d3[:, :, -2:])
                 and torch.equal(s3[:, :2, :], d3[:, :2, :]) and torch.equal(s3[:, -2:, :], d3[:, -2:, :])
                 and torch.equal(s3[:2], d3[:2]) and torch.equal(s3[-2:], d3[-2:]))
     ok = faces_equal(src, dst)
+    # and the packed faces byte for byte against the oracle on the host
+    o = yk.Yaksa(ensure_oracle())
+    o.init()
+    ofaces = make_faces(o, yk)
+    src_h = src.cpu().numpy()
+    for (name, t), pk in zip(ofaces, packed):
+        ob = np.zeros(P, dtype=np.uint8)
+        o.pack(src_h.ctypes.data, 1, t, 0, ob.ctypes.data, P)
+        ok = ok and np.array_equal(pk.cpu().numpy(), ob)
+    for _, t in ofaces:
+        o.type_free(t)
+    o.finalize()
 
-    step_bytes = 2 * P * len(faces)       # packed bytes moved per step (pack + unpack)
-    ms = tot / args.steps * 1e3
-    value = step_bytes * world / (tot / args.steps) / 1e9
-    plain_value = step_bytes * world / (tot_plain / args.steps) / 1e9
-    hbm, peak_kind = peaks()
-    # dominant kernel: yk_batch_regular_kernel; algorithmic bytes = 2 per packed byte per launch
-    alg = 2 * P * len(faces)
-    # DRAM traffic of the same launches from one ncu capture on a 384^3 grid
-    # (dram__bytes_read.sum + dram__bytes_write.sum, pack 41.81 MB, unpack 16.14 MB),
-    # scaled by the packed bytes to this grid
-    traffic = (41.814e6 + 16.137e6) / 2 * (N / 384) ** 2
-    med = {d: statistics.median(v) for d, v in per.items()}
-    mean_launch = (med["pack"] + med["unpack"]) / 2
-    achieved = alg / mean_launch / 1e9
+    # roofline of the dominant kernel of the timed step.  The plain step is twelve launches
+    # of yk_regular_kernel; the x-face launches (8-byte units, one 8-byte run per 2 KiB
+    # grid row) take the longest.  Each launch's duration is that call alone (one-node
+    # graph, CUDA events, cold L2): timing events captured inside the step's graph slow
+    # the step itself, so they are not used.  Each launch moves 2 bytes per packed byte.
+    alg = 2 * P
+    dur = {(f["face"], f["direction"]): f["time_us"] * 1e-6 for f in per_face}
+    xkeys = [k for k in dur if k[0][0] == "x"]
+    xmean = statistics.mean(dur[k] for k in xkeys)
+    share = sum(dur[k] for k in xkeys) / sum(dur.values())
+    traffic = ncu_traffic("yk_regular_kernel_halo_xface")
+    tr_launch = statistics.mean(traffic.values()) if traffic else None
+    xfloor = (fl["x1"][0] + fl["x1"][1]) / 2        # one x-face alone, mean of the directions
+    roof = {"bound": "hbm", "achieved": alg / xmean / 1e9, "peak": hbm, "unit": "GB/s",
+            "frac": alg / xmean / 1e9 / hbm, "peak_source": peak_kind,
+            "traffic": tr_launch, "traffic_frac": (tr_launch / xmean / 1e9 / hbm) if tr_launch else None,
+            "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum per x-face launch from one ncu "
+                            "capture (mean of pack and unpack): each 8-byte row costs a 128-byte DRAM fetch",
+            "kernel": "yk_regular_kernel<8,*,1> (the x-face launches of the plain step: 4 of its "
+                      f"{kernels_per_step} kernel launches, {100 * share:.0f}% of their summed duration "
+                      "alone)",
+            "duration_source": "each launch alone (one-node graph replay, CUDA events, cold L2)",
+            "algorithmic_bytes_per_launch": alg,
+            "launch_us": {d + f: dur[(f, d)] * 1e6 for (f, d) in sorted(dur)},
+            "launch_us_mean": xmean * 1e6,
+            "floor_us": xfloor * 1e6, "frac_vs_floor": xfloor / xmean,
+            "floor_note": "row-touch instrument: plain 8-byte loads (pack) and stores (unpack) over one "
+                          "x-face's 262,144 rows alone, cold L2, mean of the two directions; what any "
+                          "kernel moving that face must at least spend",
+            "floor_both_xfaces_us": {"loads": fl["x"][0] * 1e6, "stores": fl["x"][1] * 1e6},
+            "step": {"achieved": step_bytes / (ms * 1e-3) / 1e9, "frac": step_bytes / (ms * 1e-3) / 1e9 / hbm,
+                     "floor_us": floor_us, "step_us": ms * 1e3, "frac_vs_floor": floor_us / (ms * 1e3),
+                     "note": "the whole step: all six faces' bytes over its time; floor = plain loads of "
+                             "every face's typed bytes plus plain stores of them, one launch each"}}
+    btraffic = {k: v * (N / 384) ** 2 for k, v in ncu_traffic("yk_batch_regular_kernel_halo3d").items()}
+    batched = {"value": step_bytes * world / (tot_b / args.steps) / 1e9, "unit": "GB/s",
+               "ms_per_step": tot_b / args.steps * 1e3,
+               "note": "yaksa_gb300_graph_create of two batches (one launch per direction for all six "
+                       "faces), graph replay",
+               "roofline": {"bound": "hbm", "kernel": "yk_batch_regular_kernel (6 faces per launch)",
+                            "launch_us": {"pack": t_bp * 1e6, "unpack": t_bu * 1e6},
+                            "achieved": 2 * P * len(faces) / ((t_bp + t_bu) / 2) / 1e9,
+                            "frac": 2 * P * len(faces) / ((t_bp + t_bu) / 2) / 1e9 / hbm,
+                            "peak": hbm, "unit": "GB/s",
+                            "traffic": (statistics.mean(btraffic.values()) if btraffic else None),
+                            "floor_us": floor_us,
+                            "frac_vs_floor": floor_us / ((t_bp + t_bu) * 1e6),
+                            "note": "launch_us: each batched launch alone from a library-captured graph "
+                                    "of that launch, CUDA events, cold L2"}}
+    res = dict(value=value, ms=ms, wall=wall, clk=clk, launches=launches, ok=ok, roofline=roof,
+               per_face=per_face, batched=batched,
+               plain_one_stream={"value": step_bytes * world / (tot_one / args.steps) / 1e9, "unit": "GB/s",
+                                 "ms_per_step": tot_one / args.steps * 1e3,
+                                 "note": "the twelve calls on one stream, uncaptured (host work per call "
+                                         "inside the timed span)"},
+               batched_uncaptured={"value": step_bytes * world / (tot_unc / args.steps) / 1e9, "unit": "GB/s",
+                                   "ms_per_step": tot_unc / args.steps * 1e3,
+                                   "note": "yaksa_gb300_pup_batch_stream per direction, host planning "
+                                           "inside the timed span"})
 
     # e2e through the reference's C-ABI (yaksa_ipack / yaksa_iunpack + yaksa_request_wait):
     # the exchange through host memory, as a halo exchange over host buffers runs it.
@@ -872,10 +1045,14 @@ def main():
     # depend on the faces sent in the same step; here the receive buffers hold the same
     # faces, packed once before timing, so the result is checkable.  All twelve requests
     # are issued before the first wait, and the two directions of the link overlap.
-    # "e2e_serial" is the same step with the unpacks reading the send buffers, after
-    # the packs have completed.
+    y.graph_free(graph)
+    y.graph_free(g_pack_b)
+    y.graph_free(g_unpack_b)
     send = [torch.empty(P, dtype=torch.uint8).pin_memory() for _ in faces]
     recv = [torch.empty(P, dtype=torch.uint8).pin_memory() for _ in faces]
+
+    res["kernels_per_step"] = kernels_per_step
+    res["copies_per_step"] = copies_per_step
 
     def e2e_run(gsrc, gdst, steps, overlap):
         for (name, t), pk in zip(faces, recv):
@@ -904,65 +1081,115 @@ def main():
         dst.zero_()
         torch.cuda.synchronize()
         results[overlap] = e2e_run(src, dst, e_steps, overlap)
-        ok = ok and faces_equal(src, dst)
-    e2e = {"value": step_bytes * world / results[True] / 1e9, "unit": "GB/s",
-           "h2d_bytes_per_step": P * len(faces), "d2h_bytes_per_step": P * len(faces),
-           "mode": "per face yaksa_ipack (device grid -> pinned host send buffer) and yaksa_iunpack "
-                   "(pinned host receive buffer -> device grid), all twelve issued, then "
-                   "yaksa_request_wait on each; kernels access the host buffers in place over "
-                   "NVLink-C2C"}
-    e2e_serial = {"value": step_bytes * world / results[False] / 1e9, "unit": "GB/s",
-                  "note": "the six packs completed before the six unpacks, which read the send buffers"}
-    # the same with the grids themselves in pinned host memory (every byte over the link)
+        res["ok"] = res["ok"] and faces_equal(src, dst)
+    res["e2e"] = {"value": step_bytes * world / results[True] / 1e9, "unit": "GB/s",
+                  "h2d_bytes_per_step": P * len(faces), "d2h_bytes_per_step": P * len(faces),
+                  "mode": "per face yaksa_ipack (device grid -> pinned host send buffer) and yaksa_iunpack "
+                          "(pinned host receive buffer -> device grid), all twelve issued, then "
+                          "yaksa_request_wait on each; kernels access the host buffers in place over "
+                          "NVLink-C2C"}
+    res["e2e_serial"] = {"value": step_bytes * world / results[False] / 1e9, "unit": "GB/s",
+                         "note": "the six packs completed before the six unpacks, which read the send buffers"}
     hsrc = src.cpu().pin_memory()
     hdst = torch.zeros_like(hsrc).pin_memory()
     e2e_h = e2e_run(hsrc, hdst, e_steps, True)
-    ok = ok and faces_equal(hsrc, hdst)
-    e2e_host = {"value": step_bytes * world / e2e_h / 1e9, "unit": "GB/s",
-                "note": "grids and packed buffers all in pinned host memory"}
+    res["ok"] = res["ok"] and faces_equal(hsrc, hdst)
+    res["e2e_host_grid"] = {"value": step_bytes * world / e2e_h / 1e9, "unit": "GB/s",
+                            "note": "grids and packed buffers all in pinned host memory"}
+    for _, t in faces:
+        y.type_free(t)
+    del src, dst, packed, flush, hsrc, hdst, send, recv, g_plain, g_face
+    torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    return res
 
-    line = {"metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": world, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-suite", action="store_true", help="skip the per-config records")
+    ap.add_argument("--suite", default=None,
+                    help="run only the per-config records and write their JSON lines to this file")
+    ap.add_argument("--suite-only", default=None, help="comma-separated suite workloads")
+    ap.add_argument("--suite-scale", type=int, default=1,
+                    help="divide the suite's block/element counts (profiler captures)")
+    ap.add_argument("--stream", default=None,
+                    help="run only the mixed request stream (plain vs server) and write its JSON")
+    ap.add_argument("--stream-requests", type=int, default=10000)
+    ap.add_argument("--no-stream", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.suite:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        lines = run_suite(args.steps, only=args.suite_only.split(",") if args.suite_only else None,
+                          scale=args.suite_scale, log=sys.stderr)
+        with open(args.suite, "w") as f:
+            for l in lines:
+                f.write(json.dumps(l) + "\n")
+        return
+    if args.stream:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        r = run_stream(nreq=args.stream_requests, log=sys.stderr)
+        with open(args.stream, "w") as f:
+            f.write(json.dumps(r) + "\n")
+        print(json.dumps(r))
+        return
+
+    import numpy as np
+    import torch
+    import yaksa_gb300 as yk
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    if not os.path.exists(yk.LIB_PATH):
+        from yaksa_gb300 import build
+        build.build()
+    y = yk.Yaksa()
+    y.init()
+    h = run_halo(args, y, yk, torch, np, world, rank, dist)
+    line = {"metric": METRIC, "value": h["value"], "unit": "GB/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": h["ms"], "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded uniform [-1,1))",
             "config": {"workload": WORKLOAD,
-                       "path": "batched C-ABI (one launch per direction) captured once as a CUDA "
-                               "graph and replayed per step",
+                       "path": "plain: yaksa_pack_stream + yaksa_unpack_stream per face, each face on its own "
+                               "stream, the twelve calls captured once into a CUDA graph and replayed per step",
                        "parallelism": f"replicas x{world}",
                        "l2": "flushed between steps outside the event-timed span: 512 MiB written, then "
                              "512 MiB read so that no dirty flush lines remain"},
-            "bit_exact": bool(ok),
-            "plain_path": {"value": plain_value, "unit": "GB/s",
-                           "ms_per_step": tot_plain / args.steps * 1e3,
-                           "note": "one yaksa_pack_stream/yaksa_unpack_stream launch per face"},
-            "batched_uncaptured": {"value": step_bytes * world / (tot_uncap / args.steps) / 1e9,
-                                   "unit": "GB/s", "ms_per_step": tot_uncap / args.steps * 1e3,
-                                   "note": "yaksa_gb300_pup_batch_stream per direction, host "
-                                           "planning inside the timed span"},
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
-                         "frac": achieved / hbm, "traffic": traffic,
-                         "traffic_source": "ncu capture of the same kernel on a 384^3 grid, "
-                                           "scaled by packed bytes (profiles/yk_batch_regular_kernel_halo3d.md)",
-                         "kernel": "yk_batch_regular_kernel (6 faces per launch; mean of pack and unpack)",
-                         "peak_source": peak_kind,
-                         "launch_us": {d: v * 1e6 for d, v in med.items()},
-                         "algorithmic_bytes_per_launch": alg},
-            "gpu_launches": launches,
-            "clocks": clk,
-            "e2e": e2e,
-            "e2e_serial": e2e_serial,
-            "e2e_host_grid": e2e_host,
-            "torch_strided_copy": {"pack_us": torch_ref["pack"], "unpack_us": torch_ref["unpack"],
-                                   "note": "PyTorch copy_ of the same six face views, one kernel per "
-                                           "face and direction, cold L2 (a reference point for the "
-                                           "launch_us of the roofline kernel)"},
-            "wall_s": wall}
+            "bit_exact": bool(h["ok"]),
+            "roofline": h["roofline"],
+            "per_face": h["per_face"],
+            "batched_graph": h["batched"],
+            "plain_one_stream": h["plain_one_stream"],
+            "batched_uncaptured": h["batched_uncaptured"],
+            "gpu_launches": h["launches"],
+            "clocks": h["clk"],
+            "e2e": h["e2e"],
+            "e2e_serial": h["e2e_serial"],
+            "e2e_host_grid": h["e2e_host_grid"],
+            "wall_s": h["wall"]}
+    if rank == 0 and not args.no_suite:
+        lines = run_suite(args.steps)
+        line["suite"] = lines
+        line["suite_bit_exact"] = all(l["bit_exact"] for l in lines)
     if not args.no_stream:
         # the metric's second half: batched (persistent server) vs plain p50/p99 on the
-        # mixed request stream; the grids of the halo step are released first
-        y.graph_free(graph)
-        torch.cuda.synchronize()
-        del src, dst, packed, flush, hsrc, hdst, send, recv
-        torch.cuda.empty_cache()
+        # mixed request stream
         r = run_stream(nreq=args.stream_requests, check=True)
         line["stream"] = {
             "workload": f"{r['requests']} pack/unpack requests, Poisson {r['rate_per_s']:.0f}/s, "
@@ -983,15 +1210,15 @@ def main():
                         "classes": "small <= 64 KiB < medium <= 4 MiB < large"},
             "capacity_ratio": r["server_over_plain"]["closed_loop_throughput"],
             "p99_ratio": r["server_over_plain"]["open_loop_p99"],
+            "xface_floor": r.get("xface_floor"),
             "bit_exact": r["plain"]["bit_exact"] and r["server"]["bit_exact"],
             "checked_requests": r["checked_requests"],
+            "checked_size_classes": r["checked_size_classes"],
+            "largest_checked_bytes": r["largest_checked_bytes"],
             "note": "p50/p99 from arrival to completion seen by the serving loop; capacity = all "
                     "requests arriving at once; batched = persistent-kernel server"}
     if rank == 0 and not args.no_cpu:
-        oracle_path = os.path.join(ROOT, "oracle", "_ref", "liboracle_yaksa.so")
-        if not os.path.exists(oracle_path):
-            subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle")], check=True)
-        b = cpu_baseline(oracle_path, args.cpu_seconds, 1)
+        b = cpu_halo(args.cpu_seconds, 1)
         line["cpu_baseline"] = {k: b[k] for k in ("value", "unit", "cores", "kind", "cpu", "sample")}
         line["cpu_baseline"]["faces_equal"] = bool(b["ok"])
     if rank == 0:

@@ -92,10 +92,17 @@ int yaksa_gb300_server_destroy(yaksa_gb300_server_t server);
  * yaksa_pack_stream/yaksa_unpack_stream; the type's descriptor tables are copied into
  * a static 8 MiB device array on *stream (NULL: the legacy default stream) just before
  * the kernel; the call returns once both are enqueued and sets op->actual.
- *   - The first call on a device resolves that array's address (and may load the
- *     library's module): make it before any stream capture begins.  The first call
- *     for a type builds the type's host-side tables on the host heap, kept with the
- *     type until yaksa_type_free.
+ *   - Stream: the legacy default stream (NULL) waits for all work on blocking streams
+ *     and blocking streams wait for it.  Beside a resident kernel that runs on a
+ *     blocking stream, pass a stream created with cudaStreamNonBlocking, or the table
+ *     copy and the kernel wait for the resident kernel to end.
+ *   - First calls: the first pack/unpack of the process (through any entry point)
+ *     creates the library's own non-blocking streams; the first call on a device
+ *     resolves the array's address (and may load the library's module); make these
+ *     calls before any stream capture begins.  The first call for a type builds the
+ *     type's host-side tables on the host heap, kept with the type until
+ *     yaksa_type_free.  None of these allocates device memory.
+ *   - kind other than 0 or 1 is refused with YAKSA_ERR__INTERNAL.
  *   - Types whose tables exceed 8 MiB (about 500,000 hindexed blocks) are refused
  *     with YAKSA_ERR__NOT_SUPPORTED and a message on stderr; so are buffers the GPU
  *     cannot address (staging would need device memory).
@@ -132,6 +139,33 @@ int yaksa_gb300_shard(yaksa_type_t type, uintptr_t count, int rank, int nranks,
  * allocations fail as if memory were exhausted, without calling the allocator, so that
  * error paths are exercised with no GPU fault.  0 clears it. */
 int yaksa_gb300_debug_fail_alloc(int n);
+
+/* Measurement instrument (no counterpart in the reference): touch the typed-side bytes
+ * of up to 16 strided layouts in one launch, with plain loads (write = 0) or plain
+ * stores of zeros (write = 1) and nothing else.  Pattern k is n1 x n0 runs of `run`
+ * bytes (a multiple of 4) at base + i1 * s1 + i0 * s0.  The bench times it over the
+ * addresses of a pack or unpack to measure the floor that DRAM row accesses set for
+ * any kernel moving those bytes.  Stores overwrite the runs: use scratch buffers. */
+typedef struct {
+    void *base;
+    uint64_t n1;
+    int64_t s1;
+    uint64_t n0;
+    int64_t s0;
+    uint32_t run;
+    uint32_t pad;
+} yaksa_gb300_rows_t;
+int yaksa_gb300_probe_rows(const yaksa_gb300_rows_t * pats, int npats, int write, void *stream);
+
+/* Test hook (no counterpart in the reference): the TMA forms of the REPLACE kernels for
+ * regular nests (cp.async.bulk.tensor over the typed side).  mode 0 never uses them, 1
+ * lets the launch-shape autotuner choose them per shape class where they are faster
+ * (the default; YAKSA_GB300_TMA=0/1/2 in the environment sets the initial mode), 2 uses
+ * them wherever one exists.  Results are identical in every mode.
+ * yaksa_gb300_debug_tma_stats reports the TMA launches so far and the TMA waits that ran
+ * out (always 0 in correct operation). */
+int yaksa_gb300_debug_tma(int mode);
+int yaksa_gb300_debug_tma_stats(unsigned long long *launches, unsigned int *failures);
 
 /* Runtime counters since load: kernel launches, calls served in place (device or
  * GPU-addressable host memory), calls that staged host data through device memory,

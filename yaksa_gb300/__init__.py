@@ -112,6 +112,13 @@ class PupOp(ctypes.Structure):
                 ("actual", _up)]
 
 
+class Rows(ctypes.Structure):
+    """yaksa_gb300_rows_t (include/yaksa_gb300.h): n1 x n0 runs of `run` bytes at
+    base + i1 * s1 + i0 * s0, for the row-touch measurement instrument."""
+    _fields_ = [("base", _vp), ("n1", _u64), ("s1", ctypes.c_int64), ("n0", _u64),
+                ("s0", ctypes.c_int64), ("run", ctypes.c_uint32), ("pad", ctypes.c_uint32)]
+
+
 def pack_op(inbuf, count, t, offset, outbuf, maxbytes, op=10):
     return PupOp(0, 0, inbuf, outbuf, count, t, offset, maxbytes, op, 0)
 
@@ -170,6 +177,7 @@ def load_library(path):
                                                          ctypes.POINTER(ctypes.c_uint32)]),
                            ("yaksa_gb300_server_destroy", [_vp]),
                            ("yaksa_gb300_pup_noalloc", [ctypes.POINTER(PupOp), _vp]),
+                           ("yaksa_gb300_probe_rows", [ctypes.POINTER(Rows), ctypes.c_int, ctypes.c_int, _vp]),
                            ("yaksa_gb300_serve_trace", [ctypes.POINTER(PupOp), ctypes.POINTER(ctypes.c_double),
                                                         ctypes.c_int, ctypes.c_int, _vp, _vp,
                                                         ctypes.POINTER(ctypes.c_double),
@@ -476,6 +484,13 @@ class Yaksa:
         """yaksa_gb300_pup_noalloc: one request through the static descriptor scratch;
         returns the YAKSA_* code (0 on success) and sets op.actual."""
         return self.lib.yaksa_gb300_pup_noalloc(ctypes.byref(op), stream_ptr)
+
+    def probe_rows(self, rows, write, stream_ptr=None):
+        """yaksa_gb300_probe_rows: touch the runs of up to 16 Rows patterns in one launch
+        (loads, or stores of zeros when `write`)."""
+        arr = (Rows * len(rows))(*rows)
+        self._chk("yaksa_gb300_probe_rows", self.lib.yaksa_gb300_probe_rows(arr, len(rows), int(write),
+                                                                            stream_ptr))
 
     def graph_launch(self, g, stream_ptr=None):
         self._chk("yaksa_gb300_graph_launch", self.lib.yaksa_gb300_graph_launch(g, stream_ptr))

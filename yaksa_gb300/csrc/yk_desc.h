@@ -156,6 +156,11 @@ typedef struct {
                                          * apart); lane k's counter c means its next item
                                          * is c * YK_SRV_LANES + k */
     volatile uint32_t *status;  /* [0] idle exits, [1] stop exits, [2] rejected items */
+    const uint64_t *req_nitems; /* per request slot: its item count (host-mapped, written
+                                 * by the host before the items are published) */
+    unsigned long long *cq;     /* completion queue (host-mapped, qr entries): slot + 1 of
+                                 * each finished request, in finishing order; 0 = empty */
+    unsigned long long *cq_tail;        /* device memory: next completion queue position */
     uint32_t qi, qr;            /* ring sizes */
     uint32_t max_idle_spins;    /* bounded wait for new items */
     uint32_t pad;
@@ -180,6 +185,11 @@ int yk_cuda_launch_pup_cfg(const yk_launch * l, void *stream, int units_per_thre
 /* Ordered unpack for types whose targets may overlap: sorted-block owner-computes
  * kernel when the descriptor allows it, otherwise a single-warp ordered kernel. */
 int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blocks, void *stream);
+
+/* TMA form of a REPLACE launch over a regular nest (yk_tma.cu): 1 when it exists; the
+ * launch returns -1 when it does not, else a cudaError_t value. */
+int yk_cuda_tma_ok(const yk_launch * l);
+int yk_cuda_launch_tma(const yk_launch * l, void *stream, int ctas_per_sm);
 
 /* SM count of the current device (cached). */
 int yk_cuda_num_sms(void);

@@ -1323,6 +1323,21 @@ __device__ __forceinline__ uint64_t yk_ld_sys(const void *p)
     return v;
 }
 
+/* An item of request slot `slot` is finished: count it into the request's completion
+ * word; the CTA that finishes the request's last item appends slot + 1 to the completion
+ * queue, so the host learns of completions without scanning every request in flight.
+ * The item's bytes are made visible to the host first. */
+__device__ __forceinline__ void yk_srv_item_done(const yk_server_args & A, uint32_t slot)
+{
+    __threadfence_system();
+    const unsigned long long old = atomicAdd_system(&A.req_done[slot], 1ull);
+    if (old + 1 == yk_ld_sys(A.req_nitems + slot)) {
+        const unsigned long long pos = atomicAdd(A.cq_tail, 1ull);
+        asm volatile ("st.release.sys.global.u64 [%0], %1;"
+                      :: "l"(A.cq + pos % A.qr), "l"((unsigned long long) slot + 1ull) : "memory");
+    }
+}
+
 /* a record the GPU can act on: a known kind, a sane unit and an ordered range */
 __device__ __forceinline__ bool yk_item_ok(const yk_item & it, const yk_launch & L)
 {
@@ -1439,10 +1454,8 @@ yk_server_kernel(const __grid_constant__ yk_server_args A)
                 /* counted for its request only when the item record itself was current;
                  * otherwise the request stays incomplete and the host's bounded wait
                  * reports the error */
-                if (s_it.seq == s_item) {
-                    __threadfence_system();
-                    atomicAdd_system(&A.req_done[s_it.req % A.qr], 1ull);
-                }
+                if (s_it.seq == s_item)
+                    yk_srv_item_done(A, s_it.req % A.qr);
             }
             __syncthreads();
             continue;
@@ -1499,11 +1512,8 @@ yk_server_kernel(const __grid_constant__ yk_server_args A)
                 break;
         }
         __syncthreads();
-        if (threadIdx.x == 0) {
-            /* the item's bytes become visible before its request's count moves */
-            __threadfence_system();
-            atomicAdd_system(&A.req_done[it.req % A.qr], 1ull);
-        }
+        if (threadIdx.x == 0)
+            yk_srv_item_done(A, it.req % A.qr);   /* the item's bytes first, then its count */
     }
 }
 

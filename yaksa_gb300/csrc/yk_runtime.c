@@ -47,6 +47,9 @@ static struct {
     int device;
     int pageable_access;        /* the GPU reads/writes pageable host memory (ATS) */
     int host_ptr_ok;            /* registered host memory uses the host address */
+    int host_direct;            /* 0: host memory is never addressed in place, always
+                                 * staged (YAKSA_GB300_HOST_DIRECT=0) */
+    int tma_mode;               /* TMA forms: 0 off, 1 autotuner candidates, 2 forced */
     /* library streams: requests that are not stream-ordered go round robin over
      * these, so independent requests (whose order the API leaves open) overlap on the
      * GPU; streams[0] is also the default stream of graph replays */
@@ -61,7 +64,7 @@ static struct {
     size_t nev, capev;
     /* counters (yaksa_gb300_stats) */
     uint64_t launches, staged_calls, direct_calls, memcpy_calls;
-} R = { .mu = PTHREAD_MUTEX_INITIALIZER };
+} R = { .mu = PTHREAD_MUTEX_INITIALIZER, .tma_mode = -1 };
 
 /* a library stream for a request that is not stream-ordered (round robin) */
 static cudaStream_t lib_stream(void)
@@ -112,6 +115,12 @@ static int runtime_ready(void)
             const char *l2 = getenv("YAKSA_GB300_L2_FETCH_BYTES");
             if (l2 && atoi(l2) > 0)
                 cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t) atoi(l2));
+            if (R.tma_mode < 0) {
+                const char *tm = getenv("YAKSA_GB300_TMA");
+                R.tma_mode = tm && tm[0] >= '0' && tm[0] <= '2' ? tm[0] - '0' : 0;
+            }
+            const char *hd = getenv("YAKSA_GB300_HOST_DIRECT");
+            R.host_direct = !(hd && hd[0] == '0');
             const char *ns = getenv("YAKSA_GB300_LIB_STREAMS");
             R.nstreams = ns ? atoi(ns) : 4;
             if (R.nstreams < 1 || R.nstreams > YK_LIB_STREAMS)
@@ -132,9 +141,12 @@ static int runtime_ready(void)
     return rc;
 }
 
+static void stage_finalize(void);
+
 void yk_runtime_finalize(void)
 {
     yk_tune_reset();
+    stage_finalize();
     pthread_mutex_lock(&R.mu);
     if (R.ready) {
         for (int k = 0; k < R.nstreams; k++)
@@ -305,7 +317,7 @@ static char *device_alias(const char *base, const char *probe, int host_hint, in
      * alike through the caller's pointer, so no per-call attribute query is needed
      * (the reference queries both pointers of every request,
      * src/backend/src/yaksur_pup.c:31-58) */
-    if (R.pageable_access && R.host_ptr_ok)
+    if (R.host_direct && R.pageable_access && R.host_ptr_ok)
         return (char *) base;
     struct cudaPointerAttributes a;
     memset(&a, 0, sizeof(a));
@@ -320,11 +332,15 @@ static char *device_alias(const char *base, const char *probe, int host_hint, in
         case cudaMemoryTypeManaged:
             return (char *) base;
         case cudaMemoryTypeHost:
+            if (!R.host_direct) {
+                *staged = 1;
+                return NULL;
+            }
             if (a.devicePointer)
                 return (char *) base + ((const char *) a.devicePointer - probe);
             return (char *) base;
         default:
-            if (R.pageable_access)
+            if (R.pageable_access && R.host_direct)
                 return (char *) base;
             *staged = 1;
             return NULL;
@@ -403,6 +419,21 @@ static int plan(int dir, const void *packed_in, void *packed_out, char *typed, u
     p->dpacked = device_alias(p->packed, p->packed, host_hint, &st_p);
     p->staged = st_t | (st_p << 1);
     return YAKSA_SUCCESS;
+}
+
+/* plan() for one yaksa_gb300_pup_t record: kind 0 packs, 1 unpacks, anything else is
+ * refused (a corrupt record must not swap the buffer roles) */
+static int plan_op(const yaksa_gb300_pup_t * o, yk_type * t, yaksa_info_t info, yk_plan * p)
+{
+    if (o->kind == 0)
+        return plan(0, NULL, o->outbuf, (char *) o->inbuf, o->count, t, o->offset, o->maxbytes,
+                    info, o->op, p);
+    if (o->kind == 1)
+        return plan(1, o->inbuf, NULL, (char *) o->outbuf, o->count, t, o->offset, o->maxbytes,
+                    info, o->op, p);
+    fprintf(stderr, "yaksa-gb300: request kind %d is neither pack (0) nor unpack (1)\n",
+            (int) o->kind);
+    return YAKSA_ERR__INTERNAL;
 }
 
 /* ------------------------------------------------------------------------- */
@@ -541,19 +572,42 @@ static int launch_prepared(const yk_plan * p, const yk_launch * L, int kind, int
     __atomic_add_fetch(&R.launches, 1, __ATOMIC_RELAXED);
     if (kind == YK_X_ORDERED)
         return cuda_err((cudaError_t) yk_cuda_launch_unpack_ordered(L, sorted, s), "kernel launch");
-    if (kind == YK_X_BYTES && runs_pack_ok(L))
+    const int runs = kind == YK_X_BYTES && runs_pack_ok(L);
+    const uint64_t units = L->nbytes / (uint64_t) L->vec;
+    /* a TMA form competes as a candidate of the autotuner (or is forced by the test hook) */
+    const int tma = kind == YK_X_BYTES && !L->hidx && R.tma_mode &&
+        (R.tma_mode == 2 || (tune && units >= yk_tune_min_units())) && yk_cuda_tma_ok(L);
+    if (tma && R.tma_mode == 2) {
+        int e = yk_cuda_launch_tma(L, s, 0);
+        if (e != -1)
+            return cuda_err((cudaError_t) e, "kernel launch");
+    }
+    if (runs && !tma)
         return cuda_err((cudaError_t) yk_cuda_launch_runs_pack(L, (uint32_t) L->desc.run, s),
                         "kernel launch");
-    yk_tune_cfg cfg = { 0, 0 };
+    yk_tune_cfg cfg = { 0, 0, runs ? YK_VARIANT_RUNS : YK_VARIANT_BYTES };
     int probe = -1;
     if (tune && kind == YK_X_BYTES && !L->hidx) {
-        uint64_t units = L->nbytes / (uint64_t) L->vec;
-        probe = yk_tune_begin(yk_tune_key(YK_TUNE_SINGLE, L->regular, L->vec, L->dir, L->use64,
-                                          units), YK_TUNE_SINGLE, units, s, &cfg);
+        const int fam = runs ? YK_TUNE_RUNS_TMA : tma ? YK_TUNE_SINGLE_TMA : YK_TUNE_SINGLE;
+        probe = yk_tune_begin(yk_tune_key(fam, L->regular, L->vec, L->dir, L->use64, units), fam,
+                              units, s, &cfg);
     }
-    int e = yk_cuda_launch_pup_cfg(L, s, cfg.units_per_thread, cfg.ctas_per_sm);
+    int e = cfg.variant == YK_VARIANT_TMA && tma ? yk_cuda_launch_tma(L, s, cfg.ctas_per_sm) : -1;
+    if (e == -1)        /* not the TMA form, or its tensor map could not be encoded */
+        e = runs && cfg.variant != YK_VARIANT_BYTES ?
+            yk_cuda_launch_runs_pack(L, (uint32_t) L->desc.run, s) :
+            yk_cuda_launch_pup_cfg(L, s, cfg.units_per_thread, cfg.ctas_per_sm);
     yk_tune_end(probe, s);
     return cuda_err((cudaError_t) e, "kernel launch");
+}
+
+/* TMA forms: 0 never, 1 as autotuner candidates (default), 2 always where one exists */
+int yaksa_gb300_debug_tma(int mode)
+{
+    if (mode < 0 || mode > 2)
+        return YAKSA_ERR__INTERNAL;
+    __atomic_store_n(&R.tma_mode, mode, __ATOMIC_RELAXED);
+    return YAKSA_SUCCESS;
 }
 
 static int enqueue(const yk_plan * p, char *typed, char *packed, cudaStream_t s)
@@ -566,15 +620,196 @@ static int enqueue(const yk_plan * p, char *typed, char *packed, cudaStream_t s)
     return launch_prepared(p, &L, kind, sorted, s, 1);
 }
 
-/* The GPU cannot address a buffer: copy the touched span to device memory from the
- * stream-ordered pool, run, copy back; completes before returning. */
-static int run_staged(const yk_plan * p, cudaStream_t s)
+/* ------------------------------------------------------------------------- */
+/* staging: buffers the GPU cannot address                                    */
+/* ------------------------------------------------------------------------- */
+
+/* A ring of fixed slabs (the reference stages through 16 x 1 MiB pinned and device
+ * buffers, src/backend/src/yaksuri.h:25-26, src/util/yaksu_buffer_pool.c:77-230).  Each
+ * slab is a device half and a pinned-host half, each holding a packed chunk and a typed
+ * chunk.  A staged request is cut into chunks; chunk i uses slab i mod nslabs and runs
+ * as three event-chained stages on three library streams, so that copies of one chunk
+ * overlap the kernel of the next:
+ *   in:   wait for the slab to be free; user buffer -> pinned slab (a host function:
+ *         plain memcpy on the driver's callback thread), pinned -> device slab;
+ *   run:  the chunk's kernel, device slab in place of the unaddressable buffer;
+ *   out:  device slab -> pinned slab -> user buffer (host function); the slab is free.
+ * Everything is enqueued before the call returns: yaksa_ipack never waits, and the
+ * request's event follows the last host copy (the reference's progress engine instead
+ * polls its chunks from yaksa_request_test/wait, src/backend/src/yaksuri_progress.c:
+ * 2862-3088).  A typed chunk is the span its elements touch, rewritten whole on the way
+ * out (bytes of the span outside the typemap get back the values read at the chunk's
+ * start).  An element whose span exceeds a slab is staged through one stream-ordered
+ * allocation of that span instead. */
+
+#define YK_STAGE_MAX_SLABS 256
+
+typedef struct {
+    pthread_mutex_t mu;
+    int ready;
+    int nslabs;
+    size_t slab;                /* bytes of one side (packed or typed) of one slab */
+    char *dev, *host;           /* nslabs x 2 x (slab + 16) */
+    cudaEvent_t ev_in[YK_STAGE_MAX_SLABS], ev_run[YK_STAGE_MAX_SLABS],
+        ev_free[YK_STAGE_MAX_SLABS], ev_start, ev_end;
+    cudaStream_t s_in, s_run, s_out;
+    unsigned next;
+    uint64_t chunks;
+} yk_stage_ring;
+
+static yk_stage_ring ST = { .mu = PTHREAD_MUTEX_INITIALIZER };
+
+/* caller holds ST.mu */
+static int stage_ready(void)
 {
-    __atomic_add_fetch(&R.staged_calls, 1, __ATOMIC_RELAXED);
-    void *scr_t = NULL, *scr_p = NULL;
-    char *dtyped = p->dtyped, *dpacked = p->dpacked;
+    if (ST.ready)
+        return YAKSA_SUCCESS;
+    const char *e = getenv("YAKSA_GB300_STAGE_SLABS");
+    ST.nslabs = e ? atoi(e) : 16;
+    if (ST.nslabs < 2 || ST.nslabs > YK_STAGE_MAX_SLABS)
+        ST.nslabs = 16;
+    e = getenv("YAKSA_GB300_STAGE_SLAB_KIB");
+    long kib = e ? atol(e) : 1024;
+    if (kib < 64 || kib > (1 << 20))
+        kib = 1024;
+    ST.slab = (size_t) kib << 10;
+    size_t bytes = (size_t) ST.nslabs * 2 * (ST.slab + 16);
+    if (yk_fail_injected() || cudaMalloc((void **) &ST.dev, bytes) != cudaSuccess) {
+        ST.dev = NULL;
+        return YAKSA_ERR__OUT_OF_MEM;
+    }
+    if (yk_fail_injected() || cudaHostAlloc((void **) &ST.host, bytes, cudaHostAllocPortable) != cudaSuccess) {
+        cudaFree(ST.dev);
+        ST.dev = ST.host = NULL;
+        return YAKSA_ERR__OUT_OF_MEM;
+    }
+    cudaError_t c = cudaSuccess;
+    for (int k = 0; k < ST.nslabs && c == cudaSuccess; k++) {
+        c = cudaEventCreateWithFlags(&ST.ev_in[k], cudaEventDisableTiming);
+        if (c == cudaSuccess)
+            c = cudaEventCreateWithFlags(&ST.ev_run[k], cudaEventDisableTiming);
+        if (c == cudaSuccess)
+            c = cudaEventCreateWithFlags(&ST.ev_free[k], cudaEventDisableTiming);
+    }
+    if (c == cudaSuccess)
+        c = cudaEventCreateWithFlags(&ST.ev_start, cudaEventDisableTiming);
+    if (c == cudaSuccess)
+        c = cudaEventCreateWithFlags(&ST.ev_end, cudaEventDisableTiming);
+    if (c == cudaSuccess)
+        c = cudaStreamCreateWithFlags(&ST.s_in, cudaStreamNonBlocking);
+    if (c == cudaSuccess)
+        c = cudaStreamCreateWithFlags(&ST.s_run, cudaStreamNonBlocking);
+    if (c == cudaSuccess)
+        c = cudaStreamCreateWithFlags(&ST.s_out, cudaStreamNonBlocking);
+    if (c != cudaSuccess)
+        return cuda_err(c, "staging ring setup");
+    ST.ready = 1;
+    return YAKSA_SUCCESS;
+}
+
+static void stage_finalize(void)
+{
+    pthread_mutex_lock(&ST.mu);
+    if (ST.ready) {
+        cudaStreamSynchronize(ST.s_in);
+        cudaStreamSynchronize(ST.s_run);
+        cudaStreamSynchronize(ST.s_out);
+        for (int k = 0; k < ST.nslabs; k++) {
+            cudaEventDestroy(ST.ev_in[k]);
+            cudaEventDestroy(ST.ev_run[k]);
+            cudaEventDestroy(ST.ev_free[k]);
+        }
+        cudaEventDestroy(ST.ev_start);
+        cudaEventDestroy(ST.ev_end);
+        cudaStreamDestroy(ST.s_in);
+        cudaStreamDestroy(ST.s_run);
+        cudaStreamDestroy(ST.s_out);
+        cudaFree(ST.dev);
+        cudaFreeHost(ST.host);
+        ST.dev = ST.host = NULL;
+        ST.ready = 0;
+    }
+    pthread_mutex_unlock(&ST.mu);
+}
+
+typedef struct {
+    void *dst;
+    const void *src;
+    size_t n;
+} yk_hcopy;
+
+static void CUDART_CB hcopy_fn(void *arg)
+{
+    yk_hcopy *c = (yk_hcopy *) arg;
+    memcpy(c->dst, c->src, c->n);
+    free(c);
+}
+
+/* a host-side copy in stream order (user memory the GPU cannot address <-> pinned slab) */
+static int host_copy(cudaStream_t s, void *dst, const void *src, size_t n)
+{
+    yk_hcopy *c = malloc(sizeof(*c));
+    if (!c)
+        return YAKSA_ERR__OUT_OF_MEM;
+    c->dst = dst;
+    c->src = src;
+    c->n = n;
+    cudaError_t e = cudaLaunchHostFunc(s, hcopy_fn, c);
+    if (e != cudaSuccess) {
+        free(c);
+        return cuda_err(e, "cudaLaunchHostFunc");
+    }
+    return YAKSA_SUCCESS;
+}
+
+/* typed bytes [lo, hi) touched by the packed range [b0, b1) of (count, t), relative to the
+ * typed pointer (the same bounds plan() computes for the whole request) */
+static void typed_span(const yk_type * t, uintptr_t b0, uintptr_t b1, int64_t * lo, int64_t * hi)
+{
+    uintptr_t e0 = b0 / t->size, e1 = (b1 + t->size - 1) / t->size;
+    int64_t ext = t->extent;
+    *lo = (ext >= 0 ? (int64_t) e0 * ext : (int64_t) (e1 - 1) * ext) + t->true_lb;
+    *hi = (ext >= 0 ? (int64_t) (e1 - 1) * ext : (int64_t) e0 * ext) + t->true_ub;
+}
+
+/* end of the chunk that starts at packed byte b: at most `slab` packed bytes (when the
+ * packed side is staged) and a typed span of at most `slab` bytes (when the typed side
+ * is), on builtin boundaries; returns b when not even one element's span fits */
+static uintptr_t chunk_end(const yk_plan * p, uintptr_t b, size_t slab)
+{
+    yk_type *t = p->t;
+    uintptr_t e = YK_MIN(p->b1, b + slab);
+    if (p->staged & 1) {
+        /* whole elements while their span fits */
+        uint64_t ext = (uint64_t) (t->extent < 0 ? -t->extent : t->extent);
+        uint64_t span1 = (uint64_t) (t->true_ub - t->true_lb);
+        if (span1 > slab)
+            return b;
+        uint64_t m = ext ? 1 + (slab - span1) / ext : p->count;
+        uintptr_t eb = b / t->size;
+        uintptr_t lim = (eb + m) * t->size;
+        e = YK_MIN(e, lim);
+        while (e > b) {
+            int64_t lo, hi;
+            typed_span(t, b, e, &lo, &hi);
+            if ((uint64_t) (hi - lo) <= slab)
+                break;
+            e = b + (e - b) / 2;
+        }
+    }
+    uintptr_t f = yk_builtin_floor(t, p->count, e);
+    return f > b ? f : (e == p->b1 ? e : f);
+}
+
+/* An element whose typed span exceeds a slab: one stream-ordered allocation of the span
+ * (and of the packed range when that side is staged too), released in stream order. */
+static int stage_oversize(const yk_plan * p)
+{
+    cudaStream_t s = ST.s_run;
     uintptr_t n = p->b1 - p->b0;
     size_t span = (size_t) (p->hi - p->lo);
+    char *dt = p->dtyped, *dp = p->dpacked;
+    void *scr_t = NULL, *scr_p = NULL;
     int rc = YAKSA_SUCCESS;
     if (p->staged & 1) {
         rc = yk_fail_injected() ? YAKSA_ERR__OUT_OF_MEM :
@@ -582,18 +817,17 @@ static int run_staged(const yk_plan * p, cudaStream_t s)
         if (!rc)
             rc = cuda_err(cudaMemcpyAsync(scr_t, p->typed + p->lo, span, cudaMemcpyHostToDevice, s),
                           "stage in");
-        dtyped = (char *) scr_t - p->lo;
+        dt = (char *) scr_t - p->lo;
     }
     if (!rc && (p->staged & 2)) {
         rc = yk_fail_injected() ? YAKSA_ERR__OUT_OF_MEM :
             cuda_err(cudaMallocAsync(&scr_p, n, s), "cudaMallocAsync");
         if (!rc && (p->dir == 1 || p->op != YAKSA_OP__REPLACE))
-            rc = cuda_err(cudaMemcpyAsync(scr_p, p->packed, n, cudaMemcpyHostToDevice, s),
-                          "stage in");
-        dpacked = scr_p;
+            rc = cuda_err(cudaMemcpyAsync(scr_p, p->packed, n, cudaMemcpyHostToDevice, s), "stage in");
+        dp = scr_p;
     }
     if (!rc)
-        rc = enqueue(p, dtyped, dpacked, s);
+        rc = enqueue(p, dt, dp, s);
     if (!rc && p->dir == 0 && (p->staged & 2))
         rc = cuda_err(cudaMemcpyAsync(p->packed, scr_p, n, cudaMemcpyDeviceToHost, s), "stage out");
     if (!rc && p->dir == 1 && (p->staged & 1))
@@ -603,8 +837,123 @@ static int run_staged(const yk_plan * p, cudaStream_t s)
         cudaFreeAsync(scr_t, s);
     if (scr_p)
         cudaFreeAsync(scr_p, s);
+    return rc;
+}
+
+/* one chunk [cb0, cb1) through slab k (caller holds ST.mu); prev >= 0: the slab of the
+ * previous chunk, whose copy out this chunk's copy in must follow (typed spans that a
+ * staged unpack writes back may overlap from chunk to chunk) */
+static int stage_chunk(const yk_plan * p, uintptr_t cb0, uintptr_t cb1, unsigned k, int prev)
+{
+    const size_t side = ST.slab + 16;
+    char *dslab = ST.dev + (size_t) k * 2 * side, *hslab = ST.host + (size_t) k * 2 * side;
+    char *dpk = dslab, *hpk = hslab;            /* packed half */
+    yk_plan q = *p;
+    q.b0 = cb0;
+    q.b1 = cb1;
+    uintptr_t n = cb1 - cb0;
+    int64_t tlo = 0, thi = 0;
+    size_t tmis = 0;
+    char *dty = NULL, *hty = NULL;              /* typed half, same alignment mod 16 */
+    if (p->staged & 1) {
+        typed_span(p->t, cb0, cb1, &tlo, &thi);
+        tmis = (size_t) ((uintptr_t) (p->typed + tlo) & 15);
+        dty = dslab + side + tmis;
+        hty = hslab + side + tmis;
+        q.dtyped = dty - tlo;
+    } else {
+        q.dtyped = p->dtyped;
+    }
+    q.dpacked = (p->staged & 2) ? dpk : p->dpacked + (cb0 - p->b0);
+    char *upk = p->packed + (cb0 - p->b0);       /* the caller's packed bytes of the chunk */
+    int rc = cuda_err(cudaStreamWaitEvent(ST.s_in, ST.ev_free[k], 0), "stage wait");
+    if (!rc && prev >= 0)
+        rc = cuda_err(cudaStreamWaitEvent(ST.s_in, ST.ev_free[prev], 0), "stage wait");
+    /* in: what the kernel reads from staged memory */
+    if (!rc && (p->staged & 2) && (p->dir == 1 || p->op != YAKSA_OP__REPLACE)) {
+        rc = host_copy(ST.s_in, hpk, upk, n);
+        if (!rc)
+            rc = cuda_err(cudaMemcpyAsync(dpk, hpk, n, cudaMemcpyHostToDevice, ST.s_in), "stage in");
+    }
+    if (!rc && (p->staged & 1)) {
+        rc = host_copy(ST.s_in, hty, p->typed + tlo, (size_t) (thi - tlo));
+        if (!rc)
+            rc = cuda_err(cudaMemcpyAsync(dty, hty, (size_t) (thi - tlo), cudaMemcpyHostToDevice,
+                                          ST.s_in), "stage in");
+    }
     if (!rc)
-        rc = cuda_err(cudaStreamSynchronize(s), "staged completion");
+        rc = cuda_err(cudaEventRecord(ST.ev_in[k], ST.s_in), "stage record");
+    /* run */
+    if (!rc)
+        rc = cuda_err(cudaStreamWaitEvent(ST.s_run, ST.ev_in[k], 0), "stage wait");
+    if (!rc)
+        rc = enqueue(&q, q.dtyped, q.dpacked, ST.s_run);
+    if (!rc)
+        rc = cuda_err(cudaEventRecord(ST.ev_run[k], ST.s_run), "stage record");
+    /* out: what the kernel wrote to staged memory */
+    if (!rc)
+        rc = cuda_err(cudaStreamWaitEvent(ST.s_out, ST.ev_run[k], 0), "stage wait");
+    if (!rc && p->dir == 0 && (p->staged & 2)) {
+        rc = cuda_err(cudaMemcpyAsync(hpk, dpk, n, cudaMemcpyDeviceToHost, ST.s_out), "stage out");
+        if (!rc)
+            rc = host_copy(ST.s_out, upk, hpk, n);
+    }
+    if (!rc && p->dir == 1 && (p->staged & 1)) {
+        rc = cuda_err(cudaMemcpyAsync(hty, dty, (size_t) (thi - tlo), cudaMemcpyDeviceToHost, ST.s_out),
+                      "stage out");
+        if (!rc)
+            rc = host_copy(ST.s_out, p->typed + tlo, hty, (size_t) (thi - tlo));
+    }
+    if (!rc)
+        rc = cuda_err(cudaEventRecord(ST.ev_free[k], ST.s_out), "stage record");
+    return rc;
+}
+
+/* A request with a buffer the GPU cannot address, ordered after the work already on
+ * stream s and before anything enqueued on s later; nothing waits on the host. */
+static int run_staged(const yk_plan * p, cudaStream_t s)
+{
+    __atomic_add_fetch(&R.staged_calls, 1, __ATOMIC_RELAXED);
+    pthread_mutex_lock(&ST.mu);
+    int rc = stage_ready();
+    if (!rc)
+        rc = cuda_err(cudaEventRecord(ST.ev_start, s), "stage record");
+    if (!rc)
+        rc = cuda_err(cudaStreamWaitEvent(ST.s_in, ST.ev_start, 0), "stage wait");
+    if (!rc)
+        rc = cuda_err(cudaStreamWaitEvent(ST.s_run, ST.ev_start, 0), "stage wait");
+    int prev = -1;
+    for (uintptr_t b = p->b0; !rc && b < p->b1;) {
+        uintptr_t e = chunk_end(p, b, ST.slab);
+        if (e <= b) {
+            /* one element's typed span is larger than a slab: the whole request at once,
+             * after every chunk enqueued so far (stream order on s_run) */
+            yk_plan q = *p;
+            q.b0 = b;
+            typed_span(p->t, q.b0, q.b1, &q.lo, &q.hi);
+            if (p->staged & 2)
+                q.packed = p->packed + (b - p->b0);
+            if (!(p->staged & 2))
+                q.dpacked = p->dpacked + (b - p->b0);
+            rc = stage_oversize(&q);
+            if (!rc)
+                rc = cuda_err(cudaEventRecord(ST.ev_end, ST.s_run), "stage record");
+            if (!rc)
+                rc = cuda_err(cudaStreamWaitEvent(ST.s_out, ST.ev_end, 0), "stage wait");
+            break;
+        }
+        unsigned k = ST.next++ % (unsigned) ST.nslabs;
+        rc = stage_chunk(p, b, e, k, (p->dir == 1 && (p->staged & 1)) ? prev : -1);
+        prev = (int) k;
+        ST.chunks++;
+        b = e;
+    }
+    /* s continues after the last copy out */
+    if (!rc)
+        rc = cuda_err(cudaEventRecord(ST.ev_end, ST.s_out), "stage record");
+    if (!rc)
+        rc = cuda_err(cudaStreamWaitEvent(s, ST.ev_end, 0), "stage wait");
+    pthread_mutex_unlock(&ST.mu);
     return rc;
 }
 
@@ -669,12 +1018,10 @@ static int pup(int dir, const void *packed_in, void *packed_out, char *typed, ui
     cudaStream_t s = (mode == YK_MODE_STREAM && stream) ? *(cudaStream_t *) stream : lib_stream();
     if (p.staged) {
         rc = run_staged(&p, s);
-        if (!rc)
-            *actual = p.b1 - p.b0;
-        return rc;
+    } else {
+        __atomic_add_fetch(&R.direct_calls, 1, __ATOMIC_RELAXED);
+        rc = enqueue(&p, p.dtyped, p.dpacked, s);
     }
-    __atomic_add_fetch(&R.direct_calls, 1, __ATOMIC_RELAXED);
-    rc = enqueue(&p, p.dtyped, p.dpacked, s);
     if (rc)
         return rc;
     *actual = p.b1 - p.b0;
@@ -876,12 +1223,7 @@ static int batch_run_ranges(yaksa_gb300_pup_t * ops, int n, yaksa_info_t info, c
             break;
         }
         yk_plan p;
-        if (o->kind == 0)
-            rc = plan(0, NULL, o->outbuf, (char *) o->inbuf, o->count, t, o->offset, o->maxbytes,
-                      info, o->op, &p);
-        else
-            rc = plan(1, o->inbuf, NULL, (char *) o->outbuf, o->count, t, o->offset, o->maxbytes,
-                      info, o->op, &p);
+        rc = plan_op(o, t, info, &p);
         if (rc || p.b1 == p.b0)
             continue;
         o->actual = p.b1 - p.b0;
@@ -986,11 +1328,7 @@ int yaksa_gb300_pup_noalloc(yaksa_gb300_pup_t * o, void *stream)
     if (!t)
         return YAKSA_ERR__INTERNAL;
     yk_plan p;
-    int rc = o->kind == 0 ?
-        plan(0, NULL, o->outbuf, (char *) o->inbuf, o->count, t, o->offset, o->maxbytes, NULL,
-             o->op, &p) :
-        plan(1, o->inbuf, NULL, (char *) o->outbuf, o->count, t, o->offset, o->maxbytes, NULL,
-             o->op, &p);
+    int rc = plan_op(o, t, NULL, &p);
     if (rc || p.b1 == p.b0)
         return rc;
     if (p.staged) {
@@ -1053,6 +1391,7 @@ typedef struct {
     uint64_t bytes;
     yk_type *t;
     int busy;
+    int64_t user;               /* the serving loop's index of the request (-1: none) */
 } yk_srv_slot;
 
 struct yaksa_gb300_server_s {
@@ -1063,9 +1402,17 @@ struct yaksa_gb300_server_s {
     yk_launch *reqs;            /* pinned, mapped */
     yk_item *items;             /* pinned, mapped */
     unsigned long long *req_done;       /* pinned, mapped: items finished per request slot */
+    uint64_t *req_nitems;       /* pinned, mapped: items per request slot */
+    unsigned long long *cq;     /* pinned, mapped: completion queue written by the GPU */
+    uint64_t cq_head;           /* next completion queue entry the host reads */
     uint64_t *ctl;              /* pinned, mapped: [0] items published, [1] stop, [2] status */
-    unsigned long long *next_item;      /* device: the lanes' claim counters */
+    unsigned long long *next_item;      /* device: the lanes' claim counters, then the
+                                         * completion queue's tail */
     yk_srv_slot *slots;
+    int64_t *done_log;          /* serving loop: user indices of requests completed since
+                                 * it last looked (NULL: not logged) */
+    int ndone;
+    uint64_t ctas_launched;     /* resident CTAs launched so far (all launches) */
     uint64_t req_seq, item_seq, oldest_req;
     uint64_t inflight_bytes, budget;
     uint64_t relaunches;
@@ -1117,14 +1464,16 @@ int yaksa_gb300_server_create(uint32_t ring_requests, uint64_t budget_bytes,
     S->reqs = pinned(sizeof(yk_launch) * S->qr);
     S->items = pinned(sizeof(yk_item) * S->qi);
     S->req_done = pinned(sizeof(unsigned long long) * S->qr);
+    S->req_nitems = pinned(sizeof(uint64_t) * S->qr);
+    S->cq = pinned(sizeof(unsigned long long) * S->qr);
     S->ctl = pinned(64);
     S->slots = calloc(S->qr, sizeof(yk_srv_slot));
-    if (!S->reqs || !S->items || !S->req_done || !S->ctl || !S->slots ||
-        yk_fail_injected() ||
-        cudaMalloc((void **) &S->next_item, sizeof(unsigned long long) * YK_SRV_LANES *
-                   YK_SRV_LANE_STRIDE) != cudaSuccess ||
-        cudaMemset(S->next_item, 0, sizeof(unsigned long long) * YK_SRV_LANES *
-                   YK_SRV_LANE_STRIDE) != cudaSuccess ||
+    /* device counters: the claim lanes (one 128-byte line each), then the queue's tail */
+    const size_t nctr = (size_t) (YK_SRV_LANES + 1) * YK_SRV_LANE_STRIDE;
+    if (!S->reqs || !S->items || !S->req_done || !S->req_nitems || !S->cq || !S->ctl ||
+        !S->slots || yk_fail_injected() ||
+        cudaMalloc((void **) &S->next_item, sizeof(unsigned long long) * nctr) != cudaSuccess ||
+        cudaMemset(S->next_item, 0, sizeof(unsigned long long) * nctr) != cudaSuccess ||
         cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking) != cudaSuccess) {
         yaksa_gb300_server_destroy(S);
         return YAKSA_ERR__OUT_OF_MEM;
@@ -1138,6 +1487,9 @@ int yaksa_gb300_server_create(uint32_t ring_requests, uint64_t budget_bytes,
     S->args.stop = (const volatile int *) &S->ctl[1];
     S->args.next_item = S->next_item;
     S->args.status = (volatile uint32_t *) &S->ctl[2];
+    S->args.req_nitems = S->req_nitems;
+    S->args.cq = S->cq;
+    S->args.cq_tail = S->next_item + (size_t) YK_SRV_LANES * YK_SRV_LANE_STRIDE;
     S->args.qi = S->qi;
     S->args.qr = S->qr;
     S->args.max_idle_spins = 4000;      /* ~8 ms without work at the 2 us poll interval */
@@ -1145,38 +1497,48 @@ int yaksa_gb300_server_create(uint32_t ring_requests, uint64_t budget_bytes,
     return YAKSA_SUCCESS;
 }
 
-/* reclaim finished requests (oldest first) and keep a kernel resident while items are
- * pending; caller holds S->mu */
+/* a request leaves the server; caller holds S->mu */
+static void server_retire(struct yaksa_gb300_server_s *S, yk_srv_slot * sl)
+{
+    sl->busy = 0;
+    S->inflight_bytes -= sl->bytes;
+    if (sl->t)
+        yk_type_unref(sl->t);
+    sl->t = NULL;
+    if (S->done_log && sl->user >= 0)
+        S->done_log[S->ndone++] = sl->user;
+}
+
+/* reclaim finished requests and keep a kernel resident while items are pending; caller
+ * holds S->mu.  The GPU appends each finished request's slot to the completion queue, so
+ * this costs one read per completion, not one per request in flight. */
 static int server_progress_locked(struct yaksa_gb300_server_s *S)
 {
-    /* any request whose items are all done completes, in whatever order */
-    for (uint64_t s = S->oldest_req; s < S->req_seq; s++) {
-        yk_srv_slot *sl = &S->slots[s % S->qr];
-        if (!sl->busy)
-            continue;
-        /* one word per request: the GPU counts the request's finished items */
-        if (sl->nitems &&
-            __atomic_load_n(&S->req_done[s % S->qr], __ATOMIC_ACQUIRE) < sl->nitems)
-            continue;
-        sl->busy = 0;
-        S->inflight_bytes -= sl->bytes;
-        if (sl->t)
-            yk_type_unref(sl->t);
-        sl->t = NULL;
+    for (;;) {
+        unsigned long long *e = &S->cq[S->cq_head % S->qr];
+        unsigned long long v = __atomic_load_n(e, __ATOMIC_ACQUIRE);
+        if (!v)
+            break;              /* empty, or its position taken and the write not seen yet */
+        __atomic_store_n(e, 0ull, __ATOMIC_RELAXED);
+        S->cq_head++;
+        yk_srv_slot *sl = &S->slots[(v - 1) % S->qr];
+        if (sl->busy)
+            server_retire(S, sl);
     }
     while (S->oldest_req < S->req_seq && !S->slots[S->oldest_req % S->qr].busy)
         S->oldest_req++;
-    if (S->running && cudaStreamQuery(S->stream) != cudaErrorNotReady) {
-        S->running = 0;
-        cudaGetLastError();
-    }
-    uint64_t claimed_upto = S->item_seq;
+    /* every resident CTA counts its exit: none is resident once the exits reach the CTAs
+     * launched (no CUDA call on this path) */
+    const volatile uint32_t *st = (const volatile uint32_t *) &S->ctl[2];
+    uint64_t exits = (uint64_t) st[0] + (uint64_t) st[1];
+    S->running = exits < S->ctas_launched;
     int pending = S->oldest_req < S->req_seq;
-    if (pending && !S->running && claimed_upto) {
+    if (pending && !S->running && S->item_seq) {
         int e = yk_cuda_server_launch(&S->args, S->ctas, S->stream);
         if (e)
             return cuda_err((cudaError_t) e, "server launch");
         S->running = 1;
+        S->ctas_launched += (uint64_t) S->ctas;
         S->relaunches++;
     }
     return YAKSA_SUCCESS;
@@ -1190,19 +1552,25 @@ int yaksa_gb300_server_progress(yaksa_gb300_server_t S)
     return rc;
 }
 
+static int server_submit(struct yaksa_gb300_server_s *S, yaksa_gb300_pup_t * o, yaksa_info_t info,
+                         uint64_t * ticket, int64_t user);
+
 int yaksa_gb300_server_submit(yaksa_gb300_server_t S, yaksa_gb300_pup_t * o, yaksa_info_t info,
                               uint64_t * ticket)
+{
+    return server_submit(S, o, info, ticket, -1);
+}
+
+/* user: the serving loop's index of the request, logged at completion (-1: none) */
+static int server_submit(struct yaksa_gb300_server_s *S, yaksa_gb300_pup_t * o, yaksa_info_t info,
+                         uint64_t * ticket, int64_t user)
 {
     o->actual = 0;
     yk_type *t = yk_type_get(o->type);
     if (!t)
         return YAKSA_ERR__INTERNAL;
     yk_plan p;
-    int rc = o->kind == 0 ?
-        plan(0, NULL, o->outbuf, (char *) o->inbuf, o->count, t, o->offset, o->maxbytes, info,
-             o->op, &p) :
-        plan(1, o->inbuf, NULL, (char *) o->outbuf, o->count, t, o->offset, o->maxbytes, info,
-             o->op, &p);
+    int rc = plan_op(o, t, info, &p);
     if (rc)
         return rc;
     if (p.staged)
@@ -1268,12 +1636,15 @@ int yaksa_gb300_server_submit(yaksa_gb300_server_t S, yaksa_gb300_pup_t * o, yak
     sl->item0 = S->item_seq;
     sl->nitems = nitems;
     sl->bytes = n;
-    sl->busy = 1;
-    sl->t = t;
-    yk_type_ref(t);
-    S->inflight_bytes += n;
+    sl->busy = nitems > 0;      /* an empty request is complete at once */
+    sl->t = NULL;
+    sl->user = user;
     if (nitems) {
+        sl->t = t;
+        yk_type_ref(t);
+        S->inflight_bytes += n;
         __atomic_store_n(&S->req_done[slot], 0ull, __ATOMIC_RELAXED);
+        S->req_nitems[slot] = nitems;
         memcpy(&S->reqs[slot], &L, sizeof(L));
         for (uint64_t i = 0; i < nitems; i++) {
             yk_item *it = &S->items[(S->item_seq + i) % S->qi];
@@ -1288,7 +1659,7 @@ int yaksa_gb300_server_submit(yaksa_gb300_server_t S, yaksa_gb300_pup_t * o, yak
         __atomic_store_n(&S->ctl[0], S->item_seq, __ATOMIC_RELEASE);
     }
     o->actual = n;
-    rc = server_progress_locked(S);
+    rc = server_progress_locked(S);     /* relaunches the resident kernel if it left */
     pthread_mutex_unlock(&S->mu);
     *ticket = seq;
     return rc;
@@ -1374,6 +1745,10 @@ int yaksa_gb300_server_destroy(yaksa_gb300_server_t S)
             cudaFreeHost(S->items);
         if (S->req_done)
             cudaFreeHost(S->req_done);
+        if (S->req_nitems)
+            cudaFreeHost(S->req_nitems);
+        if (S->cq)
+            cudaFreeHost(S->cq);
         if (S->ctl)
             cudaFreeHost(S->ctl);
     }
@@ -1411,6 +1786,19 @@ int yaksa_gb300_serve_trace(yaksa_gb300_pup_t * ops, const double *arrival_s, in
         return YAKSA_ERR__OUT_OF_MEM;
     }
     int next = 0, done = 0, oldest = 0;
+    if (mode == 1) {
+        /* the server logs the loop's index of each request it completes */
+        int64_t *log = malloc(sizeof(int64_t) * (n > 0 ? n : 1));
+        if (!log) {
+            free(handle);
+            free(state);
+            return YAKSA_ERR__OUT_OF_MEM;
+        }
+        pthread_mutex_lock(&server->mu);
+        server->done_log = log;
+        server->ndone = 0;
+        pthread_mutex_unlock(&server->mu);
+    }
     double t0 = now_s(), last = t0;
     while (done < n && !rc) {
         double t = now_s() - t0;
@@ -1419,7 +1807,7 @@ int yaksa_gb300_serve_trace(yaksa_gb300_pup_t * ops, const double *arrival_s, in
             yaksa_gb300_pup_t *o = &ops[next];
             if (mode == 1) {
                 uint64_t tk;
-                int r = yaksa_gb300_server_submit(server, o, info, &tk);
+                int r = server_submit(server, o, info, &tk, next);
                 if (r == YAKSA_ERR__OUT_OF_MEM)
                     break;      /* rings or byte budget full: retry after progress */
                 if (r) {
@@ -1427,10 +1815,17 @@ int yaksa_gb300_serve_trace(yaksa_gb300_pup_t * ops, const double *arrival_s, in
                     break;
                 }
                 handle[next] = tk;
+                if (!o->actual) {
+                    /* an empty request completes at submission, without a queue entry */
+                    latency_s[next] = now_s() - t0 - arrival_s[next];
+                    state[next++] = 2;
+                    done++;
+                    continue;
+                }
             } else {
                 yaksa_request_t req;
                 uintptr_t actual;
-                int r = o->kind == 0 ?
+                int r = o->kind != 0 && o->kind != 1 ? YAKSA_ERR__INTERNAL : o->kind == 0 ?
                     yaksa_ipack(o->inbuf, o->count, o->type, o->offset, o->outbuf, o->maxbytes,
                                 &actual, info, o->op, &req) :
                     yaksa_iunpack(o->inbuf, o->maxbytes, o->outbuf, o->count, o->type, o->offset,
@@ -1445,32 +1840,47 @@ int yaksa_gb300_serve_trace(yaksa_gb300_pup_t * ops, const double *arrival_s, in
             state[next] = 1;
             next++;
         }
-        /* completions: one progress pass, then a cheap done check per request in flight
-         * (requests may finish out of order) */
+        /* completions (requests may finish out of order): the server reports the ones it
+         * saw, in one progress pass; plain requests are tested one by one */
         if (mode == 1) {
             pthread_mutex_lock(&server->mu);
             rc = server_progress_locked(server);
-        }
-        double tc = now_s();
-        for (int i = oldest; i < next && !rc; i++) {
-            if (state[i] != 1)
-                continue;
-            int c = 0;
-            if (mode == 1)
-                c = server_done_locked(server, handle[i]);
-            else
+            double tc = now_s();
+            for (int k = 0; k < server->ndone; k++) {
+                int64_t i = server->done_log[k];
+                if (i >= 0 && i < n && state[i] == 1) {
+                    latency_s[i] = tc - t0 - arrival_s[i];
+                    state[i] = 2;
+                    done++;
+                    last = tc;
+                }
+            }
+            server->ndone = 0;
+            pthread_mutex_unlock(&server->mu);
+        } else {
+            double tc = now_s();
+            for (int i = oldest; i < next && !rc; i++) {
+                if (state[i] != 1)
+                    continue;
+                int c = 0;
                 rc = yaksa_request_test(handle[i], &c);
-            if (c) {
-                latency_s[i] = tc - t0 - arrival_s[i];
-                state[i] = 2;
-                done++;
-                last = tc;
+                if (c) {
+                    latency_s[i] = tc - t0 - arrival_s[i];
+                    state[i] = 2;
+                    done++;
+                    last = tc;
+                }
             }
         }
-        if (mode == 1)
-            pthread_mutex_unlock(&server->mu);
         while (oldest < next && state[oldest] == 2)
             oldest++;
+    }
+    if (mode == 1) {
+        pthread_mutex_lock(&server->mu);
+        free(server->done_log);
+        server->done_log = NULL;
+        server->ndone = 0;
+        pthread_mutex_unlock(&server->mu);
     }
     *makespan_s = last - t0;
     free(handle);
@@ -1518,11 +1928,7 @@ int yaksa_gb300_graph_create(yaksa_gb300_pup_t * ops, const int *batch_ends, int
             break;
         }
         yk_plan p;
-        rc = o->kind == 0 ?
-            plan(0, NULL, o->outbuf, (char *) o->inbuf, o->count, t, o->offset, o->maxbytes,
-                 info, o->op, &p) :
-            plan(1, o->inbuf, NULL, (char *) o->outbuf, o->count, t, o->offset, o->maxbytes,
-                 info, o->op, &p);
+        rc = plan_op(o, t, info, &p);
         if (rc)
             break;
         if (p.b1 == p.b0)

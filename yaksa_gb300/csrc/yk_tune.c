@@ -30,16 +30,21 @@
 /* candidate shapes per family: units per thread, CTAs per SM (0 = default) */
 /* candidate shapes per family: units per thread, CTAs per SM; the first is the default
  * rule (units per thread by size, 64 or 8 CTAs per SM) */
-static const yk_tune_cfg cand_single[] = { {0, 0}, {1, 64}, {4, 8}, {4, 16}, {1, 16} };
-static const yk_tune_cfg cand_batch_regular[] = { {1, 0}, {1, 8}, {1, 4} };
-static const yk_tune_cfg cand_batch[] = { {0, 0}, {1, 64}, {4, 8}, {4, 16} };
+static const yk_tune_cfg cand_single[] = { {0, 0, 0}, {1, 64, 0}, {4, 8, 0}, {4, 16, 0}, {1, 16, 0} };
+static const yk_tune_cfg cand_batch_regular[] = { {1, 0, 0}, {1, 8, 0}, {1, 4, 0} };
+static const yk_tune_cfg cand_batch[] = { {0, 0, 0}, {1, 64, 0}, {4, 8, 0}, {4, 16, 0} };
+/* the same launches when a TMA form exists (yk_tma.cu): two residencies of it compete */
+static const yk_tune_cfg cand_single_tma[] = { {0, 0, 0}, {1, 64, 0}, {4, 8, 0}, {4, 16, 0},
+    {1, 16, 0}, {0, 4, YK_VARIANT_TMA}, {0, 8, YK_VARIANT_TMA} };
+static const yk_tune_cfg cand_runs_tma[] = { {0, 0, YK_VARIANT_RUNS}, {0, 4, YK_VARIANT_TMA},
+    {0, 8, YK_VARIANT_TMA} };
 
 typedef struct {
     uint64_t key;               /* 0: empty */
     const yk_tune_cfg *cand;
     int ncand;
     float fastest[8];           /* best sample per candidate (ms) */
-    int done[8], issued[8];
+    int done[8], issued[8];     /* at most 8 candidates per family */
     int best;                   /* -1 while timing */
 } slot_t;
 
@@ -68,7 +73,7 @@ static int log2u(uint64_t v)
 
 uint64_t yk_tune_key(int family, int depth, int vec, int dir, int wide, uint64_t units)
 {
-    /* nonzero by construction: family is 1..3 */
+    /* nonzero by construction: family is 1..5 */
     return ((uint64_t) family << 32) | ((uint64_t) (depth + 1) << 24) |
         ((uint64_t) vec << 16) | ((uint64_t) dir << 12) | ((uint64_t) wide << 8) |
         (uint64_t) log2u(units);
@@ -132,6 +137,12 @@ static slot_t *slot_locked(uint64_t key, int family)
             if (family == YK_TUNE_SINGLE) {
                 s->cand = cand_single;
                 s->ncand = (int) (sizeof(cand_single) / sizeof(cand_single[0]));
+            } else if (family == YK_TUNE_SINGLE_TMA) {
+                s->cand = cand_single_tma;
+                s->ncand = (int) (sizeof(cand_single_tma) / sizeof(cand_single_tma[0]));
+            } else if (family == YK_TUNE_RUNS_TMA) {
+                s->cand = cand_runs_tma;
+                s->ncand = (int) (sizeof(cand_runs_tma) / sizeof(cand_runs_tma[0]));
             } else if (family == YK_TUNE_BATCH_REGULAR) {
                 s->cand = cand_batch_regular;
                 s->ncand = (int) (sizeof(cand_batch_regular) / sizeof(cand_batch_regular[0]));
@@ -150,6 +161,7 @@ int yk_tune_begin(uint64_t key, int family, uint64_t units, void *stream, yk_tun
     cudaStream_t st = (cudaStream_t) stream;
     cfg->units_per_thread = family == YK_TUNE_BATCH_REGULAR ? 1 : 0;
     cfg->ctas_per_sm = 0;
+    cfg->variant = family == YK_TUNE_RUNS_TMA ? YK_VARIANT_RUNS : YK_VARIANT_BYTES;
     pthread_mutex_lock(&T.mu);
     init_locked();
     if (!T.enabled || units < YK_TUNE_MIN_UNITS) {
@@ -221,6 +233,11 @@ void yk_tune_end(int probe, void *stream)
         T.probes[probe].armed = 1;
     }
     pthread_mutex_unlock(&T.mu);
+}
+
+uint64_t yk_tune_min_units(void)
+{
+    return YK_TUNE_MIN_UNITS;
 }
 
 void yk_tune_reset(void)

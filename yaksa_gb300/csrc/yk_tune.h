@@ -4,11 +4,17 @@
 
 #include <stdint.h>
 
-enum { YK_TUNE_SINGLE = 1, YK_TUNE_BATCH_REGULAR = 2, YK_TUNE_BATCH = 3 };
+/* SINGLE_TMA: a single launch that also has a TMA form; RUNS_TMA: a struct-like pack
+ * (one element per thread) that also has a TMA form */
+enum { YK_TUNE_SINGLE = 1, YK_TUNE_BATCH_REGULAR = 2, YK_TUNE_BATCH = 3, YK_TUNE_SINGLE_TMA = 4,
+    YK_TUNE_RUNS_TMA = 5 };
+
+enum { YK_VARIANT_BYTES = 0, YK_VARIANT_TMA = 1, YK_VARIANT_RUNS = 2 };
 
 typedef struct {
     int units_per_thread;       /* 1 or 4; 0 = chosen by size */
     int ctas_per_sm;            /* grid cap; 0 = by units per thread */
+    int variant;                /* YK_VARIANT_*: which kernel runs the launch */
 } yk_tune_cfg;
 
 /* shape class of a launch */
@@ -18,5 +24,7 @@ uint64_t yk_tune_key(int family, int depth, int vec, int dir, int wide, uint64_t
 int yk_tune_begin(uint64_t key, int family, uint64_t units, void *stream, yk_tune_cfg * cfg);
 void yk_tune_end(int probe, void *stream);
 void yk_tune_reset(void);
+/* launches smaller than this are never timed */
+uint64_t yk_tune_min_units(void);
 
 #endif
