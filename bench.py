@@ -294,6 +294,13 @@ def suite_types(y, yk, np, rng_seed=7, scale=1):
     # hvector of double: 4-column block of a 1024x16 row-major matrix
     out["hvector"] = dict(mk=lambda L: L.type_create_hvector(1024, 4, 128, yk.TYPE_DOUBLE),
                           base="double", count=1, extent=1024 * 16 * 8, gran=8)
+    # single halo faces of the 512^3 float grid, one per orientation: the default run
+    # reports every face in its halo section, so these run only when named (profiling)
+    for name, sub, st in face_specs(512)[0::2]:
+        out["halo_" + name[0]] = dict(
+            mk=lambda L, sub=sub, st=st: L.type_create_subarray([512, 512, 512], sub, st,
+                                                                yk.SUBARRAY_ORDER_C, yk.TYPE_FLOAT),
+            base="float", count=1, extent=512 ** 3 * 4, gran=4, named_only=True)
     # hindexed int32: 2^20 blocks, lognormal lengths (median 16, sigma 1, clipped 1..4096),
     # non-overlapping blocks in shuffled order with random gaps inside 1 GiB
     nb = (1 << 20) // scale
@@ -381,7 +388,7 @@ def run_suite(steps, only=None, scale=1, threads=None, log=None):
     pool = OraclePool(o, threads)
     lines = []
     for name, w in suite_types(y, yk, np, scale=scale).items():
-        if only and name not in only:
+        if (only and name not in only) or (not only and w.get("named_only")):
             continue
         tp, to = w["mk"](y), w["mk"](o)
         size = y.size(tp)

@@ -117,7 +117,7 @@ static int runtime_ready(void)
                 cudaDeviceSetLimit(cudaLimitMaxL2FetchGranularity, (size_t) atoi(l2));
             if (R.tma_mode < 0) {
                 const char *tm = getenv("YAKSA_GB300_TMA");
-                R.tma_mode = tm && tm[0] >= '0' && tm[0] <= '2' ? tm[0] - '0' : 0;
+                R.tma_mode = tm && tm[0] >= '0' && tm[0] <= '2' ? tm[0] - '0' : 1;
             }
             const char *hd = getenv("YAKSA_GB300_HOST_DIRECT");
             R.host_direct = !(hd && hd[0] == '0');
