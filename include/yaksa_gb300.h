@@ -157,15 +157,31 @@ typedef struct {
 } yaksa_gb300_rows_t;
 int yaksa_gb300_probe_rows(const yaksa_gb300_rows_t * pats, int npats, int write, void *stream);
 
-/* Test hook (no counterpart in the reference): the TMA forms of the REPLACE kernels for
- * regular nests (cp.async.bulk.tensor over the typed side).  mode 0 never uses them, 1
- * lets the launch-shape autotuner choose them per shape class where they are faster
- * (the default; YAKSA_GB300_TMA=0/1/2 in the environment sets the initial mode), 2 uses
- * them wherever one exists.  Results are identical in every mode.
- * yaksa_gb300_debug_tma_stats reports the TMA launches so far and the TMA waits that ran
- * out (always 0 in correct operation). */
+/* Test hook (no counterpart in the reference): the forms of the kernels that move data
+ * with the tensor memory accelerator -- the TMA tensor-map kernels for regular nests
+ * (cp.async.bulk.tensor over the typed side) and the hindexed unpack that stages the
+ * packed stream with cp.async.bulk.  mode 0 never uses them, 1 lets the launch-shape
+ * autotuner choose them per shape class where they are faster (the default;
+ * YAKSA_GB300_TMA=0/1/2 in the environment sets the initial mode), 2 uses them wherever
+ * one exists.  Results are identical in every mode.  yaksa_gb300_debug_tma_stats reports
+ * the launches of these forms so far and the tensor-map waits that ran out;
+ * yaksa_gb300_debug_bulk_failures the bulk-staged unpack's waits that ran out (both
+ * always 0 in correct operation). */
 int yaksa_gb300_debug_tma(int mode);
 int yaksa_gb300_debug_tma_stats(unsigned long long *launches, unsigned int *failures);
+int yaksa_gb300_debug_bulk_failures(unsigned int *n);
+
+/* Segment list on the GPU (no counterpart in the reference, whose yaksa_iov fills a
+ * host array, src/frontend/include/yaksa.h.in:609): the same entries as yaksa_iov --
+ * count, type, iov_offset and max_iov_len mean the same, and *actual_iov_len is set on
+ * return -- written by a kernel into `iov`, an array of struct iovec in memory the GPU
+ * can address, enqueued on *(cudaStream_t *) stream (NULL: the legacy default stream).
+ * For a NIC gathering from a list in GPU memory (GPUDirect RDMA) or GPU-initiated
+ * transfers, with no host round trip per message.  The first call for a type keeps one
+ * element's pieces in device memory until yaksa_type_free. */
+int yaksa_gb300_iov_stream(const char *buf, uintptr_t count, yaksa_type_t type,
+                           uintptr_t iov_offset, struct iovec *iov, uintptr_t max_iov_len,
+                           uintptr_t * actual_iov_len, void *stream);
 
 /* Runtime counters since load: kernel launches, calls served in place (device or
  * GPU-addressable host memory), calls that staged host data through device memory,

@@ -70,3 +70,77 @@ def test_batch_launch_shape_is_tuned_and_exact(cuda, prod, oracle):
     for tp, to in types:
         prod.type_free(tp)
         oracle.type_free(to)
+
+
+def test_operator_and_hindexed_grids_are_tuned_and_exact(cuda, prod, oracle):
+    """the typed-operator kernel (SUM into a strided target) and the hindexed kernel take
+    their grid caps from the autotuner; every launch gives the oracle's bytes"""
+    rng = np.random.default_rng(5)
+    vp, vo = (y.type_create_hvector(1 << 16, 2, 24, yk.TYPE_DOUBLE) for y in (prod, oracle))
+    nb = 40000
+    blens = rng.integers(1, 40, nb)
+    displs = (np.cumsum(blens + rng.integers(0, 9, nb)) - blens) * 4
+    perm = rng.permutation(nb)
+    hp, ho = (y.type_create_hindexed(blens[perm].tolist(), displs[perm].tolist(), yk.TYPE_INT32_T)
+              for y in (prod, oracle))
+    before = prod.autotune_stats()
+    for (tp, to, base, op) in ((vp, vo, "double", yk.OP_SUM), (hp, ho, "int32", yk.OP_REPLACE)):
+        lb, text = prod.true_extent(tp)
+        n = prod.size(tp)
+        typed0 = fill(rng, lb + text, base)
+        packed0 = fill(rng, n, base)
+        exp = typed0.copy()
+        oracle.unpack(packed0.ctypes.data, n, exp.ctypes.data, 1, to, 0, op=op)
+        pg = dev_copy(cuda, packed0)
+        for i in range(40):
+            tg = dev_copy(cuda, typed0)
+            prod.unpack(pg.data_ptr(), n, tg.data_ptr(), 1, tp, 0, op=op)
+            cuda.cuda.synchronize()
+            assert np.array_equal(host_of(cuda, tg), exp), (base, i)
+    after = prod.autotune_stats()
+    assert after["decided"] >= before["decided"] + 2
+    for y, t in ((prod, vp), (prod, hp), (oracle, vo), (oracle, ho)):
+        y.type_free(t)
+
+
+_PERSIST_CHILD = r"""
+import ctypes, json, sys
+sys.path.insert(0, sys.argv[1]); sys.path.insert(0, sys.argv[2])
+import numpy as np, torch
+import yaksa_gb300 as yk
+from conftest import _ensure_product
+y = yk.Yaksa(_ensure_product()); y.init()
+t = y.type_create_hvector(1 << 17, 1, 64, yk.TYPE_DOUBLE)
+src = torch.zeros((1 << 17) * 64, dtype=torch.uint8, device="cuda")
+out = torch.zeros(1 << 20, dtype=torch.uint8, device="cuda")
+for _ in range(int(sys.argv[3])):
+    y.pack(src.data_ptr(), 1, t, 0, out.data_ptr(), 1 << 20)
+torch.cuda.synchronize()
+print(json.dumps(y.autotune_stats()))
+"""
+
+
+def test_decisions_persist_across_processes(cuda, tmp_path):
+    """with YAKSA_GB300_TUNE_FILE set, a process appends each decided shape class to the
+    file, and the next process on the same kind of GPU starts with that class decided:
+    its launches of the shape are not timed"""
+    import json
+    import os
+    import subprocess
+    import sys
+    tests = os.path.dirname(os.path.abspath(__file__))
+    root = os.path.dirname(tests)
+    f = tmp_path / "tune.txt"
+    env = dict(os.environ, YAKSA_GB300_TUNE_FILE=str(f))
+
+    def child(n):
+        r = subprocess.run([sys.executable, "-c", _PERSIST_CHILD, root, tests, str(n)], env=env,
+                           capture_output=True, text=True, timeout=300)
+        assert r.returncode == 0, r.stderr[-3000:]
+        return json.loads(r.stdout.strip().splitlines()[-1])
+
+    first = child(40)
+    assert first["decided"] >= 1 and first["probes"] > 0, first
+    assert f.exists() and f.read_text().strip(), "no decision written"
+    second = child(5)
+    assert second["decided"] == second["classes"] and second["probes"] == 0, second

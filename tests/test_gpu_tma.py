@@ -1,5 +1,6 @@
-"""GPU: the TMA (cp.async.bulk.tensor) form of the REPLACE kernels for regular nests,
-against the oracle.
+"""GPU: the forms that move data with the tensor memory accelerator, against the oracle:
+the TMA (cp.async.bulk.tensor) form of the REPLACE kernels for regular nests, and the
+hindexed unpack whose packed stream is staged by cp.async.bulk.
 
 With the test hook set to 2 every launch that has a TMA form takes it: packs of nests of
 one to three strided levels over runs of up to 256 bytes (the run may start anywhere in
@@ -143,3 +144,59 @@ def test_tma_tuned_repeats(cuda, prod, oracle):
         oracle.type_free(to)
     finally:
         prod.lib.yaksa_gb300_debug_tma(1)
+
+
+def _bulk_failures(prod):
+    f = ctypes.c_uint()
+    prod.lib.yaksa_gb300_debug_bulk_failures.argtypes = [ctypes.POINTER(ctypes.c_uint)]
+    assert prod.lib.yaksa_gb300_debug_bulk_failures(ctypes.byref(f)) == 0
+    return f.value
+
+
+@pytest.mark.parametrize("maxlen,seed", [(40, 1), (5000, 2)])
+def test_hindexed_bulk_unpack(cuda, tma, oracle, maxlen, seed):
+    """hook 2 forces the bulk-staged hindexed unpack: shuffled blocks (some longer than
+    an 8 KiB tile), a packed size that is not a multiple of 16 (the last tile's tail is
+    read with plain loads), the whole request and a part starting on a 16-byte boundary
+    in the middle of it"""
+    prod = tma
+    rng = np.random.default_rng(seed)
+    nb = 30001
+    blens = rng.integers(1, maxlen, nb)
+    blens[0] += (1 - int(blens.sum()) % 2)          # an odd element count: size % 16 != 0
+    displs = (np.cumsum(blens + rng.integers(0, 9, nb)) - blens) * 4
+    perm = rng.permutation(nb)
+    args = (blens[perm].tolist(), displs[perm].tolist(), yk.TYPE_INT32_T)
+    tp, to = prod.type_create_hindexed(*args), oracle.type_create_hindexed(*args)
+    n = prod.size(tp)
+    assert n % 16
+    lo, hi = _bounds(prod, tp, 1)
+    packed = rng.integers(0, 256, n, dtype=np.uint8)
+    target = rng.integers(0, 256, hi - lo, dtype=np.uint8)
+    pd = dev_copy(cuda, packed)
+    before = _stats(prod)[0]
+    for b0, b1 in ((0, n), (16 * (n // 48), n - 4 * 1001)):
+        th = target.copy()
+        oracle.unpack(packed.ctypes.data + b0, b1 - b0, th.ctypes.data - lo, 1, to, b0)
+        td = dev_copy(cuda, target)
+        prod.unpack(pd.data_ptr() + b0, b1 - b0, td.data_ptr() - lo, 1, tp, b0)
+        cuda.cuda.synchronize()
+        assert np.array_equal(td.cpu().numpy(), th), (b0, b1)
+    assert _stats(prod)[0] - before == 2, "both unpacks took the bulk-staged form"
+    assert _bulk_failures(prod) == 0
+    # outside its rules: a packed pointer off 16 bytes, and a pack, take the other kernels
+    before = _stats(prod)[0]
+    th = target.copy()
+    oracle.unpack(packed.ctypes.data + 4, n - 4, th.ctypes.data - lo, 1, to, 4)
+    td = dev_copy(cuda, target)
+    prod.unpack(pd.data_ptr() + 4, n - 4, td.data_ptr() - lo, 1, tp, 4)
+    out = cuda.zeros(n, dtype=cuda.uint8, device="cuda")
+    prod.pack(dev_copy(cuda, target).data_ptr() - lo, 1, tp, 0, out.data_ptr(), n)
+    cuda.cuda.synchronize()
+    assert np.array_equal(td.cpu().numpy(), th)
+    ph = np.zeros(n, dtype=np.uint8)
+    oracle.pack(target.ctypes.data - lo, 1, to, 0, ph.ctypes.data, n)
+    assert np.array_equal(out.cpu().numpy(), ph)
+    assert _stats(prod)[0] == before
+    prod.type_free(tp)
+    oracle.type_free(to)

@@ -856,6 +856,7 @@ int yaksa_gb300_debug_desc_info(yaksa_type_t type, int typed, int *vec_align, in
 
 void yk_desc_release(yk_type * t)
 {
+    yk_iov_release(t);
     if (t->bytes_desc.dev_tables)
         cudaFree(t->bytes_desc.dev_tables);
     if (t->typed_desc.dev_tables)

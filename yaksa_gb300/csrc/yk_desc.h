@@ -178,18 +178,30 @@ void yk_level_set_magic(yk_level * l);
 
 /* Launch on `stream` (a cudaStream_t).  Returns 0 or a cudaError_t value. */
 int yk_cuda_launch_pup(const yk_launch * l, void *stream);
-/* the same with a launch shape for the REPLACE byte kernels (0, 0 = by size) */
+/* the same with a launch shape: units per thread for the REPLACE byte kernels, and a
+ * grid cap in CTAs per SM for every kernel (0, 0 = the defaults) */
 int yk_cuda_launch_pup_cfg(const yk_launch * l, void *stream, int units_per_thread,
                            int ctas_per_sm);
 
 /* Ordered unpack for types whose targets may overlap: sorted-block owner-computes
  * kernel when the descriptor allows it, otherwise a single-warp ordered kernel. */
-int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blocks, void *stream);
+int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blocks, void *stream,
+                                  int ctas_per_sm);
 
 /* TMA form of a REPLACE launch over a regular nest (yk_tma.cu): 1 when it exists; the
  * launch returns -1 when it does not, else a cudaError_t value. */
 int yk_cuda_tma_ok(const yk_launch * l);
 int yk_cuda_launch_tma(const yk_launch * l, void *stream, int ctas_per_sm);
+
+/* Segment-list expansion (yk_iov_dev.cu): out[k] = (buf + e * extent + tpl[j].off,
+ * tpl[j].len) for piece g = first + k = e * n + j, k < m; with tpl NULL, one piece
+ * (buf + off1, len1).  Returns a cudaError_t value. */
+int yk_cuda_iov_expand(const char *buf, int64_t extent, const int64_t * tpl, uint64_t n, uint64_t first,
+                       uint64_t m, int64_t off1, uint64_t len1, void *out, void *stream);
+
+/* The hindexed unpack with the packed stream staged by bulk copies (yk_kernels.cu): -1
+ * when it does not apply, else a cudaError_t value. */
+int yk_cuda_launch_hidx_bulk(const yk_launch * l, void *stream, int ctas_per_sm);
 
 /* SM count of the current device (cached). */
 int yk_cuda_num_sms(void);

@@ -64,6 +64,13 @@ struct yk_type {
      * whose tables travel in the static device scratch (yaksa_gb300_pup_noalloc) */
     yk_devdesc host_bytes_desc;
     yk_devdesc host_typed_desc;
+    /* segment list of one element (yaksa_gb300_iov_stream), built at its first use:
+     * num_contig (offset, length) pieces on the host and on the device, and which
+     * pieces are the first half of a pair builtin listed as two pieces */
+    int iov_built, iov_status;
+    int64_t *iov_tpl;           /* host: 2 x num_contig words (offset, length) */
+    uint8_t *iov_first;
+    void *iov_dev;              /* device copy of iov_tpl */
 };
 
 typedef struct {
@@ -99,6 +106,8 @@ int yk_noalloc_scratch(void **ptr, size_t * bytes);
 void yk_desc_release(yk_type * t);
 void yk_make_launch_desc(const yk_devdesc * dd, const yk_type * t, uintptr_t count, yk_desc * out);
 uintptr_t yk_builtin_floor(yk_type * t, uintptr_t count, uintptr_t pos);
+/* yk_iov.c: release a type's segment-list template */
+void yk_iov_release(yk_type * t);
 
 /* GPU runtime (yk_runtime.c) */
 int yk_runtime_init(void);

@@ -13,8 +13,15 @@
  *   - every other kind lists its blocks in order, recursing into the child for each
  *     block and skipping zero-length blocks of hindexed and struct types.
  * The walk is host code: it writes the caller's host array and does no data movement.
+ * yaksa_gb300_iov_stream writes the same list into device memory with a kernel, from a
+ * one-element template the walk builds once per type.
  */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#include <cuda_runtime_api.h>
 #include "yk_internal.h"
+#include "yaksa_gb300.h"
 
 int yaksa_iov_len(uintptr_t count, yaksa_type_t type, uintptr_t * iov_len)
 {
@@ -36,6 +43,7 @@ typedef struct {
     uintptr_t room;
     uintptr_t skip;
     uintptr_t n;
+    uint8_t *first;             /* optional: marks the first piece of a two-piece pair */
 } iov_cur;
 
 static int iov_walk(const char *buf, uintptr_t count, const yk_type * t, iov_cur * c);
@@ -93,6 +101,8 @@ static int iov_walk(const char *buf, uintptr_t count, const yk_type * t, iov_cur
                     const char *z = buf + (c->skip / 2) * ext;
                     uintptr_t m = YK_MIN(c->room - 1, count * 2 - c->skip);
                     for (uintptr_t x = 0; x < m; x += 2, z += ext) {
+                        if (c->first)
+                            c->first[c->n] = 1;
                         c->out[c->n].iov_base = (char *) z;
                         c->out[c->n].iov_len = sz[0];
                         c->out[c->n + 1].iov_base = (char *) z + off[1];
@@ -163,10 +173,124 @@ int yaksa_iov(const char *buf, uintptr_t count, yaksa_type_t type, uintptr_t iov
         return YAKSA_ERR__INTERNAL;
     if (max_iov_len == 0)
         return YAKSA_SUCCESS;
-    iov_cur c = { iov, max_iov_len, iov_offset, 0 };
+    iov_cur c = { iov, max_iov_len, iov_offset, 0, NULL };
     int rc = iov_walk(buf, count, t, &c);
     *actual_iov_len = c.n;
     return rc;
+}
+
+/* ------------------------------------------------------------------------- */
+/* segment lists written by the GPU (no counterpart in the reference)          */
+/* ------------------------------------------------------------------------- */
+
+void yk_iov_release(yk_type * t)
+{
+    free(t->iov_tpl);
+    free(t->iov_first);
+    if (t->iov_dev)
+        cudaFree(t->iov_dev);
+    t->iov_tpl = NULL;
+    t->iov_first = NULL;
+    t->iov_dev = NULL;
+    t->iov_built = 0;
+}
+
+/* one element's pieces, relative to the element's address, on the host and the device;
+ * caller holds t->desc_mutex */
+static int iov_template(yk_type * t)
+{
+    const uintptr_t n = t->num_contig;
+    struct iovec *tmp = malloc(sizeof(struct iovec) * (n ? n : 1));
+    t->iov_tpl = malloc(sizeof(int64_t) * 2 * (n ? n : 1));
+    t->iov_first = calloc(n ? n : 1, 1);
+    if (!tmp || !t->iov_tpl || !t->iov_first) {
+        free(tmp);
+        return YAKSA_ERR__OUT_OF_MEM;
+    }
+    iov_cur c = { tmp, n, 0, 0, t->iov_first };
+    int rc = iov_walk((const char *) 0, 1, t, &c);
+    if (!rc && c.n != n)
+        rc = YAKSA_ERR__INTERNAL;
+    for (uintptr_t j = 0; !rc && j < n; j++) {
+        t->iov_tpl[2 * j] = (int64_t) (intptr_t) tmp[j].iov_base;
+        t->iov_tpl[2 * j + 1] = (int64_t) tmp[j].iov_len;
+    }
+    free(tmp);
+    if (rc)
+        return rc;
+    const size_t bytes = sizeof(int64_t) * 2 * n;
+    if (yk_fail_injected() || cudaMalloc(&t->iov_dev, bytes) != cudaSuccess) {
+        t->iov_dev = NULL;
+        return YAKSA_ERR__OUT_OF_MEM;
+    }
+    /* on a private stream, waited for: a kernel already resident must not see it early */
+    cudaStream_t us;
+    cudaError_t e = cudaStreamCreateWithFlags(&us, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+        e = cudaMemcpyAsync(t->iov_dev, t->iov_tpl, bytes, cudaMemcpyHostToDevice, us);
+        cudaError_t e2 = cudaStreamSynchronize(us);
+        if (e == cudaSuccess)
+            e = e2;
+        cudaStreamDestroy(us);
+    }
+    return e == cudaSuccess ? YAKSA_SUCCESS : YAKSA_ERR__INTERNAL;
+}
+
+int yaksa_gb300_iov_stream(const char *buf, uintptr_t count, yaksa_type_t type,
+                           uintptr_t iov_offset, struct iovec *iov, uintptr_t max_iov_len,
+                           uintptr_t * actual_iov_len, void *stream)
+{
+    *actual_iov_len = 0;
+    yk_type *t = yk_type_get(type);
+    if (!t)
+        return YAKSA_ERR__INTERNAL;
+    if (max_iov_len == 0 || count == 0)
+        return YAKSA_SUCCESS;
+    cudaStream_t s = stream ? *(cudaStream_t *) stream : (cudaStream_t) 0;
+    if (t->is_contig) {
+        /* one piece for all `count` elements; as in yaksa_iov, the offset does not apply
+         * inside a contiguous run */
+        int e = yk_cuda_iov_expand(buf, 0, NULL, 1, 0, 1, (int64_t) t->true_lb,
+                                   (uint64_t) (count * t->size), iov, s);
+        if (e) {
+            fprintf(stderr, "yaksa-gb300: segment list launch failed: %s\n",
+                    cudaGetErrorString((cudaError_t) e));
+            return YAKSA_ERR__INTERNAL;
+        }
+        *actual_iov_len = 1;
+        return YAKSA_SUCCESS;
+    }
+    pthread_mutex_lock(&t->desc_mutex);
+    if (!t->iov_built) {
+        t->iov_status = iov_template(t);
+        if (t->iov_status == YAKSA_ERR__OUT_OF_MEM)
+            yk_iov_release(t);          /* allocation failures are retried next time */
+        else
+            t->iov_built = 1;
+    }
+    int rc = t->iov_status;
+    pthread_mutex_unlock(&t->desc_mutex);
+    if (rc)
+        return rc;
+    const uintptr_t n = t->num_contig, total = count * n;
+    if (iov_offset >= total)
+        return YAKSA_SUCCESS;
+    /* a two-piece pair is listed whole: never start on its second piece, never end on
+     * its first (the reference's rule, src/frontend/iov/yaksa_iov.c:12-46) */
+    if (iov_offset % n && t->iov_first[iov_offset % n - 1])
+        return YAKSA_ERR__INTERNAL;
+    uintptr_t m = YK_MIN(max_iov_len, total - iov_offset);
+    if (t->iov_first[(iov_offset + m - 1) % n])
+        m--;
+    int e = yk_cuda_iov_expand(buf, (int64_t) t->extent, (const int64_t *) t->iov_dev, n, iov_offset, m,
+                               0, 0, iov, s);
+    if (e) {
+        fprintf(stderr, "yaksa-gb300: segment list launch failed: %s\n",
+                cudaGetErrorString((cudaError_t) e));
+        return YAKSA_ERR__INTERNAL;
+    }
+    *actual_iov_len = m;
+    return YAKSA_SUCCESS;
 }
 
 /* ------------------------------------------------------------------------- */

@@ -27,6 +27,9 @@
 #define YK_THREADS 256
 #define YK_UNROLL 4
 
+extern "C" int yk_cuda_num_sms(void);
+extern "C" void yk_tma_count_launch(void);
+
 /* address decomposition shared with the host (yk_locate.h) */
 /* ------------------------------------------------------------------------- */
 
@@ -424,6 +427,186 @@ yk_hidx32_kernel(const __grid_constant__ yk_launch L)
             }
         }
     }
+}
+
+
+/* ------------------------------------------------------------------------- */
+/* hindexed unpack with the packed stream staged by bulk copies               */
+/* ------------------------------------------------------------------------- */
+
+/* The unpack of a contiguous-block hindexed request reads the packed stream in order,
+ * so that side can move as whole tiles: one elected thread issues cp.async.bulk of the
+ * next YK_HB_STAGES tiles (8 KiB each) into shared memory, completion counted by one
+ * mbarrier per stage, and the CTA's warps scatter the current tile to the typed side
+ * with the shuffle search of yk_hidx32_kernel (lane k holds block k's start relative to
+ * the group and its typed offset).  The loads cost no registers, so each SM keeps tens
+ * of KiB of packed bytes in flight instead of one vector per lane.  The packed pointer
+ * sits on 16 bytes (checked on the host); the last tile's bytes past its last 16-byte
+ * boundary are read with plain loads, so nothing beyond the request is read.  Every
+ * wait is bounded: a CTA that runs out counts a failure in yk_hb_failures, waits
+ * (bounded) for its copies in flight and leaves. */
+#define YK_HB_TILE 8192
+#define YK_HB_STAGES 3
+#define YK_HB_SPINS (1u << 24)
+
+__device__ unsigned int yk_hb_failures;
+
+__device__ __forceinline__ uint32_t yk_hb_smem(const void *p) { return (uint32_t) __cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ bool yk_hb_try(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile ("{\n\t.reg .pred p;\n\t"
+                  "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                  "selp.u32 %0, 1, 0, p;\n}" : "=r"(ok) : "r"(yk_hb_smem(bar)), "r"(parity) : "memory");
+    return ok != 0;
+}
+
+__device__ __forceinline__ bool yk_hb_wait(uint64_t *bar, uint32_t parity)
+{
+    for (uint32_t i = 0; i < YK_HB_SPINS; i++)
+        if (yk_hb_try(bar, parity))
+            return true;
+    return false;
+}
+
+/* thread 0: tile t (packed bytes [t * TILE, ...) of the request) into stage k */
+__device__ __forceinline__ void yk_hb_issue(const yk_launch & L, uint32_t t, unsigned char *stage,
+                                            uint64_t *bar)
+{
+    const uint64_t q0 = (uint64_t) t * YK_HB_TILE;
+    const uint32_t bytes = (uint32_t) min((uint64_t) YK_HB_TILE, L.nbytes - q0);
+    const uint32_t bulk = bytes & ~15u;
+    asm volatile ("{\n\t.reg .b64 st;\n\t"
+                  "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n}"
+                  :: "r"(yk_hb_smem(bar)), "r"(bulk) : "memory");
+    if (bulk)
+        asm volatile ("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                      :: "r"(yk_hb_smem(stage)), "l"(L.packed + q0), "r"(bulk), "r"(yk_hb_smem(bar))
+                      : "memory");
+}
+
+template <int V>
+__global__ void __launch_bounds__(YK_THREADS, 4)
+yk_hidx_unpack_bulk_kernel(const __grid_constant__ yk_launch L)
+{
+    typedef typename yk_vec<V>::T VT;
+    extern __shared__ __align__(128) unsigned char yk_hb_tiles[];
+    __shared__ __align__(8) uint64_t bar[YK_HB_STAGES];
+    __shared__ int s_ok;
+    const yk_level *lv = &L.desc.lv[0];
+    const uint64_t p0 = L.p0, n = L.nbytes;
+    const uint32_t ntiles = (uint32_t) ((n + YK_HB_TILE - 1) / YK_HB_TILE);
+    char *typed = L.typed + L.desc.base;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (threadIdx.x == 0) {
+        for (int k = 0; k < YK_HB_STAGES; k++)
+            asm volatile ("mbarrier.init.shared::cta.b64 [%0], 1;" :: "r"(yk_hb_smem(&bar[k])) : "memory");
+        asm volatile ("fence.mbarrier_init.release.cluster;" ::: "memory");
+        for (int k = 0; k < YK_HB_STAGES; k++) {
+            const uint32_t t = blockIdx.x + (uint32_t) k * gridDim.x;
+            if (t < ntiles)
+                yk_hb_issue(L, t, yk_hb_tiles + (size_t) k * YK_HB_TILE, &bar[k]);
+        }
+    }
+    __syncthreads();
+    uint32_t phase = 0;         /* bit k: the parity stage k waits for next */
+    bool failed = false;
+    int k = 0;
+    for (uint32_t t = blockIdx.x; t < ntiles; t += gridDim.x, k = (k + 1 == YK_HB_STAGES) ? 0 : k + 1) {
+        unsigned char *tile = yk_hb_tiles + (size_t) k * YK_HB_TILE;
+        const uint64_t q0 = (uint64_t) t * YK_HB_TILE;
+        const uint32_t bytes = (uint32_t) min((uint64_t) YK_HB_TILE, n - q0);
+        if (threadIdx.x == 0) {
+            s_ok = yk_hb_wait(&bar[k], (phase >> k) & 1);
+            /* the bytes past the last 16-byte boundary (last tile only), plain loads */
+            for (uint32_t b = bytes & ~15u; s_ok && b < bytes; b++)
+                tile[b] = (unsigned char) L.packed[q0 + b];
+        }
+        __syncthreads();
+        if (!s_ok) {
+            failed = true;
+            break;
+        }
+        (void) yk_hb_try(&bar[k], (phase >> k) & 1);      /* observe the completed phase */
+        phase ^= 1u << k;
+        /* the blocks that intersect the tile, in groups of 32 per warp */
+        const uint64_t a = p0 + q0, e = a + bytes;
+        const uint64_t jb = yk_hidx_block(lv, a), je = yk_hidx_block(lv, e - 1);
+        const uint64_t ngroups = (je - jb + 32) / 32;
+        for (uint64_t g = (uint64_t) warp; g < ngroups; g += YK_THREADS / 32) {
+            const uint64_t j0 = jb + g * 32, jl = j0 + (uint64_t) lane;
+            const uint64_t jend = min(j0 + 32, je + 1);
+            const uint64_t gs = max(__ldg(lv->pfx + j0), a);
+            const uint32_t ng = (uint32_t) (min(__ldg(lv->pfx + jend), e) - gs);
+            uint32_t my_rel = 0xffffffffu;
+            int64_t my_adj = 0;
+            if (jl < jend) {
+                const uint64_t bp = __ldg(lv->pfx + jl);
+                my_rel = bp <= gs ? 0u : (uint32_t) (bp - gs);
+                my_adj = __ldg(lv->disp + jl) - ((int64_t) bp - (int64_t) gs);
+            }
+            const unsigned char *src = tile + (gs - a);
+            for (uint32_t base = 0; base < ng; base += 32u * V * YK_HW_UNROLL) {
+#pragma unroll
+                for (int u = 0; u < YK_HW_UNROLL; u++) {
+                    const uint32_t r = base + (uint32_t) (u * 32 + lane) * V;
+                    int idx = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1) {
+                        const uint32_t c = __shfl_sync(0xffffffffu, my_rel, idx + step);
+                        if (c <= r)
+                            idx += step;
+                    }
+                    const int64_t off = __shfl_sync(0xffffffffu, my_adj, idx) + (int64_t) r;
+                    if (r < ng)
+                        *(VT *) (typed + off) = *(const VT *) (src + r);
+                }
+            }
+        }
+        /* every warp is done with this stage: refill it with the tile STAGES ahead */
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            const uint32_t tn = t + (uint32_t) YK_HB_STAGES * gridDim.x;
+            if (tn < ntiles) {
+                asm volatile ("fence.proxy.async.shared::cta;" ::: "memory");
+                yk_hb_issue(L, tn, tile, &bar[k]);
+            }
+        }
+    }
+    if (failed && threadIdx.x == 0) {
+        atomicAdd(&yk_hb_failures, 1u);
+        for (int j = 0; j < YK_HB_STAGES; j++)
+            (void) yk_hb_wait(&bar[j], (phase >> j) & 1);
+    }
+}
+
+/* the bulk-staged unpack of a contiguous-block hindexed request: -1 when it does not
+ * apply (not an unpack, packed pointer off 16 bytes, 4 GiB or more), else a cudaError_t */
+extern "C" int yk_cuda_launch_hidx_bulk(const yk_launch * l, void *stream, int ctas_per_sm)
+{
+    if (l->typed_op || !l->hidx || l->dir != 1 || ((uintptr_t) l->packed & 15) ||
+        l->nbytes == 0 || l->nbytes > 0xffffffffull)
+        return -1;
+    yk_tma_count_launch();
+    const uint64_t ntiles = (l->nbytes + YK_HB_TILE - 1) / YK_HB_TILE;
+    const uint64_t cap = (uint64_t) yk_cuda_num_sms() * (uint64_t) (ctas_per_sm > 0 ? ctas_per_sm : 4);
+    const unsigned g = (unsigned) (ntiles < cap ? ntiles : cap);
+    const size_t smem = (size_t) YK_HB_STAGES * YK_HB_TILE;
+    cudaStream_t s = (cudaStream_t) stream;
+    switch (l->vec) {
+        case 16: yk_hidx_unpack_bulk_kernel<16><<<g, YK_THREADS, smem, s>>>(*l); break;
+        case 8: yk_hidx_unpack_bulk_kernel<8><<<g, YK_THREADS, smem, s>>>(*l); break;
+        case 4: yk_hidx_unpack_bulk_kernel<4><<<g, YK_THREADS, smem, s>>>(*l); break;
+        case 2: yk_hidx_unpack_bulk_kernel<2><<<g, YK_THREADS, smem, s>>>(*l); break;
+        default: yk_hidx_unpack_bulk_kernel<1><<<g, YK_THREADS, smem, s>>>(*l); break;
+    }
+    return (int) cudaGetLastError();
+}
+
+extern "C" int yaksa_gb300_debug_bulk_failures(unsigned int *n)
+{
+    return cudaMemcpyFromSymbol(n, yk_hb_failures, sizeof(unsigned int)) == cudaSuccess ? 0 : 2;
 }
 
 
@@ -1662,7 +1845,7 @@ extern "C" int yk_cuda_launch_pup_cfg(const yk_launch * l, void *stream, int uni
         /* one warp per group of 32 blocks, 8 warps per CTA */
         uint64_t groups = (l->desc.lv[0].count + 31) / 32;
         uint64_t ctas = (groups + (YK_THREADS / 32) - 1) / (YK_THREADS / 32);
-        uint64_t cap = (uint64_t) yk_cuda_num_sms() * 8u;
+        uint64_t cap = (uint64_t) yk_cuda_num_sms() * (uint64_t) (ctas_per_sm > 0 ? ctas_per_sm : 8);
         unsigned g = (unsigned) (ctas < cap ? (ctas ? ctas : 1) : cap);
 #define YK_H(V) do { if (l->nbytes <= 0xffffffffull) {                                     \
                          if (l->dir == 0) yk_hidx32_kernel<V, 0><<<g, YK_THREADS, 0, s>>>(*l); \
@@ -1685,7 +1868,7 @@ extern "C" int yk_cuda_launch_pup_cfg(const yk_launch * l, void *stream, int uni
     } else {
         const yk_launch & c = *l;
         uint64_t units = c.nbytes / (uint64_t) c.vec;
-        unsigned g = yk_grid(units, YK_THREADS, 16);
+        unsigned g = yk_grid(units, YK_THREADS, ctas_per_sm > 0 ? ctas_per_sm : 16);
         if (c.use64) {
             if (c.dir == 0)
                 yk_typed_kernel<uint64_t, 0><<<g, YK_THREADS, 0, s>>>(c);
@@ -1758,7 +1941,7 @@ static bool yk_owner_lane_cplx(const yk_launch & c, int rshift, cudaStream_t s, 
     return false;
 }
 
-static bool yk_owner_lane_launch(const yk_launch & c, int bt, int rshift, cudaStream_t s)
+static bool yk_owner_lane_launch(const yk_launch & c, int bt, int rshift, cudaStream_t s, int cap)
 {
     const uint64_t es = (uint64_t) yk_bt_size(bt);
     /* chunks of CW bytes: blocks a multiple of CW bytes, range and packed pointer on CW
@@ -1776,7 +1959,7 @@ static bool yk_owner_lane_launch(const yk_launch & c, int bt, int rshift, cudaSt
                 chunk = cw;
     }
     const uint64_t units = c.nbytes / (chunk ? (uint64_t) chunk : es);
-    const unsigned g = yk_grid(units, YK_THREADS, 16);
+    const unsigned g = yk_grid(units, YK_THREADS, cap > 0 ? cap : 16);
     switch (bt) {
         case YK_BT_I8: return yk_owner_lane_int<YK_BT_I8>(c, rshift, s, g, chunk);
         case YK_BT_I16: return yk_owner_lane_int<YK_BT_I16>(c, rshift, s, g, chunk);
@@ -1802,7 +1985,8 @@ extern "C" int yk_cuda_launch_runs_pack(const yk_launch * l, uint32_t run, void 
     return (int) cudaGetLastError();
 }
 
-extern "C" int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blocks, void *stream)
+extern "C" int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blocks, void *stream,
+                                             int ctas_per_sm)
 {
     cudaStream_t s = (cudaStream_t) stream;
     if (l->nbytes == 0)
@@ -1816,11 +2000,12 @@ extern "C" int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blo
     int rshift = 0;
     while (rshift < 31 && (1ull << rshift) < R)
         rshift++;
-    if (typed_ok && !c.use64 && (1ull << rshift) == R && yk_owner_lane_launch(c, bt, rshift, s)) {
+    if (typed_ok && !c.use64 && (1ull << rshift) == R &&
+        yk_owner_lane_launch(c, bt, rshift, s, ctas_per_sm)) {
         /* launched: power-of-two blocks, operator in the type's table */
     } else if (typed_ok) {
         uint64_t units = c.nbytes / (uint64_t) yk_bt_size(bt);
-        unsigned g = yk_grid(units, YK_THREADS * 4, 8);
+        unsigned g = yk_grid(units, YK_THREADS * 4, ctas_per_sm > 0 ? ctas_per_sm : 8);
 #define YK_OT(IDX) do { switch (bt) {                                                          \
             case YK_BT_I8: yk_owner_typed_kernel<IDX, YK_BT_I8, 4><<<g, YK_THREADS, 0, s>>>(c); break;   \
             case YK_BT_I16: yk_owner_typed_kernel<IDX, YK_BT_I16, 4><<<g, YK_THREADS, 0, s>>>(c); break; \
@@ -1838,7 +2023,7 @@ extern "C" int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blo
 #undef YK_OT
     } else if (sorted_blocks) {
         uint64_t units = c.nbytes / (uint64_t) c.vec;
-        unsigned g = yk_grid(units, YK_THREADS, 16);
+        unsigned g = yk_grid(units, YK_THREADS, ctas_per_sm > 0 ? ctas_per_sm : 16);
         if (c.use64)
             yk_owner_kernel<uint64_t><<<g, YK_THREADS, 0, s>>>(c);
         else

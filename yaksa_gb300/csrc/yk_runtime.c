@@ -570,12 +570,31 @@ static int launch_prepared(const yk_plan * p, const yk_launch * L, int kind, int
                                         cudaMemcpyDefault, s), "cudaMemcpyAsync");
     }
     __atomic_add_fetch(&R.launches, 1, __ATOMIC_RELAXED);
-    if (kind == YK_X_ORDERED)
-        return cuda_err((cudaError_t) yk_cuda_launch_unpack_ordered(L, sorted, s), "kernel launch");
-    const int runs = kind == YK_X_BYTES && runs_pack_ok(L);
     const uint64_t units = L->nbytes / (uint64_t) L->vec;
+    if (kind == YK_X_ORDERED || kind == YK_X_TYPED || (kind == YK_X_BYTES && L->hidx)) {
+        /* the grid cap of the hindexed, typed-operator and sorted-block kernels; the class
+         * is keyed by operator and base type as well */
+        yk_tune_cfg cfg = { 0, 0, 0 };
+        int probe = -1;
+        const int fam = kind == YK_X_ORDERED ? YK_TUNE_OWNER : kind == YK_X_TYPED ? YK_TUNE_TYPED :
+            L->dir == 1 ? YK_TUNE_HIDX_UNPACK : YK_TUNE_HIDX;
+        if (fam == YK_TUNE_HIDX_UNPACK && R.tma_mode == 2)
+            cfg.variant = YK_VARIANT_BULK;      /* the test hook forces the bulk form */
+        else if (tune && (kind != YK_X_ORDERED || sorted))
+            probe = yk_tune_begin(yk_tune_key(fam, (int) L->op, L->desc.leaf_type * 17 + L->vec, L->dir,
+                                              L->use64, units), fam, units, s, &cfg);
+        int e = -1;
+        if (cfg.variant == YK_VARIANT_BULK && R.tma_mode)
+            e = yk_cuda_launch_hidx_bulk(L, s, cfg.ctas_per_sm);   /* -1: it does not apply */
+        if (e == -1)
+            e = kind == YK_X_ORDERED ? yk_cuda_launch_unpack_ordered(L, sorted, s, cfg.ctas_per_sm) :
+                yk_cuda_launch_pup_cfg(L, s, 0, cfg.ctas_per_sm);
+        yk_tune_end(probe, s);
+        return cuda_err((cudaError_t) e, "kernel launch");
+    }
+    const int runs = kind == YK_X_BYTES && runs_pack_ok(L);
     /* a TMA form competes as a candidate of the autotuner (or is forced by the test hook) */
-    const int tma = kind == YK_X_BYTES && !L->hidx && R.tma_mode &&
+    const int tma = kind == YK_X_BYTES && R.tma_mode &&
         (R.tma_mode == 2 || (tune && units >= yk_tune_min_units())) && yk_cuda_tma_ok(L);
     if (tma && R.tma_mode == 2) {
         int e = yk_cuda_launch_tma(L, s, 0);
@@ -587,7 +606,7 @@ static int launch_prepared(const yk_plan * p, const yk_launch * L, int kind, int
                         "kernel launch");
     yk_tune_cfg cfg = { 0, 0, runs ? YK_VARIANT_RUNS : YK_VARIANT_BYTES };
     int probe = -1;
-    if (tune && kind == YK_X_BYTES && !L->hidx) {
+    if (tune && kind == YK_X_BYTES) {
         const int fam = runs ? YK_TUNE_RUNS_TMA : tma ? YK_TUNE_SINGLE_TMA : YK_TUNE_SINGLE;
         probe = yk_tune_begin(yk_tune_key(fam, L->regular, L->vec, L->dir, L->use64, units), fam,
                               units, s, &cfg);

@@ -346,6 +346,13 @@ extern "C" int yk_cuda_tma_ok(const yk_launch * l)
 
 static unsigned long long yk_tma_launches;
 
+/* launches of the forms that move data with the tensor memory accelerator (tensor maps
+ * here, and the bulk-staged hindexed unpack) */
+extern "C" void yk_tma_count_launch(void)
+{
+    __atomic_add_fetch(&yk_tma_launches, 1ull, __ATOMIC_RELAXED);
+}
+
 extern "C" int yk_cuda_num_sms(void);
 
 /* Launch the TMA form with ctas_per_sm resident CTAs per SM (0: 4); returns a
@@ -367,7 +374,8 @@ extern "C" int yk_cuda_launch_tma(const yk_launch * l, void *stream, int ctas_pe
     return (int) cudaGetLastError();
 }
 
-/* TMA launches so far, and TMA waits that ran out (0 in correct operation) */
+/* launches of the TMA-unit forms so far, and tensor-map waits that ran out (0 in
+ * correct operation) */
 extern "C" int yaksa_gb300_debug_tma_stats(unsigned long long *launches, unsigned int *failures)
 {
     *launches = __atomic_load_n(&yk_tma_launches, __ATOMIC_RELAXED);

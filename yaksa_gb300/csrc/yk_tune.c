@@ -13,7 +13,17 @@
  * capture, small launches and YAKSA_GB300_AUTOTUNE=0 use the decided (or default)
  * shape without timing.  No reference counterpart: the reference fixes its launch
  * shape (src/backend/cuda/pup/yaksuri_cudai_pup.c:20-48).
+ *
+ * Families: the REPLACE byte/regular kernels (units per thread x CTAs per SM, and the
+ * TMA or one-element-per-thread forms where they exist), batches, and the grid cap of
+ * the hindexed, typed-operator and sorted-block kernels.
+ *
+ * Decisions persist when YAKSA_GB300_TUNE_FILE names a file: each decided class is
+ * appended as one line "<device> <class key> <units per thread> <CTAs per SM> <variant>",
+ * the device being the GPU's name and SM count, and a later process on the same kind of
+ * GPU starts with those classes decided (no timed launches for them).
  */
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include <pthread.h>
@@ -38,6 +48,15 @@ static const yk_tune_cfg cand_single_tma[] = { {0, 0, 0}, {1, 64, 0}, {4, 8, 0},
     {1, 16, 0}, {0, 4, YK_VARIANT_TMA}, {0, 8, YK_VARIANT_TMA} };
 static const yk_tune_cfg cand_runs_tma[] = { {0, 0, YK_VARIANT_RUNS}, {0, 4, YK_VARIANT_TMA},
     {0, 8, YK_VARIANT_TMA} };
+/* grid caps of the hindexed shuffle-search kernel (default 8 CTAs per SM), the typed
+ * operator kernel and the sorted-block kernels (default 16) */
+static const yk_tune_cfg cand_hidx[] = { {0, 0, 0}, {0, 5, 0}, {0, 12, 0}, {0, 16, 0} };
+/* hindexed unpacks: also the bulk-staged form at 2, 4 and 6 CTAs per SM */
+static const yk_tune_cfg cand_hidx_unpack[] = { {0, 0, 0}, {0, 5, 0}, {0, 12, 0},
+    {0, 2, YK_VARIANT_BULK}, {0, 4, YK_VARIANT_BULK}, {0, 6, YK_VARIANT_BULK} };
+static const yk_tune_cfg cand_grid16[] = { {0, 0, 0}, {0, 8, 0}, {0, 32, 0} };
+
+#define YK_TUNE_PRELOAD 1024
 
 typedef struct {
     uint64_t key;               /* 0: empty */
@@ -55,13 +74,87 @@ typedef struct {
     int armed;                  /* e1 recorded after that launch: may be read */
 } probe_t;
 
+typedef struct {
+    uint64_t key;
+    yk_tune_cfg cfg;
+} preload_t;
+
 static struct {
     pthread_mutex_t mu;
     int init, enabled;
     slot_t slots[YK_TUNE_SLOTS];
     probe_t probes[YK_TUNE_PROBES];
     uint64_t nprobes;
-} T = { PTHREAD_MUTEX_INITIALIZER, 0, 0, {{0}}, {{0}}, 0 };
+    char file[512];             /* decisions file (empty: not persisted) */
+    char device[288];           /* "<name>/<SMs>" with spaces as '_' */
+    preload_t pre[YK_TUNE_PRELOAD];
+    int npre;
+    uint32_t loaded;            /* classes decided from the file */
+} T = { .mu = PTHREAD_MUTEX_INITIALIZER };
+
+static const yk_tune_cfg *family_cands(int family, int *n)
+{
+#define YK_C(a) (*n = (int) (sizeof(a) / sizeof(a[0])), a)
+    switch (family) {
+        case YK_TUNE_SINGLE: return YK_C(cand_single);
+        case YK_TUNE_SINGLE_TMA: return YK_C(cand_single_tma);
+        case YK_TUNE_RUNS_TMA: return YK_C(cand_runs_tma);
+        case YK_TUNE_BATCH_REGULAR: return YK_C(cand_batch_regular);
+        case YK_TUNE_HIDX: return YK_C(cand_hidx);
+        case YK_TUNE_HIDX_UNPACK: return YK_C(cand_hidx_unpack);
+        case YK_TUNE_TYPED: case YK_TUNE_OWNER: return YK_C(cand_grid16);
+        default: return YK_C(cand_batch);
+    }
+#undef YK_C
+}
+
+static void persist_locked(const slot_t * s)
+{
+    if (!T.file[0])
+        return;
+    FILE *f = fopen(T.file, "a");
+    if (!f)
+        return;
+    const yk_tune_cfg *c = &s->cand[s->best];
+    fprintf(f, "%s %llx %d %d %d\n", T.device, (unsigned long long) s->key, c->units_per_thread,
+            c->ctas_per_sm, c->variant);
+    fclose(f);
+}
+
+static void load_locked(void)
+{
+    const char *fn = getenv("YAKSA_GB300_TUNE_FILE");
+    if (!fn || !fn[0] || strlen(fn) >= sizeof(T.file))
+        return;
+    strcpy(T.file, fn);
+    int dev = 0;
+    struct cudaDeviceProp pr;
+    if (cudaGetDevice(&dev) != cudaSuccess || cudaGetDeviceProperties(&pr, dev) != cudaSuccess) {
+        cudaGetLastError();
+        T.file[0] = 0;
+        return;
+    }
+    snprintf(T.device, sizeof(T.device), "%s/%d", pr.name, pr.multiProcessorCount);
+    for (char *c = T.device; *c; c++)
+        if (*c == ' ')
+            *c = '_';
+    FILE *f = fopen(T.file, "r");
+    if (!f)
+        return;
+    char line[640], devname[288];
+    unsigned long long key;
+    int u, c, v;
+    while (fgets(line, sizeof(line), f) && T.npre < YK_TUNE_PRELOAD)
+        if (sscanf(line, "%287s %llx %d %d %d", devname, &key, &u, &c, &v) == 5 &&
+            !strcmp(devname, T.device) && key) {
+            T.pre[T.npre].key = key;
+            T.pre[T.npre].cfg.units_per_thread = u;
+            T.pre[T.npre].cfg.ctas_per_sm = c;
+            T.pre[T.npre].cfg.variant = v;
+            T.npre++;
+        }
+    fclose(f);
+}
 
 static int log2u(uint64_t v)
 {
@@ -73,7 +166,7 @@ static int log2u(uint64_t v)
 
 uint64_t yk_tune_key(int family, int depth, int vec, int dir, int wide, uint64_t units)
 {
-    /* nonzero by construction: family is 1..5 */
+    /* nonzero by construction: family is 1..9 */
     return ((uint64_t) family << 32) | ((uint64_t) (depth + 1) << 24) |
         ((uint64_t) vec << 16) | ((uint64_t) dir << 12) | ((uint64_t) wide << 8) |
         (uint64_t) log2u(units);
@@ -106,6 +199,7 @@ static void drain_locked(void)
                         s->fastest[c] < s->fastest[b])
                         b = c;
                 s->best = b;
+                persist_locked(s);
             }
         } else {
             cudaGetLastError();
@@ -121,6 +215,8 @@ static void init_locked(void)
     const char *e = getenv("YAKSA_GB300_AUTOTUNE");
     T.enabled = !(e && e[0] == '0');
     T.init = 1;
+    if (T.enabled)
+        load_locked();
 }
 
 static slot_t *slot_locked(uint64_t key, int family)
@@ -134,22 +230,16 @@ static slot_t *slot_locked(uint64_t key, int family)
             memset(s, 0, sizeof(*s));
             s->key = key;
             s->best = -1;
-            if (family == YK_TUNE_SINGLE) {
-                s->cand = cand_single;
-                s->ncand = (int) (sizeof(cand_single) / sizeof(cand_single[0]));
-            } else if (family == YK_TUNE_SINGLE_TMA) {
-                s->cand = cand_single_tma;
-                s->ncand = (int) (sizeof(cand_single_tma) / sizeof(cand_single_tma[0]));
-            } else if (family == YK_TUNE_RUNS_TMA) {
-                s->cand = cand_runs_tma;
-                s->ncand = (int) (sizeof(cand_runs_tma) / sizeof(cand_runs_tma[0]));
-            } else if (family == YK_TUNE_BATCH_REGULAR) {
-                s->cand = cand_batch_regular;
-                s->ncand = (int) (sizeof(cand_batch_regular) / sizeof(cand_batch_regular[0]));
-            } else {
-                s->cand = cand_batch;
-                s->ncand = (int) (sizeof(cand_batch) / sizeof(cand_batch[0]));
-            }
+            s->cand = family_cands(family, &s->ncand);
+            /* a decision from the file, if it names one of this family's candidates */
+            for (int i = T.npre - 1; i >= 0 && s->best < 0; i--)
+                if (T.pre[i].key == key)
+                    for (int c = 0; c < s->ncand; c++)
+                        if (!memcmp(&s->cand[c], &T.pre[i].cfg, sizeof(yk_tune_cfg))) {
+                            s->best = c;
+                            T.loaded++;
+                            break;
+                        }
             return s;
         }
     }
@@ -159,9 +249,8 @@ static slot_t *slot_locked(uint64_t key, int family)
 int yk_tune_begin(uint64_t key, int family, uint64_t units, void *stream, yk_tune_cfg * cfg)
 {
     cudaStream_t st = (cudaStream_t) stream;
-    cfg->units_per_thread = family == YK_TUNE_BATCH_REGULAR ? 1 : 0;
-    cfg->ctas_per_sm = 0;
-    cfg->variant = family == YK_TUNE_RUNS_TMA ? YK_VARIANT_RUNS : YK_VARIANT_BYTES;
+    int nc;
+    *cfg = family_cands(family, &nc)[0];        /* the default shape */
     pthread_mutex_lock(&T.mu);
     init_locked();
     if (!T.enabled || units < YK_TUNE_MIN_UNITS) {
@@ -253,6 +342,9 @@ void yk_tune_reset(void)
     memset(T.slots, 0, sizeof(T.slots));
     T.nprobes = 0;
     T.init = 0;
+    T.npre = 0;
+    T.loaded = 0;
+    T.file[0] = 0;
     pthread_mutex_unlock(&T.mu);
 }
 

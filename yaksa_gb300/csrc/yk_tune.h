@@ -7,9 +7,11 @@
 /* SINGLE_TMA: a single launch that also has a TMA form; RUNS_TMA: a struct-like pack
  * (one element per thread) that also has a TMA form */
 enum { YK_TUNE_SINGLE = 1, YK_TUNE_BATCH_REGULAR = 2, YK_TUNE_BATCH = 3, YK_TUNE_SINGLE_TMA = 4,
-    YK_TUNE_RUNS_TMA = 5 };
+    YK_TUNE_RUNS_TMA = 5, YK_TUNE_HIDX = 6, YK_TUNE_TYPED = 7, YK_TUNE_OWNER = 8,
+    YK_TUNE_HIDX_UNPACK = 9 };
 
-enum { YK_VARIANT_BYTES = 0, YK_VARIANT_TMA = 1, YK_VARIANT_RUNS = 2 };
+/* BULK: the hindexed unpack with the packed stream staged by cp.async.bulk */
+enum { YK_VARIANT_BYTES = 0, YK_VARIANT_TMA = 1, YK_VARIANT_RUNS = 2, YK_VARIANT_BULK = 3 };
 
 typedef struct {
     int units_per_thread;       /* 1 or 4; 0 = chosen by size */
