@@ -53,7 +53,7 @@ enum {
     YK_BT_I8, YK_BT_I16, YK_BT_I32, YK_BT_I64,
     YK_BT_F32, YK_BT_F64,
     YK_BT_C32, YK_BT_C64,       /* float / double complex */
-    YK_BT_LDOUBLE, YK_BT_CLDOUBLE,      /* REPLACE only on the GPU */
+    YK_BT_LDOUBLE, YK_BT_CLDOUBLE,      /* binary128 on the GPU (yk_quad.h) */
     YK_BT_LAST
 };
 
@@ -103,6 +103,8 @@ typedef struct {
     int32_t regular;            /* 0..YK_REGULAR_MAX: that many VEC levels over a RUN leaf
                                  * with 32-bit positions; -1: any other shape */
     int32_t hidx;               /* 1: one HIDX level of contiguous blocks over its run */
+    int32_t ldouble;            /* 1: the type holds long double (binary128 operators) */
+    int32_t pad_ld;
 } yk_launch;
 
 #define YK_REGULAR_MAX 3

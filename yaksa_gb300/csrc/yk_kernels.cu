@@ -23,6 +23,7 @@
 #include <stdint.h>
 #include "yk_desc.h"
 #include "yk_locate.h"
+#include "yk_quad.h"
 
 #define YK_THREADS 256
 #define YK_UNROLL 4
@@ -360,9 +361,11 @@ yk_hidx_kernel(const __grid_constant__ yk_launch L)
  * state small enough for every warp slot of the SM to stay resident.  Lane k keeps its
  * block's start relative to the group (0 for a block that starts before the range) and
  * the typed offset of relative position 0 in that block, so a unit's typed offset is one
- * shuffle and one add. */
-template <int V, int DIR>
-__global__ void __launch_bounds__(YK_THREADS, 6)
+ * shuffle and one add.  U units per lane are in flight at once and MINB CTAs of the
+ * block size are meant to stay resident; the autotuner chooses among three shapes for
+ * 4- and 8-byte units (latency hiding by loads per lane against warps per SM). */
+template <int V, int DIR, int U, int MINB>
+__global__ void __launch_bounds__(YK_THREADS, MINB)
 yk_hidx32_kernel(const __grid_constant__ yk_launch L)
 {
     typedef typename yk_vec<V>::T VT;
@@ -388,11 +391,11 @@ yk_hidx32_kernel(const __grid_constant__ yk_launch L)
             my_adj = __ldg(lv->disp + jl) - ((int64_t) bp - (int64_t) gs);
         }
         VT *pk = (VT *) (L.packed + (gs - p0));
-        for (uint32_t base = 0; base < n; base += 32u * V * YK_HW_UNROLL) {
-            int64_t off[YK_HW_UNROLL];
-            bool act[YK_HW_UNROLL];
+        for (uint32_t base = 0; base < n; base += 32u * V * U) {
+            int64_t off[U];
+            bool act[U];
 #pragma unroll
-            for (int k = 0; k < YK_HW_UNROLL; k++) {
+            for (int k = 0; k < U; k++) {
                 const uint32_t r = base + (uint32_t) (k * 32 + lane) * V;
                 act[k] = r < n;
                 int idx = 0;
@@ -405,23 +408,23 @@ yk_hidx32_kernel(const __grid_constant__ yk_launch L)
                 off[k] = __shfl_sync(0xffffffffu, my_adj, idx) + (int64_t) r;
             }
             if (DIR == 0) {
-                VT v[YK_HW_UNROLL];
+                VT v[U];
 #pragma unroll
-                for (int k = 0; k < YK_HW_UNROLL; k++)
+                for (int k = 0; k < U; k++)
                     if (act[k])
                         v[k] = yk_ldcg((const VT *) (typed + off[k]));
 #pragma unroll
-                for (int k = 0; k < YK_HW_UNROLL; k++)
+                for (int k = 0; k < U; k++)
                     if (act[k])
                         pk[base / V + (uint32_t) (k * 32 + lane)] = v[k];
             } else {
-                VT v[YK_HW_UNROLL];
+                VT v[U];
 #pragma unroll
-                for (int k = 0; k < YK_HW_UNROLL; k++)
+                for (int k = 0; k < U; k++)
                     if (act[k])
                         v[k] = yk_ldcg(pk + base / V + (uint32_t) (k * 32 + lane));
 #pragma unroll
-                for (int k = 0; k < YK_HW_UNROLL; k++)
+                for (int k = 0; k < U; k++)
                     if (act[k])
                         *(VT *) (typed + off[k]) = v[k];
             }
@@ -859,7 +862,62 @@ __device__ __forceinline__ bool yk_cplx_op(int op, const F in[2], F out[2])
     return false;
 }
 
-/* apply op to one element of base type bt; `dst` is updated in place from `src` */
+__device__ __forceinline__ yk_u128 yk_ldq(const char *p)
+{
+    return ((yk_u128) yk_ld<uint64_t>(p + 8) << 64) | (yk_u128) yk_ld<uint64_t>(p);
+}
+
+__device__ __forceinline__ void yk_stq(char *p, yk_u128 v)
+{
+    yk_st<uint64_t>(p, (uint64_t) v);
+    yk_st<uint64_t>(p + 8, (uint64_t) (v >> 64));
+}
+
+/* long double and long double complex in binary128: `out = out op in` as the
+ * reference's seq loops compute it (MAX and MIN are the selects of the float types) */
+__device__ __forceinline__ void yk_q_apply(int bt, int op, char *dst, const char *src)
+{
+    if (bt == YK_BT_LDOUBLE) {
+        const yk_u128 in = yk_ldq(src), out = yk_ldq(dst);
+        yk_u128 r;
+        switch (op) {
+            case OP_REPLACE: r = in; break;
+            case OP_MAX: r = yk_q_lt(in, out) ? out : in; break;
+            case OP_MIN: r = yk_q_lt(out, in) ? out : in; break;
+            case OP_SUM: r = yk_q_add(out, in); break;
+            case OP_PROD: r = yk_q_mul(out, in); break;
+            default: return;
+        }
+        yk_stq(dst, r);
+        return;
+    }
+    const yk_u128 ir = yk_ldq(src), ii = yk_ldq(src + 16);
+    yk_u128 orr = yk_ldq(dst), oi = yk_ldq(dst + 16);
+    switch (op) {
+        case OP_REPLACE:
+            orr = ir;
+            oi = ii;
+            break;
+        case OP_SUM:
+            orr = yk_q_add(orr, ir);
+            oi = yk_q_add(oi, ii);
+            break;
+        case OP_PROD:
+            yk_q_cmul(orr, oi, ir, ii, &orr, &oi);
+            break;
+        default:
+            return;
+    }
+    yk_stq(dst, orr);
+    yk_stq(dst + 16, oi);
+}
+
+/* apply op to one element of base type bt; `dst` is updated in place from `src`.
+ * LD: the instance for types that hold long double, with the binary128 operators;
+ * the other instance moves long double bytes for REPLACE only (the host sends every
+ * long double operator to the LD instances), which keeps the 128-bit arithmetic out
+ * of the register budget of the common kernels. */
+template <bool LD>
 __device__ __forceinline__ void yk_apply(int bt, int op, char *dst, const char *src)
 {
     switch (bt) {
@@ -926,9 +984,17 @@ __device__ __forceinline__ void yk_apply(int bt, int op, char *dst, const char *
                 }
                 return;
             }
+        case YK_BT_LDOUBLE: case YK_BT_CLDOUBLE:
+            if (LD) {
+                yk_q_apply(bt, op, dst, src);
+            } else if (op == OP_REPLACE) {
+                yk_stq(dst, yk_ldq(src));
+                if (bt == YK_BT_CLDOUBLE)
+                    yk_stq(dst + 16, yk_ldq(src + 16));
+            }
+            return;
         default:
-            /* CHAR/WCHAR only have REPLACE, which never reaches the typed kernel;
-             * long double arithmetic is refused on the host */
+            /* CHAR/WCHAR only have REPLACE, which never reaches the typed kernel */
             return;
     }
 }
@@ -940,14 +1006,15 @@ __host__ __device__ __forceinline__ int yk_bt_size(int bt)
         case YK_BT_I16: return 2;
         case YK_BT_WCHAR: case YK_BT_I32: case YK_BT_F32: return 4;
         case YK_BT_I64: case YK_BT_F64: case YK_BT_C32: return 8;
-        case YK_BT_C64: return 16;
+        case YK_BT_C64: case YK_BT_LDOUBLE: return 16;
+        case YK_BT_CLDOUBLE: return 32;
         default: return 1;
     }
 }
 
 /* Operators: one work unit = `vec` bytes (the gcd of the element sizes); the unit
  * that starts an element applies op to that whole element. */
-template <typename IDX, int DIR>
+template <typename IDX, int DIR, bool LD>
 __global__ void __launch_bounds__(YK_THREADS)
 yk_typed_kernel(const __grid_constant__ yk_launch L)
 {
@@ -965,9 +1032,9 @@ yk_typed_kernel(const __grid_constant__ yk_launch L)
         char *t = L.typed + off;
         char *p = L.packed + (uint64_t) u * (uint64_t) g;
         if (DIR == 0)
-            yk_apply(bt, op, p, t);
+            yk_apply<LD>(bt, op, p, t);
         else
-            yk_apply(bt, op, t, p);
+            yk_apply<LD>(bt, op, t, p);
     }
 }
 
@@ -1243,7 +1310,7 @@ yk_owner_chunk_kernel(const __grid_constant__ yk_launch L, int rshift)
  * owner: the thread of its first in-range contributor, which applies the
  * contributions of all later blocks in block order (the reference's seq order,
  * src/backend/seq/genpup.py:119-211). */
-template <typename IDX>
+template <typename IDX, bool LD>
 __global__ void __launch_bounds__(YK_THREADS)
 yk_owner_kernel(const __grid_constant__ yk_launch L)
 {
@@ -1273,14 +1340,14 @@ yk_owner_kernel(const __grid_constant__ yk_launch L)
             IDX pp = bb * R + (IDX) (x - db);
             if (pp >= p1)
                 break;
-            yk_apply(bt, op, t, L.packed + (pp - p0));
+            yk_apply<LD>(bt, op, t, L.packed + (pp - p0));
         }
     }
 }
 
 /* General ordered fallback: one warp walks the packed range in order, 32 units at a
  * time; a chunk whose target ranges intersect runs lane by lane. */
-template <typename IDX>
+template <typename IDX, bool LD>
 __global__ void yk_ordered_warp_kernel(const __grid_constant__ yk_launch L)
 {
     const int lane = threadIdx.x;
@@ -1318,7 +1385,7 @@ __global__ void yk_ordered_warp_kernel(const __grid_constant__ yk_launch L)
                 char *t = L.typed + off;
                 char *p = L.packed + (uint64_t) u * (uint64_t) g;
                 if (L.typed_op) {
-                    yk_apply(bt, (int) L.op, t, p);
+                    yk_apply<LD>(bt, (int) L.op, t, p);
                 } else {
                     for (int i = 0; i < len; i++)
                         t[i] = p[i];
@@ -1363,9 +1430,9 @@ __device__ void yk_srv_typed(const yk_launch & L, uint64_t ub, uint64_t ue)
         char *t = L.typed + off;
         char *p = L.packed + u * g;
         if (L.dir == 0)
-            yk_apply(bt, op, p, t);
+            yk_apply<false>(bt, op, p, t);
         else
-            yk_apply(bt, op, t, p);
+            yk_apply<false>(bt, op, t, p);
     }
 }
 
@@ -1394,7 +1461,7 @@ __device__ void yk_srv_owner(const yk_launch & L, uint64_t ub, uint64_t ue)
             uint64_t pp = bb * R + (uint64_t) (x - db);
             if (pp >= p1)
                 break;
-            yk_apply(bt, op, t, L.packed + (pp - p0));
+            yk_apply<false>(bt, op, t, L.packed + (pp - p0));
         }
     }
 }
@@ -1438,7 +1505,7 @@ __device__ void yk_srv_ordered(const yk_launch & L, uint64_t ub, uint64_t ue)
                 char *t = L.typed + off;
                 char *p = L.packed + u * g;
                 if (L.typed_op)
-                    yk_apply(bt, (int) L.op, t, p);
+                    yk_apply<false>(bt, (int) L.op, t, p);
                 else
                     for (int i = 0; i < len; i++)
                         t[i] = p[i];
@@ -1830,6 +1897,43 @@ extern "C" int yk_cuda_launch_batch(const yk_batch * b, int units_per_thread, in
     return (int) cudaGetLastError();
 }
 
+template <int V, int U, int MINB>
+static void yk_launch_hidx32(const yk_launch * l, unsigned g, cudaStream_t s)
+{
+    if (l->dir == 0)
+        yk_hidx32_kernel<V, 0, U, MINB><<<g, YK_THREADS, 0, s>>>(*l);
+    else
+        yk_hidx32_kernel<V, 1, U, MINB><<<g, YK_THREADS, 0, s>>>(*l);
+}
+
+/* contiguous-block hindexed: the 64-bit kernel past 4 GiB of packed bytes, else the
+ * 32-bit one in the shape units_per_thread names (2: two units per lane at 8 resident
+ * CTAs, 8: eight at 4; anything else: YK_HW_UNROLL at 6) */
+template <int V>
+static void yk_launch_hidx(const yk_launch * l, unsigned g, cudaStream_t s, int units_per_thread)
+{
+    if (l->nbytes > 0xffffffffull) {
+        if (l->dir == 0)
+            yk_hidx_kernel<V, 0><<<g, YK_THREADS, 0, s>>>(*l);
+        else
+            yk_hidx_kernel<V, 1><<<g, YK_THREADS, 0, s>>>(*l);
+        return;
+    }
+    if constexpr (V == 4 || V == 8) {
+        if (units_per_thread == 2)
+            return yk_launch_hidx32<V, 2, 8>(l, g, s);
+        if (units_per_thread == 8)
+            return yk_launch_hidx32<V, 8, 4>(l, g, s);
+    }
+    yk_launch_hidx32<V, YK_HW_UNROLL, 6>(l, g, s);
+}
+
+/* a long double operator other than REPLACE: the binary128 kernel instances */
+static bool yk_ld_ops(const yk_launch & c)
+{
+    return c.ldouble && c.typed_op && c.op != OP_REPLACE;
+}
+
 extern "C" int yk_cuda_launch_pup(const yk_launch * l, void *stream)
 {
     return yk_cuda_launch_pup_cfg(l, stream, 0, 0);
@@ -1847,19 +1951,13 @@ extern "C" int yk_cuda_launch_pup_cfg(const yk_launch * l, void *stream, int uni
         uint64_t ctas = (groups + (YK_THREADS / 32) - 1) / (YK_THREADS / 32);
         uint64_t cap = (uint64_t) yk_cuda_num_sms() * (uint64_t) (ctas_per_sm > 0 ? ctas_per_sm : 8);
         unsigned g = (unsigned) (ctas < cap ? (ctas ? ctas : 1) : cap);
-#define YK_H(V) do { if (l->nbytes <= 0xffffffffull) {                                     \
-                         if (l->dir == 0) yk_hidx32_kernel<V, 0><<<g, YK_THREADS, 0, s>>>(*l); \
-                         else yk_hidx32_kernel<V, 1><<<g, YK_THREADS, 0, s>>>(*l);            \
-                     } else if (l->dir == 0) yk_hidx_kernel<V, 0><<<g, YK_THREADS, 0, s>>>(*l); \
-                     else yk_hidx_kernel<V, 1><<<g, YK_THREADS, 0, s>>>(*l); } while (0)
         switch (l->vec) {
-            case 16: YK_H(16); break;
-            case 8: YK_H(8); break;
-            case 4: YK_H(4); break;
-            case 2: YK_H(2); break;
-            default: YK_H(1); break;
+            case 16: yk_launch_hidx<16>(l, g, s, units_per_thread); break;
+            case 8: yk_launch_hidx<8>(l, g, s, units_per_thread); break;
+            case 4: yk_launch_hidx<4>(l, g, s, units_per_thread); break;
+            case 2: yk_launch_hidx<2>(l, g, s, units_per_thread); break;
+            default: yk_launch_hidx<1>(l, g, s, units_per_thread); break;
         }
-#undef YK_H
     } else if (!l->typed_op) {
         if (l->use64)
             launch_bytes<uint64_t>(l, s, units_per_thread, ctas_per_sm);
@@ -1869,17 +1967,19 @@ extern "C" int yk_cuda_launch_pup_cfg(const yk_launch * l, void *stream, int uni
         const yk_launch & c = *l;
         uint64_t units = c.nbytes / (uint64_t) c.vec;
         unsigned g = yk_grid(units, YK_THREADS, ctas_per_sm > 0 ? ctas_per_sm : 16);
-        if (c.use64) {
-            if (c.dir == 0)
-                yk_typed_kernel<uint64_t, 0><<<g, YK_THREADS, 0, s>>>(c);
+#define YK_TK(IDX, LD) do { if (c.dir == 0) yk_typed_kernel<IDX, 0, LD><<<g, YK_THREADS, 0, s>>>(c); \
+                            else yk_typed_kernel<IDX, 1, LD><<<g, YK_THREADS, 0, s>>>(c); } while (0)
+        if (yk_ld_ops(c)) {
+            if (c.use64)
+                YK_TK(uint64_t, true);
             else
-                yk_typed_kernel<uint64_t, 1><<<g, YK_THREADS, 0, s>>>(c);
+                YK_TK(uint32_t, true);
+        } else if (c.use64) {
+            YK_TK(uint64_t, false);
         } else {
-            if (c.dir == 0)
-                yk_typed_kernel<uint32_t, 0><<<g, YK_THREADS, 0, s>>>(c);
-            else
-                yk_typed_kernel<uint32_t, 1><<<g, YK_THREADS, 0, s>>>(c);
+            YK_TK(uint32_t, false);
         }
+#undef YK_TK
     }
     return (int) cudaGetLastError();
 }
@@ -2024,15 +2124,27 @@ extern "C" int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blo
     } else if (sorted_blocks) {
         uint64_t units = c.nbytes / (uint64_t) c.vec;
         unsigned g = yk_grid(units, YK_THREADS, ctas_per_sm > 0 ? ctas_per_sm : 16);
-        if (c.use64)
-            yk_owner_kernel<uint64_t><<<g, YK_THREADS, 0, s>>>(c);
-        else
-            yk_owner_kernel<uint32_t><<<g, YK_THREADS, 0, s>>>(c);
+        if (yk_ld_ops(c)) {
+            if (c.use64)
+                yk_owner_kernel<uint64_t, true><<<g, YK_THREADS, 0, s>>>(c);
+            else
+                yk_owner_kernel<uint32_t, true><<<g, YK_THREADS, 0, s>>>(c);
+        } else if (c.use64) {
+            yk_owner_kernel<uint64_t, false><<<g, YK_THREADS, 0, s>>>(c);
+        } else {
+            yk_owner_kernel<uint32_t, false><<<g, YK_THREADS, 0, s>>>(c);
+        }
     } else {
-        if (c.use64)
-            yk_ordered_warp_kernel<uint64_t><<<1, 32, 0, s>>>(c);
-        else
-            yk_ordered_warp_kernel<uint32_t><<<1, 32, 0, s>>>(c);
+        if (yk_ld_ops(c)) {
+            if (c.use64)
+                yk_ordered_warp_kernel<uint64_t, true><<<1, 32, 0, s>>>(c);
+            else
+                yk_ordered_warp_kernel<uint32_t, true><<<1, 32, 0, s>>>(c);
+        } else if (c.use64) {
+            yk_ordered_warp_kernel<uint64_t, false><<<1, 32, 0, s>>>(c);
+        } else {
+            yk_ordered_warp_kernel<uint32_t, false><<<1, 32, 0, s>>>(c);
+        }
     }
     return (int) cudaGetLastError();
 }

@@ -21,6 +21,7 @@
  * Partial packs follow the reference exactly: the packed range starts at inoffset
  * and ends at the last builtin boundary that fits (src/frontend/pup/yaksi_ipack.c:12-107).
  */
+#include <float.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -370,10 +371,25 @@ typedef struct {
     int64_t lo, hi;             /* typed bytes touched, relative to typed */
 } yk_plan;
 
-static int op_needs_host_arith(yk_type * t, yaksa_op_t op)
+/* The GPU computes long double as IEEE binary128 (yk_quad.h), the long double of
+ * aarch64 Linux.  A host whose long double is another format (x87 extended precision
+ * on x86_64) has no GPU form of the long double operators. */
+#if LDBL_MANT_DIG == 113 && LDBL_MAX_EXP == 16384
+#define YK_LDBL_ON_GPU 1
+#else
+#define YK_LDBL_ON_GPU 0
+#endif
+
+/* an arithmetic operator on a type that holds long double */
+static int ldbl_arith(yk_type * t, yaksa_op_t op)
 {
     return t->needs_host_ops && (op == YAKSA_OP__SUM || op == YAKSA_OP__PROD ||
                                  op == YAKSA_OP__MIN || op == YAKSA_OP__MAX);
+}
+
+static int op_needs_host_arith(yk_type * t, yaksa_op_t op)
+{
+    return !YK_LDBL_ON_GPU && ldbl_arith(t, op);
 }
 
 /* Partial packs follow the reference: start at `offset` and stop at the last builtin
@@ -401,7 +417,7 @@ static int plan(int dir, const void *packed_in, void *packed_out, char *typed, u
     if (b1 <= b0)
         return YAKSA_SUCCESS;
     if (op != YAKSA_OP__REPLACE && op_needs_host_arith(t, op))
-        return YAKSA_ERR__NOT_SUPPORTED;        /* long double arithmetic has no GPU form */
+        return YAKSA_ERR__NOT_SUPPORTED;        /* no binary128 long double on this host */
     int rc = runtime_ready();
     if (rc)
         return rc;
@@ -458,6 +474,7 @@ static int prepare_with(const yk_plan * p, char *typed, char *packed, yk_launch 
     L->op = op;
     L->dir = p->dir;
     L->use64 = (p->b1 > 0xffffffffull);
+    L->ldouble = t->needs_host_ops;
     *sorted = 0;
     if (op == YAKSA_OP__REPLACE && t->is_contig) {
         *kind = YK_X_MEMCPY;
@@ -588,7 +605,7 @@ static int launch_prepared(const yk_plan * p, const yk_launch * L, int kind, int
             e = yk_cuda_launch_hidx_bulk(L, s, cfg.ctas_per_sm);   /* -1: it does not apply */
         if (e == -1)
             e = kind == YK_X_ORDERED ? yk_cuda_launch_unpack_ordered(L, sorted, s, cfg.ctas_per_sm) :
-                yk_cuda_launch_pup_cfg(L, s, 0, cfg.ctas_per_sm);
+                yk_cuda_launch_pup_cfg(L, s, cfg.units_per_thread, cfg.ctas_per_sm);
         yk_tune_end(probe, s);
         return cuda_err((cudaError_t) e, "kernel launch");
     }
@@ -1594,6 +1611,8 @@ static int server_submit(struct yaksa_gb300_server_s *S, yaksa_gb300_pup_t * o, 
         return rc;
     if (p.staged)
         return YAKSA_ERR__NOT_SUPPORTED;        /* the GPU cannot address a buffer */
+    if (ldbl_arith(t, o->op))
+        return YAKSA_ERR__NOT_SUPPORTED;        /* the server kernel has no binary128 operators */
     yk_launch L;
     int kind = YK_X_BYTES, sorted = 0;
     if (p.b1 > p.b0) {

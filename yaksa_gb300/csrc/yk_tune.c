@@ -48,12 +48,14 @@ static const yk_tune_cfg cand_single_tma[] = { {0, 0, 0}, {1, 64, 0}, {4, 8, 0},
     {1, 16, 0}, {0, 4, YK_VARIANT_TMA}, {0, 8, YK_VARIANT_TMA} };
 static const yk_tune_cfg cand_runs_tma[] = { {0, 0, YK_VARIANT_RUNS}, {0, 4, YK_VARIANT_TMA},
     {0, 8, YK_VARIANT_TMA} };
-/* grid caps of the hindexed shuffle-search kernel (default 8 CTAs per SM), the typed
- * operator kernel and the sorted-block kernels (default 16) */
-static const yk_tune_cfg cand_hidx[] = { {0, 0, 0}, {0, 5, 0}, {0, 12, 0}, {0, 16, 0} };
-/* hindexed unpacks: also the bulk-staged form at 2, 4 and 6 CTAs per SM */
+/* the hindexed shuffle-search kernel: grid caps (default 8 CTAs per SM) and, for 4- and
+ * 8-byte units, its two other shapes (units per lane 2 at 8 resident CTAs, 8 at 4) */
+static const yk_tune_cfg cand_hidx[] = { {0, 0, 0}, {0, 5, 0}, {0, 12, 0}, {0, 16, 0},
+    {2, 8, 0}, {2, 16, 0}, {8, 4, 0} };
+/* hindexed unpacks: also the bulk-staged form at 4 CTAs per SM */
 static const yk_tune_cfg cand_hidx_unpack[] = { {0, 0, 0}, {0, 5, 0}, {0, 12, 0},
-    {0, 2, YK_VARIANT_BULK}, {0, 4, YK_VARIANT_BULK}, {0, 6, YK_VARIANT_BULK} };
+    {2, 8, 0}, {2, 16, 0}, {8, 4, 0}, {0, 4, YK_VARIANT_BULK} };
+/* the typed operator kernel and the sorted-block kernels (default 16 CTAs per SM) */
 static const yk_tune_cfg cand_grid16[] = { {0, 0, 0}, {0, 8, 0}, {0, 32, 0} };
 
 #define YK_TUNE_PRELOAD 1024

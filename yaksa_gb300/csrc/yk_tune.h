@@ -14,7 +14,8 @@ enum { YK_TUNE_SINGLE = 1, YK_TUNE_BATCH_REGULAR = 2, YK_TUNE_BATCH = 3, YK_TUNE
 enum { YK_VARIANT_BYTES = 0, YK_VARIANT_TMA = 1, YK_VARIANT_RUNS = 2, YK_VARIANT_BULK = 3 };
 
 typedef struct {
-    int units_per_thread;       /* 1 or 4; 0 = chosen by size */
+    int units_per_thread;       /* 1 or 4; 0 = chosen by size (hindexed: 2 or 8 name that
+                                 * kernel's other two shapes) */
     int ctas_per_sm;            /* grid cap; 0 = by units per thread */
     int variant;                /* YK_VARIANT_*: which kernel runs the launch */
 } yk_tune_cfg;
