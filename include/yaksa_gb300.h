@@ -171,6 +171,16 @@ int yaksa_gb300_debug_tma(int mode);
 int yaksa_gb300_debug_tma_stats(unsigned long long *launches, unsigned int *failures);
 int yaksa_gb300_debug_bulk_failures(unsigned int *n);
 
+/* Test hook (no counterpart in the reference): the launch shape of contiguous-block
+ * hindexed packs and unpacks.  variant < 0 lets the launch-shape autotuner choose (the
+ * default).  variant 0 forces the shuffle-search kernel with `units` naming its shape
+ * for 4- and 8-byte units (0: 8 units per lane at 4 resident CTAs per SM, 4: 4 at 6,
+ * 2: 2 at 8; unpacks also 16: 16 at 3) and `ctas` CTAs per SM in the grid (0: the
+ * shape's residency, one wave); variant 3
+ * forces the bulk-staged unpack with `ctas` CTAs per SM (packs, and unpacks outside its
+ * rules, take the shuffle kernel).  Results are identical in every shape. */
+int yaksa_gb300_debug_hidx_shape(int variant, int units, int ctas);
+
 /* Segment list on the GPU (no counterpart in the reference, whose yaksa_iov fills a
  * host array, src/frontend/include/yaksa.h.in:609): the same entries as yaksa_iov --
  * count, type, iov_offset and max_iov_len mean the same, and *actual_iov_len is set on

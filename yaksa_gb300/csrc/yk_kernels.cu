@@ -361,10 +361,16 @@ yk_hidx_kernel(const __grid_constant__ yk_launch L)
  * state small enough for every warp slot of the SM to stay resident.  Lane k keeps its
  * block's start relative to the group (0 for a block that starts before the range) and
  * the typed offset of relative position 0 in that block, so a unit's typed offset is one
- * shuffle and one add.  U units per lane are in flight at once and MINB CTAs of the
- * block size are meant to stay resident; the autotuner chooses among three shapes for
- * 4- and 8-byte units (latency hiding by loads per lane against warps per SM). */
-template <int V, int DIR, int U, int MINB>
+ * shuffle and one add.
+ *
+ * The kernel is latency-bound (random block starts, a few KiB per group), so each warp
+ * keeps as much in flight as its registers allow: the four index words of its next
+ * group are loaded while the current group is walked, and U units per lane move per
+ * step.  A pack finds the units' typed offsets first and then loads them; an unpack
+ * loads its contiguous packed units first (no offsets needed) and locates each unit
+ * only to store it, so no offsets are live across the load.  MINB CTAs of the block
+ * size are meant to stay resident; the autotuner chooses among the shapes. */
+template <int V, int DIR, int U, int MINB, bool PF>
 __global__ void __launch_bounds__(YK_THREADS, MINB)
 yk_hidx32_kernel(const __grid_constant__ yk_launch L)
 {
@@ -377,56 +383,83 @@ yk_hidx32_kernel(const __grid_constant__ yk_launch L)
     char *typed = L.typed + L.desc.base;
     const uint64_t jb = yk_hidx_block(lv, p0), je = yk_hidx_block(lv, p1 - 1);
     const uint64_t ngroups = (je - jb + 32) / 32;
+    /* the index words of the group a warp takes next: its first block's packed start,
+     * the end of its last block, and this lane's block start and displacement */
+    uint64_t f_first = 0, f_end = 0, f_bp = 0;
+    int64_t f_disp = 0;
+    auto fetch = [&](uint64_t gg) {
+        const uint64_t j0 = jb + gg * 32, jl = j0 + (uint64_t) lane;
+        const uint64_t jend = min(j0 + 32, je + 1);
+        f_first = __ldg(lv->pfx + j0);
+        f_end = __ldg(lv->pfx + jend);
+        if (jl < jend) {
+            f_bp = __ldg(lv->pfx + jl);
+            f_disp = __ldg(lv->disp + jl);
+        }
+    };
+    if (PF && warp < ngroups)
+        fetch(warp);
     for (uint64_t g = warp; g < ngroups; g += nwarps) {
         const uint64_t j0 = jb + g * 32;
         const uint64_t jl = j0 + (uint64_t) lane;
         const uint64_t jend = min(j0 + 32, je + 1);
-        const uint64_t gs = max(__ldg(lv->pfx + j0), p0);
-        const uint32_t n = (uint32_t) (min(__ldg(lv->pfx + jend), p1) - gs);
+        if (!PF)
+            fetch(g);
+        const uint64_t gs = max(f_first, p0);
+        const uint32_t n = (uint32_t) (min(f_end, p1) - gs);
         uint32_t my_rel = 0xffffffffu;
         int64_t my_adj = 0;
         if (jl < jend) {
-            const uint64_t bp = __ldg(lv->pfx + jl);
-            my_rel = bp <= gs ? 0u : (uint32_t) (bp - gs);
-            my_adj = __ldg(lv->disp + jl) - ((int64_t) bp - (int64_t) gs);
+            my_rel = f_bp <= gs ? 0u : (uint32_t) (f_bp - gs);
+            my_adj = f_disp - ((int64_t) f_bp - (int64_t) gs);
         }
+        if (PF && g + nwarps < ngroups)
+            fetch(g + nwarps);
         VT *pk = (VT *) (L.packed + (gs - p0));
         for (uint32_t base = 0; base < n; base += 32u * V * U) {
-            int64_t off[U];
-            bool act[U];
-#pragma unroll
-            for (int k = 0; k < U; k++) {
-                const uint32_t r = base + (uint32_t) (k * 32 + lane) * V;
-                act[k] = r < n;
-                int idx = 0;
-#pragma unroll
-                for (int step = 16; step > 0; step >>= 1) {
-                    const uint32_t c = __shfl_sync(0xffffffffu, my_rel, idx + step);
-                    if (c <= r)
-                        idx += step;
-                }
-                off[k] = __shfl_sync(0xffffffffu, my_adj, idx) + (int64_t) r;
-            }
             if (DIR == 0) {
+                int64_t off[U];
+#pragma unroll
+                for (int k = 0; k < U; k++) {
+                    const uint32_t r = base + (uint32_t) (k * 32 + lane) * V;
+                    int idx = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1) {
+                        const uint32_t c = __shfl_sync(0xffffffffu, my_rel, idx + step);
+                        if (c <= r)
+                            idx += step;
+                    }
+                    off[k] = __shfl_sync(0xffffffffu, my_adj, idx) + (int64_t) r;
+                }
                 VT v[U];
 #pragma unroll
                 for (int k = 0; k < U; k++)
-                    if (act[k])
+                    if (base + (uint32_t) (k * 32 + lane) * V < n)
                         v[k] = yk_ldcg((const VT *) (typed + off[k]));
 #pragma unroll
                 for (int k = 0; k < U; k++)
-                    if (act[k])
+                    if (base + (uint32_t) (k * 32 + lane) * V < n)
                         pk[base / V + (uint32_t) (k * 32 + lane)] = v[k];
             } else {
                 VT v[U];
 #pragma unroll
                 for (int k = 0; k < U; k++)
-                    if (act[k])
+                    if (base + (uint32_t) (k * 32 + lane) * V < n)
                         v[k] = yk_ldcg(pk + base / V + (uint32_t) (k * 32 + lane));
 #pragma unroll
-                for (int k = 0; k < U; k++)
-                    if (act[k])
-                        *(VT *) (typed + off[k]) = v[k];
+                for (int k = 0; k < U; k++) {
+                    const uint32_t r = base + (uint32_t) (k * 32 + lane) * V;
+                    int idx = 0;
+#pragma unroll
+                    for (int step = 16; step > 0; step >>= 1) {
+                        const uint32_t c = __shfl_sync(0xffffffffu, my_rel, idx + step);
+                        if (c <= r)
+                            idx += step;
+                    }
+                    const int64_t off = __shfl_sync(0xffffffffu, my_adj, idx) + (int64_t) r;
+                    if (r < n)
+                        *(VT *) (typed + off) = v[k];
+                }
             }
         }
     }
@@ -1897,35 +1930,66 @@ extern "C" int yk_cuda_launch_batch(const yk_batch * b, int units_per_thread, in
     return (int) cudaGetLastError();
 }
 
-template <int V, int U, int MINB>
-static void yk_launch_hidx32(const yk_launch * l, unsigned g, cudaStream_t s)
+/* the grid of a contiguous-block hindexed launch: one warp per group of 32 blocks, at
+ * most `cap` CTAs per SM (the grid loops over the groups) */
+static unsigned yk_hidx_grid(const yk_launch * l, int cap)
 {
-    if (l->dir == 0)
-        yk_hidx32_kernel<V, 0, U, MINB><<<g, YK_THREADS, 0, s>>>(*l);
-    else
-        yk_hidx32_kernel<V, 1, U, MINB><<<g, YK_THREADS, 0, s>>>(*l);
+    const uint64_t groups = (l->desc.lv[0].count + 31) / 32;
+    const uint64_t ctas = (groups + (YK_THREADS / 32) - 1) / (YK_THREADS / 32);
+    const uint64_t most = (uint64_t) yk_cuda_num_sms() * (uint64_t) cap;
+    return (unsigned) (ctas < most ? (ctas ? ctas : 1) : most);
 }
 
-/* contiguous-block hindexed: the 64-bit kernel past 4 GiB of packed bytes, else the
- * 32-bit one in the shape units_per_thread names (2: two units per lane at 8 resident
- * CTAs, 8: eight at 4; anything else: YK_HW_UNROLL at 6) */
+/* ctas_per_sm 0: as many CTAs as stay resident (MINB per SM), one wave */
+template <int V, int DIR, int U, int MINB, bool PF>
+static void yk_launch_hidx32(const yk_launch * l, cudaStream_t s, int ctas_per_sm)
+{
+    const unsigned g = yk_hidx_grid(l, ctas_per_sm > 0 ? ctas_per_sm : MINB);
+    yk_hidx32_kernel<V, DIR, U, MINB, PF><<<g, YK_THREADS, 0, s>>>(*l);
+}
+
+/* The 32-bit kernel's shapes for 4- and 8-byte units, by `units`: 0 (the default)
+ * eight units per lane at 4 resident CTAs per SM, 4 four at 6, 2 two at 8, 16 (unpacks)
+ * sixteen at 3.  Measured on the hindexed config (1 GiB, 2^20 int32 blocks, cold L2):
+ * pack 72-74 us with eight units, 80 with four, 103 with two; unpack 107, 109-117 and
+ * 126 us -- the kernel is bound by the DRAM accesses of the blocks' random typed lines
+ * (and for unpacks the read-modify-write of the partial sectors at every block's two
+ * ends), not by its loads in flight.  Other unit sizes take four at 6. */
+template <int V, int DIR>
+static void yk_launch_hidx32_shape(const yk_launch * l, cudaStream_t s, int units, int ctas_per_sm)
+{
+    if constexpr (V == 4 || V == 8) {
+        switch (units) {
+            case 2: return yk_launch_hidx32<V, DIR, 2, 8, true>(l, s, ctas_per_sm);
+            case 4: return yk_launch_hidx32<V, DIR, 4, 6, true>(l, s, ctas_per_sm);
+            case 16:
+                if constexpr (DIR == 1)
+                    return yk_launch_hidx32<V, DIR, 16, 3, true>(l, s, ctas_per_sm);
+                break;
+        }
+        yk_launch_hidx32<V, DIR, 8, 4, true>(l, s, ctas_per_sm);
+    } else {
+        yk_launch_hidx32<V, DIR, YK_HW_UNROLL, 6, false>(l, s, ctas_per_sm);
+    }
+}
+
+/* Contiguous-block hindexed: the 64-bit kernel past 4 GiB of packed bytes, else the
+ * 32-bit one in the shape `units` names. */
 template <int V>
-static void yk_launch_hidx(const yk_launch * l, unsigned g, cudaStream_t s, int units_per_thread)
+static void yk_launch_hidx(const yk_launch * l, cudaStream_t s, int units, int ctas_per_sm)
 {
     if (l->nbytes > 0xffffffffull) {
+        const unsigned g = yk_hidx_grid(l, ctas_per_sm > 0 ? ctas_per_sm : 8);
         if (l->dir == 0)
             yk_hidx_kernel<V, 0><<<g, YK_THREADS, 0, s>>>(*l);
         else
             yk_hidx_kernel<V, 1><<<g, YK_THREADS, 0, s>>>(*l);
         return;
     }
-    if constexpr (V == 4 || V == 8) {
-        if (units_per_thread == 2)
-            return yk_launch_hidx32<V, 2, 8>(l, g, s);
-        if (units_per_thread == 8)
-            return yk_launch_hidx32<V, 8, 4>(l, g, s);
-    }
-    yk_launch_hidx32<V, YK_HW_UNROLL, 6>(l, g, s);
+    if (l->dir == 0)
+        yk_launch_hidx32_shape<V, 0>(l, s, units, ctas_per_sm);
+    else
+        yk_launch_hidx32_shape<V, 1>(l, s, units, ctas_per_sm);
 }
 
 /* a long double operator other than REPLACE: the binary128 kernel instances */
@@ -1946,17 +2010,12 @@ extern "C" int yk_cuda_launch_pup_cfg(const yk_launch * l, void *stream, int uni
     if (l->nbytes == 0)
         return 0;
     if (!l->typed_op && l->hidx) {
-        /* one warp per group of 32 blocks, 8 warps per CTA */
-        uint64_t groups = (l->desc.lv[0].count + 31) / 32;
-        uint64_t ctas = (groups + (YK_THREADS / 32) - 1) / (YK_THREADS / 32);
-        uint64_t cap = (uint64_t) yk_cuda_num_sms() * (uint64_t) (ctas_per_sm > 0 ? ctas_per_sm : 8);
-        unsigned g = (unsigned) (ctas < cap ? (ctas ? ctas : 1) : cap);
         switch (l->vec) {
-            case 16: yk_launch_hidx<16>(l, g, s, units_per_thread); break;
-            case 8: yk_launch_hidx<8>(l, g, s, units_per_thread); break;
-            case 4: yk_launch_hidx<4>(l, g, s, units_per_thread); break;
-            case 2: yk_launch_hidx<2>(l, g, s, units_per_thread); break;
-            default: yk_launch_hidx<1>(l, g, s, units_per_thread); break;
+            case 16: yk_launch_hidx<16>(l, s, units_per_thread, ctas_per_sm); break;
+            case 8: yk_launch_hidx<8>(l, s, units_per_thread, ctas_per_sm); break;
+            case 4: yk_launch_hidx<4>(l, s, units_per_thread, ctas_per_sm); break;
+            case 2: yk_launch_hidx<2>(l, s, units_per_thread, ctas_per_sm); break;
+            default: yk_launch_hidx<1>(l, s, units_per_thread, ctas_per_sm); break;
         }
     } else if (!l->typed_op) {
         if (l->use64)

@@ -51,6 +51,8 @@ static struct {
     int host_direct;            /* 0: host memory is never addressed in place, always
                                  * staged (YAKSA_GB300_HOST_DIRECT=0) */
     int tma_mode;               /* TMA forms: 0 off, 1 autotuner candidates, 2 forced */
+    int hidx_forced;            /* contiguous-block hindexed: 1 = hidx_cfg, 0 = autotuner */
+    yk_tune_cfg hidx_cfg;
     /* library streams: requests that are not stream-ordered go round robin over
      * these, so independent requests (whose order the API leaves open) overlap on the
      * GPU; streams[0] is also the default stream of graph replays */
@@ -595,13 +597,16 @@ static int launch_prepared(const yk_plan * p, const yk_launch * L, int kind, int
         int probe = -1;
         const int fam = kind == YK_X_ORDERED ? YK_TUNE_OWNER : kind == YK_X_TYPED ? YK_TUNE_TYPED :
             L->dir == 1 ? YK_TUNE_HIDX_UNPACK : YK_TUNE_HIDX;
-        if (fam == YK_TUNE_HIDX_UNPACK && R.tma_mode == 2)
+        const int hidx = fam == YK_TUNE_HIDX || fam == YK_TUNE_HIDX_UNPACK;
+        if (fam == YK_TUNE_HIDX_UNPACK && R.tma_mode == 2) {
             cfg.variant = YK_VARIANT_BULK;      /* the test hook forces the bulk form */
-        else if (tune && (kind != YK_X_ORDERED || sorted))
+        } else if (hidx && __atomic_load_n(&R.hidx_forced, __ATOMIC_ACQUIRE)) {
+            cfg = R.hidx_cfg;                   /* the test hook forces a shape */
+        } else if (tune && (kind != YK_X_ORDERED || sorted))
             probe = yk_tune_begin(yk_tune_key(fam, (int) L->op, L->desc.leaf_type * 17 + L->vec, L->dir,
                                               L->use64, units), fam, units, s, &cfg);
         int e = -1;
-        if (cfg.variant == YK_VARIANT_BULK && R.tma_mode)
+        if (cfg.variant == YK_VARIANT_BULK && (R.tma_mode || (hidx && R.hidx_forced)))
             e = yk_cuda_launch_hidx_bulk(L, s, cfg.ctas_per_sm);   /* -1: it does not apply */
         if (e == -1)
             e = kind == YK_X_ORDERED ? yk_cuda_launch_unpack_ordered(L, sorted, s, cfg.ctas_per_sm) :
@@ -643,6 +648,29 @@ int yaksa_gb300_debug_tma(int mode)
     if (mode < 0 || mode > 2)
         return YAKSA_ERR__INTERNAL;
     __atomic_store_n(&R.tma_mode, mode, __ATOMIC_RELAXED);
+    return YAKSA_SUCCESS;
+}
+
+/* contiguous-block hindexed launches: variant < 0 lets the autotuner choose (the
+ * default); otherwise every such launch takes {units, ctas, variant} -- YK_VARIANT_BYTES
+ * (0) the shuffle-search kernel in the shape `units` names, YK_VARIANT_BULK (3) the
+ * bulk-staged unpack (a pack, or a request outside its rules, takes the shuffle kernel) */
+int yaksa_gb300_debug_hidx_shape(int variant, int units, int ctas)
+{
+    if (variant != YK_VARIANT_BYTES && variant != YK_VARIANT_BULK && variant >= 0)
+        return YAKSA_ERR__INTERNAL;
+    if (units < 0 || ctas < 0 || ctas > 64)
+        return YAKSA_ERR__INTERNAL;
+    if (variant < 0) {
+        __atomic_store_n(&R.hidx_forced, 0, __ATOMIC_RELEASE);
+        return YAKSA_SUCCESS;
+    }
+    pthread_mutex_lock(&R.mu);
+    R.hidx_cfg.units_per_thread = units;
+    R.hidx_cfg.ctas_per_sm = ctas;
+    R.hidx_cfg.variant = variant;
+    __atomic_store_n(&R.hidx_forced, 1, __ATOMIC_RELEASE);
+    pthread_mutex_unlock(&R.mu);
     return YAKSA_SUCCESS;
 }
 

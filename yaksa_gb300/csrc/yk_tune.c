@@ -48,13 +48,12 @@ static const yk_tune_cfg cand_single_tma[] = { {0, 0, 0}, {1, 64, 0}, {4, 8, 0},
     {1, 16, 0}, {0, 4, YK_VARIANT_TMA}, {0, 8, YK_VARIANT_TMA} };
 static const yk_tune_cfg cand_runs_tma[] = { {0, 0, YK_VARIANT_RUNS}, {0, 4, YK_VARIANT_TMA},
     {0, 8, YK_VARIANT_TMA} };
-/* the hindexed shuffle-search kernel: grid caps (default 8 CTAs per SM) and, for 4- and
- * 8-byte units, its two other shapes (units per lane 2 at 8 resident CTAs, 8 at 4) */
-static const yk_tune_cfg cand_hidx[] = { {0, 0, 0}, {0, 5, 0}, {0, 12, 0}, {0, 16, 0},
-    {2, 8, 0}, {2, 16, 0}, {8, 4, 0} };
-/* hindexed unpacks: also the bulk-staged form at 4 CTAs per SM */
-static const yk_tune_cfg cand_hidx_unpack[] = { {0, 0, 0}, {0, 5, 0}, {0, 12, 0},
-    {2, 8, 0}, {2, 16, 0}, {8, 4, 0}, {0, 4, YK_VARIANT_BULK} };
+/* the hindexed shuffle-search kernel: its shapes (units per lane and residency, see
+ * yk_launch_hidx32_shape) at one wave, and the default shape at two */
+static const yk_tune_cfg cand_hidx[] = { {0, 0, 0}, {0, 8, 0}, {4, 0, 0}, {2, 0, 0} };
+/* hindexed unpacks: also sixteen units per lane, and the bulk-staged form */
+static const yk_tune_cfg cand_hidx_unpack[] = { {0, 0, 0}, {0, 8, 0}, {4, 0, 0}, {16, 0, 0},
+    {0, 4, YK_VARIANT_BULK} };
 /* the typed operator kernel and the sorted-block kernels (default 16 CTAs per SM) */
 static const yk_tune_cfg cand_grid16[] = { {0, 0, 0}, {0, 8, 0}, {0, 32, 0} };
 
