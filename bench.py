@@ -563,7 +563,7 @@ def dev_fill(torch, base, nbytes, gen):
     return out
 
 
-def run_stream(nreq=10000, rate=50e3, seed=5, check=True, log=None, floor=True):
+def run_stream(nreq=10000, rate=50e3, seed=5, check=True, log=None, floor=True, server_tune=True):
     """10,000 pack/unpack requests with Poisson arrivals at `rate` req/s: families drawn
     uniformly from hvector/halo/hindexed/struct/reduce, packed sizes log-uniform over
     19 power-of-two classes 256 B .. 64 MiB, 20% with the packed buffer in pinned host
@@ -688,23 +688,32 @@ def run_stream(nreq=10000, rate=50e3, seed=5, check=True, log=None, floor=True):
            "arena_bytes": int(sum(arena.values()))}
     zero = np.zeros(nreq)
     srv = yk.Server(y, ring_requests=4096, budget_bytes=8 << 30)
-    for mode in ("plain", "server"):
+    for mode in ("plain", "graphs", "server"):
         s = srv if mode == "server" else None
+        graphs = mode == "graphs"
+        if s is not None and server_tune:
+            # calibration of the server's item cut per request class (untimed; each
+            # class's requests run alone, once per candidate cut and repetition)
+            t_tune = time.perf_counter()
+            res["server_tuned_classes"] = srv.tune(make_ops())
+            res["server_tune_s"] = time.perf_counter() - t_tune
         # warm: every descriptor built and uploaded once, outside the timed runs
         ops = make_ops()
-        yk.serve_trace(y, ops, zero, server=s)
+        yk.serve_trace(y, ops, zero, server=s, graphs=graphs)
         torch.cuda.synchronize()
         reset_private()
         ops = make_ops()
         launches0 = y.stats()["launches"]
-        lat, mk = yk.serve_trace(y, ops, arrivals.tolist(), server=s)
+        g0 = y.graph_lane_stats()
+        lat, mk = yk.serve_trace(y, ops, arrivals.tolist(), server=s, graphs=graphs)
         torch.cuda.synchronize()
         launches = y.stats()["launches"] - launches0
+        g1 = y.graph_lane_stats()
         bad = verify() if check else []
         lat_us = np.array(lat) * 1e6
         # closed loop: everything arrives at once -> capacity
         ops2 = make_ops()
-        _, mk2 = yk.serve_trace(y, ops2, zero, server=s)
+        _, mk2 = yk.serve_trace(y, ops2, zero, server=s, graphs=graphs)
         torch.cuda.synchronize()
         # latency by packed size: small (<= 64 KiB), medium (<= 4 MiB), large
         sizes_req = np.array([k[1] for k in keys])
@@ -719,6 +728,8 @@ def run_stream(nreq=10000, rate=50e3, seed=5, check=True, log=None, floor=True):
                                    "p50_us": float(np.percentile(lat_us, 50)),
                                    "p99_us": float(np.percentile(lat_us, 99)),
                                    "mean_us": float(lat_us.mean()), "kernel_launches": launches,
+                                   "graph_captures": g1["captures"] - g0["captures"],
+                                   "graph_replays": g1["replays"] - g0["replays"],
                                    "by_size": by_size},
                      "closed_loop": {"GBps": total / mk2 / 1e9, "req_per_s": nreq / mk2, "makespan_s": mk2},
                      "bit_exact": not bad, "mismatched": bad[:10]}
@@ -1209,22 +1220,36 @@ def main():
                       "GBps": r["plain"]["open_loop"]["GBps"],
                       "capacity_GBps": r["plain"]["closed_loop"]["GBps"],
                       "capacity_req_per_s": r["plain"]["closed_loop"]["req_per_s"]},
+            "plain_graphs": {"p50_us": r["graphs"]["open_loop"]["p50_us"],
+                             "p99_us": r["graphs"]["open_loop"]["p99_us"],
+                             "GBps": r["graphs"]["open_loop"]["GBps"],
+                             "capacity_GBps": r["graphs"]["closed_loop"]["GBps"],
+                             "capacity_req_per_s": r["graphs"]["closed_loop"]["req_per_s"],
+                             "graph_captures": r["graphs"]["open_loop"]["graph_captures"],
+                             "graph_replays": r["graphs"]["open_loop"]["graph_replays"],
+                             "bit_exact": r["graphs"]["bit_exact"]},
             "batched": {"p50_us": r["server"]["open_loop"]["p50_us"], "p99_us": r["server"]["open_loop"]["p99_us"],
                         "GBps": r["server"]["open_loop"]["GBps"],
                         "capacity_GBps": r["server"]["closed_loop"]["GBps"],
-                        "capacity_req_per_s": r["server"]["closed_loop"]["req_per_s"]},
+                        "capacity_req_per_s": r["server"]["closed_loop"]["req_per_s"],
+                        "item_cut_tuning": {"classes_decided": r.get("server_tuned_classes"),
+                                            "calibration_s": r.get("server_tune_s")}},
             "by_size": {"plain": r["plain"]["open_loop"]["by_size"],
+                        "plain_graphs": r["graphs"]["open_loop"]["by_size"],
                         "batched": r["server"]["open_loop"]["by_size"],
                         "classes": "small <= 64 KiB < medium <= 4 MiB < large"},
             "capacity_ratio": r["server_over_plain"]["closed_loop_throughput"],
             "p99_ratio": r["server_over_plain"]["open_loop_p99"],
             "xface_floor": r.get("xface_floor"),
-            "bit_exact": r["plain"]["bit_exact"] and r["server"]["bit_exact"],
+            "bit_exact": r["plain"]["bit_exact"] and r["server"]["bit_exact"] and r["graphs"]["bit_exact"],
             "checked_requests": r["checked_requests"],
             "checked_size_classes": r["checked_size_classes"],
             "largest_checked_bytes": r["largest_checked_bytes"],
             "note": "p50/p99 from arrival to completion seen by the serving loop; capacity = all "
-                    "requests arriving at once; batched = persistent-kernel server"}
+                    "requests arriving at once; plain_graphs = one launch per request with "
+                    "repeated request records replayed as captured CUDA graphs; batched = "
+                    "persistent-kernel server, its item cut calibrated per request class "
+                    "before the timed runs"}
     if rank == 0 and not args.no_cpu:
         b = cpu_halo(args.cpu_seconds, 1)
         line["cpu_baseline"] = {k: b[k] for k in ("value", "unit", "cores", "kind", "cpu", "sample")}

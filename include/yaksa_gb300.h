@@ -84,6 +84,24 @@ int yaksa_gb300_server_stats(yaksa_gb300_server_t server, uint64_t * requests, u
                              uint64_t * relaunches, uint32_t * idle_exits);
 int yaksa_gb300_server_destroy(yaksa_gb300_server_t server);
 
+/* Calibration of the server's work-item cut (no counterpart in the reference).  A
+ * request of 256 KiB or more belongs to a class: work-item kind, unit, direction, base
+ * type of an operator, and size to a power of two.  For each request of `ops` whose
+ * class has no decision yet, the server runs the request under each candidate cut
+ * (largest item 64 KiB to 1 MiB, least number of items 32 to 512), several times.
+ * Each run submits enough concurrent copies for 64 MiB (at most 64, and half the
+ * request ring), so that the items meet the memory contention of a loaded server. The
+ * GPU times every item on the CTA that runs it, and the run's sample is the copies'
+ * summed item time: the time per byte that bounds a loaded server's throughput. The
+ * cut with the least time becomes the class's decision for every later submission
+ * (the server's own cut unless another one is clearly faster).
+ * Decisions persist in YAKSA_GB300_TUNE_FILE like the launch shapes.  The requests run
+ * several times: for REPLACE their targets hold the result of one run; for other
+ * operators they are left unspecified.  *classes (if not NULL) receives the number of
+ * classes this call decided.  Call it with no other request of the server in flight. */
+int yaksa_gb300_server_tune(yaksa_gb300_server_t server, yaksa_gb300_pup_t * ops, int n,
+                            yaksa_info_t info, int *classes);
+
 /* One pack (kind 0) or unpack (kind 1) that allocates nothing (no counterpart in the
  * reference).  For callers that must not allocate device memory: a library whose
  * device memory is all owned by the application's allocator, or code issuing requests
@@ -117,11 +135,17 @@ int yaksa_gb300_pup_noalloc(yaksa_gb300_pup_t * op, void *stream);
  * mode 0 issues each as yaksa_ipack/yaksa_iunpack on arrival (one launch per
  * request); mode 1 submits them to `server`, admitting in arrival order and holding
  * a refused request (rings or byte budget full) at the head until progress frees
- * room. latency_s[i] = completion time seen by the loop - arrival_s[i];
- * *makespan_s = time of the last completion. ops[i].actual is set. */
+ * room; mode 2 is mode 0 with a graph lane: a request whose record (kind, buffers,
+ * count, type, offset, size, operator) was seen before runs as the replay of a CUDA
+ * graph of its launch, captured at its second sight (requests that need staging keep
+ * the plain path; the graphs live for the call). latency_s[i] = completion time seen
+ * by the loop - arrival_s[i]; *makespan_s = time of the last completion. ops[i].actual
+ * is set. */
 int yaksa_gb300_serve_trace(yaksa_gb300_pup_t * ops, const double *arrival_s, int n, int mode,
                             yaksa_gb300_server_t server, yaksa_info_t info, double *latency_s,
                             double *makespan_s);
+/* the graph lane's launches captured and graphs replayed so far (all calls) */
+int yaksa_gb300_graph_lane_stats(uint64_t * captures, uint64_t * replays);
 
 /* Launch-shape autotuner (no counterpart in the reference): shape classes seen, classes
  * whose shape is decided, and launches timed so far.  YAKSA_GB300_AUTOTUNE=0 in the

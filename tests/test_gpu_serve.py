@@ -63,3 +63,30 @@ def test_serve_trace_empty(prod):
     lat, mk = yk.serve_trace(prod, prod.batch_array([yk.pack_op(0, 0, yk.TYPE_INT32_T, 0, 0, 0)]),
                              [0.0])
     assert lat[0] >= 0 and mk >= 0
+
+
+def test_graph_lane_replays_repeated_requests(cuda, prod, oracle):
+    """mode 2: each of 30 REPLACE records arrives six times; every record is captured
+    once (at its second sight) and replayed from then on, and the bytes equal the
+    oracle's (a REPLACE repeated with the same inputs writes the same bytes)"""
+    g, reqs = make_requests(cuda, prod, oracle, 700, 30, ops=False)
+    reps = 6
+    order = [i for _ in range(reps) for i in range(len(reqs))]
+    ops = prod.batch_array([op_of(reqs[i]) for i in order])
+    arrivals = np.linspace(0.0, 3e-3, len(order))
+    s0 = prod.graph_lane_stats()
+    lat, mk = yk.serve_trace(prod, ops, arrivals.tolist(), graphs=True)
+    cuda.cuda.synchronize()
+    s1 = prod.graph_lane_stats()
+    moving = sum(1 for i in range(len(reqs)) if ops[i].actual > 0)
+    assert moving > 20
+    assert s1["captures"] - s0["captures"] == moving
+    assert s1["replays"] - s0["replays"] == moving * (reps - 1)
+    assert all(x >= 0 for x in lat) and mk >= arrivals[-1]
+    for k in range(reps):
+        for i in range(len(reqs)):
+            assert ops[k * len(reqs) + i].actual == ops[i].actual
+    check(cuda, oracle, reqs, ops)
+    for r in reqs:
+        r["pair"].free()
+    g.free()

@@ -227,3 +227,64 @@ def test_server_item_sizes(cuda, env):
                         os.path.join(here, "test_gpu_server.py"), "-k", "not item_sizes"],
                        env=dict(os.environ, **env), capture_output=True, text=True, timeout=900)
     assert r.returncode == 0, r.stdout[-3000:] + r.stderr[-3000:]
+
+
+def test_server_tune_decides_item_cuts_and_stays_exact(cuda, prod, oracle):
+    """yaksa_gb300_server_tune times every candidate item cut of each class of 256 KiB and
+    more (hvector and hindexed packs, a strided SUM unpack) with the request alone on the
+    server, decides each class once, and later submissions -- cut the decided way --
+    give the oracle's bytes; a second call finds every class decided"""
+    rng = np.random.default_rng(31)
+    nb = 30000
+    blens = rng.integers(1, 40, nb)
+    displs = (np.cumsum(blens + rng.integers(0, 9, nb)) - blens) * 4
+    perm = rng.permutation(nb)
+    specs = [("hvector", lambda y: y.type_create_hvector(1 << 16, 4, 64, yk.TYPE_DOUBLE), "double",
+              yk.OP_REPLACE, 0),
+             ("hindexed", lambda y: y.type_create_hindexed(blens[perm].tolist(), displs[perm].tolist(),
+                                                          yk.TYPE_INT32_T), "int32", yk.OP_REPLACE, 0),
+             ("strided_sum", lambda y: y.type_create_hvector(1 << 15, 8, 96, yk.TYPE_DOUBLE), "double",
+              yk.OP_SUM, 1)]
+    srv = yk.Server(prod, ring_requests=64)
+    reqs = []
+    for name, mk, base, op, kind in specs:
+        tp, to = mk(prod), mk(oracle)
+        lb, text = prod.true_extent(tp)
+        n = prod.size(tp)
+        assert n >= 256 << 10
+        typed, packed = fill(rng, lb + text, base), fill(rng, n, base)
+        reqs.append(dict(tp=tp, to=to, lb=lb, n=n, typed=typed, packed=packed, op=op, kind=kind))
+
+    def ops_of(bufs):
+        out = []
+        for r, (tg, pg) in zip(reqs, bufs):
+            if r["kind"] == 0:
+                out.append(yk.pack_op(tg.data_ptr() - r["lb"], 1, r["tp"], 0, pg.data_ptr(), r["n"]))
+            else:
+                out.append(yk.unpack_op(pg.data_ptr(), r["n"], tg.data_ptr() - r["lb"], 1, r["tp"], 0,
+                                        op=r["op"]))
+        return prod.batch_array(out)
+
+    scratch = [(dev_copy(cuda, r["typed"]), dev_copy(cuda, r["packed"])) for r in reqs]
+    before = prod.autotune_stats()["decided"]
+    decided = srv.tune(ops_of(scratch))
+    assert decided == len(reqs)
+    assert prod.autotune_stats()["decided"] == before + len(reqs)
+    assert srv.tune(ops_of(scratch)) == 0
+    # submissions after the decision: bytes against the oracle
+    bufs = [(dev_copy(cuda, r["typed"]), dev_copy(cuda, r["packed"])) for r in reqs]
+    tickets = submit_all(srv, list(ops_of(bufs)))
+    for t in tickets:
+        srv.wait(t)
+    for r, (tg, pg) in zip(reqs, bufs):
+        th, ph = r["typed"].copy(), r["packed"].copy()
+        if r["kind"] == 0:
+            oracle.pack(th.ctypes.data - r["lb"], 1, r["to"], 0, ph.ctypes.data, r["n"])
+        else:
+            oracle.unpack(ph.ctypes.data, r["n"], th.ctypes.data - r["lb"], 1, r["to"], 0, op=r["op"])
+        assert np.array_equal(host_of(cuda, tg), th)
+        assert np.array_equal(host_of(cuda, pg), ph)
+    srv.destroy()
+    for r in reqs:
+        prod.type_free(r["tp"])
+        oracle.type_free(r["to"])

@@ -176,9 +176,12 @@ def load_library(path):
                                                          ctypes.POINTER(_u64),
                                                          ctypes.POINTER(ctypes.c_uint32)]),
                            ("yaksa_gb300_server_destroy", [_vp]),
+                           ("yaksa_gb300_server_tune", [_vp, ctypes.POINTER(PupOp), ctypes.c_int, _vp,
+                                                        ctypes.POINTER(ctypes.c_int)]),
                            ("yaksa_gb300_pup_noalloc", [ctypes.POINTER(PupOp), _vp]),
                            ("yaksa_gb300_probe_rows", [ctypes.POINTER(Rows), ctypes.c_int, ctypes.c_int, _vp]),
                            ("yaksa_gb300_debug_hidx_shape", [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+                           ("yaksa_gb300_graph_lane_stats", [ctypes.POINTER(_u64), ctypes.POINTER(_u64)]),
                            ("yaksa_gb300_serve_trace", [ctypes.POINTER(PupOp), ctypes.POINTER(ctypes.c_double),
                                                         ctypes.c_int, ctypes.c_int, _vp, _vp,
                                                         ctypes.POINTER(ctypes.c_double),
@@ -219,6 +222,13 @@ class Server:
     def progress(self):
         self.y._chk("yaksa_gb300_server_progress", self.y.lib.yaksa_gb300_server_progress(self.h))
 
+    def tune(self, ops, info=None):
+        """yaksa_gb300_server_tune over an array of PupOp; returns the classes decided."""
+        c = ctypes.c_int()
+        self.y._chk("yaksa_gb300_server_tune",
+                    self.y.lib.yaksa_gb300_server_tune(self.h, ops, len(ops), info, ctypes.byref(c)))
+        return c.value
+
     def stats(self):
         a, b, c, d = _u64(), _u64(), _u64(), ctypes.c_uint32()
         self.y.lib.yaksa_gb300_server_stats(self.h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c),
@@ -231,17 +241,18 @@ class Server:
             self.h = None
 
 
-def serve_trace(y, ops, arrival_s, server=None, info=None):
+def serve_trace(y, ops, arrival_s, server=None, info=None, graphs=False):
     """Replay `ops` (a yaksa_gb300_pup_t array) arriving at `arrival_s` seconds through
-    the plain nonblocking path (server None) or `server`; returns (latencies, makespan)."""
+    the plain nonblocking path (server None; with the graph lane for repeated requests
+    when `graphs`) or `server`; returns (latencies, makespan)."""
     n = len(ops)
     arr = (ctypes.c_double * max(1, n))(*arrival_s)
     lat = (ctypes.c_double * max(1, n))()
     mk = ctypes.c_double()
+    mode = 1 if server is not None else 2 if graphs else 0
     y._chk("yaksa_gb300_serve_trace",
-           y.lib.yaksa_gb300_serve_trace(ops, arr, n, 1 if server is not None else 0,
-                                         server.h if server is not None else None, info, lat,
-                                         ctypes.byref(mk)))
+           y.lib.yaksa_gb300_serve_trace(ops, arr, n, mode, server.h if server is not None else None,
+                                         info, lat, ctypes.byref(mk)))
     return list(lat[:n]), mk.value
 
 
@@ -505,6 +516,11 @@ class Yaksa:
         self._chk("yaksa_gb300_shard", self.lib.yaksa_gb300_shard(t, count, rank, nranks,
                                                                    ctypes.byref(o), ctypes.byref(n)))
         return o.value, n.value
+
+    def graph_lane_stats(self):
+        c, r = _u64(), _u64()
+        self.lib.yaksa_gb300_graph_lane_stats(ctypes.byref(c), ctypes.byref(r))
+        return dict(captures=c.value, replays=r.value)
 
     def autotune_stats(self):
         a, b, c = ctypes.c_uint32(), ctypes.c_uint32(), _u64()

@@ -133,6 +133,8 @@ int yk_cuda_launch_batch(const yk_batch * b, int units_per_thread, int regular, 
  * Persistent request server: a device-visible work queue drained by resident CTAs.
  * ------------------------------------------------------------------------- */
 enum { YK_SRV_REGULAR = 0, YK_SRV_BYTES, YK_SRV_TYPED, YK_SRV_OWNER, YK_SRV_ORDERED, YK_SRV_HIDX };
+/* flag in yk_item.kind: the item's busy time is added to its request's req_busy */
+#define YK_SRV_TIMED 0x100u
 
 typedef struct {
     uint64_t seq;               /* item sequence number (the GPU checks it) */
@@ -163,6 +165,10 @@ typedef struct {
     unsigned long long *cq;     /* completion queue (host-mapped, qr entries): slot + 1 of
                                  * each finished request, in finishing order; 0 = empty */
     unsigned long long *cq_tail;        /* device memory: next completion queue position */
+    unsigned long long *req_busy;       /* per request slot (host-mapped): the summed busy
+                                         * time of a timed request's items in ns, each from
+                                         * its record load to its last byte (GPU global
+                                         * timer; the host zeroes it before publishing) */
     uint32_t qi, qr;            /* ring sizes */
     uint32_t max_idle_spins;    /* bounded wait for new items */
     uint32_t pad;

@@ -1610,6 +1610,13 @@ __device__ __forceinline__ uint64_t yk_ld_sys(const void *p)
  * word; the CTA that finishes the request's last item appends slot + 1 to the completion
  * queue, so the host learns of completions without scanning every request in flight.
  * The item's bytes are made visible to the host first. */
+__device__ __forceinline__ unsigned long long yk_globaltimer(void)
+{
+    unsigned long long t;
+    asm volatile ("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 __device__ __forceinline__ void yk_srv_item_done(const yk_server_args & A, uint32_t slot)
 {
     __threadfence_system();
@@ -1624,7 +1631,8 @@ __device__ __forceinline__ void yk_srv_item_done(const yk_server_args & A, uint3
 /* a record the GPU can act on: a known kind, a sane unit and an ordered range */
 __device__ __forceinline__ bool yk_item_ok(const yk_item & it, const yk_launch & L)
 {
-    if (it.kind > YK_SRV_HIDX || it.pe <= it.pb || it.pb < L.p0 || it.pe > L.p0 + L.nbytes)
+    if ((it.kind & ~YK_SRV_TIMED) > YK_SRV_HIDX || it.pe <= it.pb || it.pb < L.p0 ||
+        it.pe > L.p0 + L.nbytes)
         return false;
     if (L.vec != 1 && L.vec != 2 && L.vec != 4 && L.vec != 8 && L.vec != 16)
         return false;
@@ -1744,9 +1752,11 @@ yk_server_kernel(const __grid_constant__ yk_server_args A)
             continue;
         }
         const yk_item it = s_it;
+        const bool timed = (it.kind & YK_SRV_TIMED) != 0;
+        const unsigned long long tb = timed && threadIdx.x == 0 ? yk_globaltimer() : 0ull;
         const uint64_t g = (uint64_t) sL.vec;
         const uint64_t ub = (it.pb - sL.p0) / g, ue = (it.pe - sL.p0) / g;
-        switch (it.kind) {
+        switch (it.kind & ~YK_SRV_TIMED) {
             case YK_SRV_REGULAR:
 #define YK_SV(V) do { if (sL.dir == 0) yk_srv_regular<V, 0>(sL, ub, ue); \
                       else yk_srv_regular<V, 1>(sL, ub, ue); } while (0)
@@ -1795,8 +1805,11 @@ yk_server_kernel(const __grid_constant__ yk_server_args A)
                 break;
         }
         __syncthreads();
-        if (threadIdx.x == 0)
+        if (threadIdx.x == 0) {
+            if (timed)
+                atomicAdd_system(A.req_busy + it.req % A.qr, yk_globaltimer() - tb);
             yk_srv_item_done(A, it.req % A.qr);   /* the item's bytes first, then its count */
+        }
     }
 }
 

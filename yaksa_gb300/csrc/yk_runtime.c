@@ -1458,6 +1458,19 @@ typedef struct {
     int64_t user;               /* the serving loop's index of the request (-1: none) */
 } yk_srv_slot;
 
+/* a request planned for the server: its launch record, work-item kind and granule */
+typedef struct {
+    yk_type *t;
+    yk_plan p;
+    yk_launch L;
+    uint32_t skind;
+    uint64_t gran;
+    uint64_t key;               /* its class for the item-cut tuner (0: not tuned) */
+} yk_srv_req;
+
+/* requests below this size are cut the same way by every candidate: not tuned */
+#define YK_SRV_TUNE_MIN (256u << 10)
+
 struct yaksa_gb300_server_s {
     pthread_mutex_t mu;
     int ctas, running;
@@ -1468,6 +1481,8 @@ struct yaksa_gb300_server_s {
     unsigned long long *req_done;       /* pinned, mapped: items finished per request slot */
     uint64_t *req_nitems;       /* pinned, mapped: items per request slot */
     unsigned long long *cq;     /* pinned, mapped: completion queue written by the GPU */
+    unsigned long long *req_busy;       /* pinned, mapped: summed item busy time (ns) of
+                                         * timed requests */
     uint64_t cq_head;           /* next completion queue entry the host reads */
     uint64_t *ctl;              /* pinned, mapped: [0] items published, [1] stop, [2] status */
     unsigned long long *next_item;      /* device: the lanes' claim counters, then the
@@ -1530,12 +1545,13 @@ int yaksa_gb300_server_create(uint32_t ring_requests, uint64_t budget_bytes,
     S->req_done = pinned(sizeof(unsigned long long) * S->qr);
     S->req_nitems = pinned(sizeof(uint64_t) * S->qr);
     S->cq = pinned(sizeof(unsigned long long) * S->qr);
+    S->req_busy = pinned(sizeof(unsigned long long) * S->qr);
     S->ctl = pinned(64);
     S->slots = calloc(S->qr, sizeof(yk_srv_slot));
     /* device counters: the claim lanes (one 128-byte line each), then the queue's tail */
     const size_t nctr = (size_t) (YK_SRV_LANES + 1) * YK_SRV_LANE_STRIDE;
     if (!S->reqs || !S->items || !S->req_done || !S->req_nitems || !S->cq || !S->ctl ||
-        !S->slots || yk_fail_injected() ||
+        !S->req_busy || !S->slots || yk_fail_injected() ||
         cudaMalloc((void **) &S->next_item, sizeof(unsigned long long) * nctr) != cudaSuccess ||
         cudaMemset(S->next_item, 0, sizeof(unsigned long long) * nctr) != cudaSuccess ||
         cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking) != cudaSuccess) {
@@ -1554,6 +1570,7 @@ int yaksa_gb300_server_create(uint32_t ring_requests, uint64_t budget_bytes,
     S->args.req_nitems = S->req_nitems;
     S->args.cq = S->cq;
     S->args.cq_tail = S->next_item + (size_t) YK_SRV_LANES * YK_SRV_LANE_STRIDE;
+    S->args.req_busy = S->req_busy;
     S->args.qi = S->qi;
     S->args.qr = S->qr;
     S->args.max_idle_spins = 4000;      /* ~8 ms without work at the 2 us poll interval */
@@ -1625,18 +1642,20 @@ int yaksa_gb300_server_submit(yaksa_gb300_server_t S, yaksa_gb300_pup_t * o, yak
     return server_submit(S, o, info, ticket, -1);
 }
 
-/* user: the serving loop's index of the request, logged at completion (-1: none) */
-static int server_submit(struct yaksa_gb300_server_s *S, yaksa_gb300_pup_t * o, yaksa_info_t info,
-                         uint64_t * ticket, int64_t user)
+/* plan one request for the server: the launch record, its work-item kind and granule,
+ * and its class for the item-cut tuner */
+static int server_plan(yaksa_gb300_pup_t * o, yaksa_info_t info, yk_srv_req * q)
 {
     o->actual = 0;
-    yk_type *t = yk_type_get(o->type);
+    memset(q, 0, sizeof(*q));
+    yk_type *t = q->t = yk_type_get(o->type);
     if (!t)
         return YAKSA_ERR__INTERNAL;
-    yk_plan p;
-    int rc = plan_op(o, t, info, &p);
+    yk_plan *pp = &q->p;
+    int rc = plan_op(o, t, info, pp);
     if (rc)
         return rc;
+    const yk_plan p = *pp;
     if (p.staged)
         return YAKSA_ERR__NOT_SUPPORTED;        /* the GPU cannot address a buffer */
     if (ldbl_arith(t, o->op))
@@ -1677,9 +1696,34 @@ static int server_submit(struct yaksa_gb300_server_s *S, yaksa_gb300_pup_t * o, 
         skind = sorted ? YK_SRV_OWNER : YK_SRV_ORDERED;
         gran = sorted ? (uint64_t) yk_base_type_size(L.desc.leaf_type) : (uint64_t) L.vec;
     }
+    q->L = L;
+    q->skind = skind;
+    q->gran = gran;
+    const uint64_t n = p.b1 - p.b0;
+    /* class: item kind, unit, direction, base type for operators, size (power of two) */
+    if (skind != YK_SRV_ORDERED && n >= YK_SRV_TUNE_MIN)
+        q->key = yk_tune_key(YK_TUNE_SERVER, (int) skind, L.vec, L.dir,
+                             L.typed_op ? L.desc.leaf_type & 15 : 0, n);
+    return YAKSA_SUCCESS;
+}
+
+/* Cut a planned request into work items and publish them.  cfg: the item cut ({0, 0}
+ * the server's own); timed: the GPU sums its items' busy time into req_busy of its
+ * slot.  user: the serving loop's index of the request, logged at completion (-1:
+ * none). */
+static int server_enqueue(struct yaksa_gb300_server_s *S, yaksa_gb300_pup_t * o, yk_srv_req * q,
+                          const yk_tune_cfg * cfg, int timed, uint64_t * ticket, int64_t user)
+{
+    int rc;
+    yk_type *t = q->t;
+    const yk_plan p = q->p;
+    const yk_launch L = q->L;
+    const uint32_t skind = q->skind;
+    const uint64_t gran = q->gran;
     uint64_t n = p.b1 - p.b0;
-    uint64_t ib = S->item_bytes;
-    while (S->min_items && ib > (32u << 10) && n < (uint64_t) S->min_items * ib)
+    uint64_t ib = cfg->units_per_thread ? (uint64_t) cfg->units_per_thread << 10 : S->item_bytes;
+    const uint64_t min_items = cfg->units_per_thread ? (uint64_t) cfg->ctas_per_sm : S->min_items;
+    while (min_items && ib > (32u << 10) && n < min_items * ib)
         ib >>= 1;       /* mid-size requests: more, smaller items, so more CTAs share them */
     uint64_t chunk = skind == YK_SRV_ORDERED ? (n ? n : 1) : YK_MAX(ib / gran, 1) * gran;
     uint64_t nitems = n ? (n + chunk - 1) / chunk : 0;
@@ -1711,12 +1755,14 @@ static int server_submit(struct yaksa_gb300_server_s *S, yaksa_gb300_pup_t * o, 
         S->inflight_bytes += n;
         __atomic_store_n(&S->req_done[slot], 0ull, __ATOMIC_RELAXED);
         S->req_nitems[slot] = nitems;
+        S->req_busy[slot] = 0;
         memcpy(&S->reqs[slot], &L, sizeof(L));
+        const uint32_t ikind = skind | (timed ? YK_SRV_TIMED : 0u);
         for (uint64_t i = 0; i < nitems; i++) {
             yk_item *it = &S->items[(S->item_seq + i) % S->qi];
             it->seq = S->item_seq + i;
             it->req = slot;
-            it->kind = skind;
+            it->kind = ikind;
             it->pb = p.b0 + i * chunk;
             it->pe = YK_MIN(p.b1, p.b0 + (i + 1) * chunk);
         }
@@ -1728,6 +1774,98 @@ static int server_submit(struct yaksa_gb300_server_s *S, yaksa_gb300_pup_t * o, 
     rc = server_progress_locked(S);     /* relaunches the resident kernel if it left */
     pthread_mutex_unlock(&S->mu);
     *ticket = seq;
+    return rc;
+}
+
+/* a request cut the way its class's tuner decided (the server's own cut until then) */
+static int server_submit(struct yaksa_gb300_server_s *S, yaksa_gb300_pup_t * o, yaksa_info_t info,
+                         uint64_t * ticket, int64_t user)
+{
+    yk_srv_req q;
+    int rc = server_plan(o, info, &q);
+    if (rc)
+        return rc;
+    yk_tune_cfg cfg = { 0, 0, 0 };
+    if (q.key)
+        yk_tune_server_cfg(q.key, &cfg);
+    return server_enqueue(S, o, &q, &cfg, 0, ticket, user);
+}
+
+/* One calibration sample: k copies of a request submitted together with item cut cfg,
+ * all waited for; *ns = the busy time of all the copies' items summed (each item from
+ * its record load to its last byte, on the CTA that ran it).  With the server loaded,
+ * resident CTAs always have items, so its throughput is CTAs / (busy time per byte):
+ * the sum measures exactly that, unlike the span of one group, which a group too small
+ * to fill the GPU would bias towards finer cuts.  The copies run at once, so the items
+ * meet the memory contention of a loaded server. */
+static int server_tune_group(struct yaksa_gb300_server_s *S, yaksa_gb300_pup_t * o, yk_srv_req * q,
+                             const yk_tune_cfg * cfg, int k, double *ns)
+{
+    uint64_t tk[64];
+    int rc = YAKSA_SUCCESS, m = 0;
+    *ns = 0;
+    struct timespec a, b;
+    clock_gettime(CLOCK_MONOTONIC, &a);
+    while (m < k && !rc) {
+        rc = server_enqueue(S, o, q, cfg, 1, &tk[m], -1);
+        if (rc == YAKSA_ERR__OUT_OF_MEM) {
+            /* rings or budget full: let the copies in flight finish (bounded) */
+            rc = yaksa_gb300_server_progress(S);
+            clock_gettime(CLOCK_MONOTONIC, &b);
+            if (!rc && b.tv_sec - a.tv_sec > 20)
+                rc = YAKSA_ERR__INTERNAL;
+            if (!rc && m == 0 && S->oldest_req == S->req_seq)
+                return YAKSA_SUCCESS;   /* one copy alone does not fit: no sample */
+            continue;
+        }
+        if (!rc)
+            m++;
+    }
+    for (int i = 0; i < m && !rc; i++)
+        rc = yaksa_gb300_server_wait(S, tk[i]);
+    if (rc)
+        return rc;
+    double busy = 0;
+    for (int i = 0; i < m; i++)
+        busy += (double) __atomic_load_n(&S->req_busy[tk[i] % S->qr], __ATOMIC_ACQUIRE);
+    if (m == k)
+        *ns = busy;
+    return YAKSA_SUCCESS;
+}
+
+int yaksa_gb300_server_tune(yaksa_gb300_server_t S, yaksa_gb300_pup_t * ops, int n,
+                            yaksa_info_t info, int *classes)
+{
+    int decided = 0, rc = YAKSA_SUCCESS;
+    for (int i = 0; i < n && !rc; i++) {
+        /* each undecided class: every candidate cut in turn, a group of copies at a time,
+         * until the tuner decides.  The group holds enough copies for 64 MiB (at most 64,
+         * and half the request ring) so that the GPU is as full as under load. */
+        for (int guard = 0; guard < 64 && !rc; guard++) {
+            yk_srv_req q;
+            rc = server_plan(&ops[i], info, &q);
+            if (rc || !q.key)
+                break;
+            yk_tune_cfg cfg;
+            const int cand = yk_tune_server_next(q.key, &cfg);
+            if (cand < 0) {
+                decided += guard > 0;
+                break;
+            }
+            const uint64_t bytes = q.p.b1 - q.p.b0;
+            uint64_t k = ((64ull << 20) + bytes - 1) / bytes;
+            k = YK_MIN(k, 64);
+            k = YK_MIN(k, (uint64_t) (S->qr / 2 ? S->qr / 2 : 1));
+            double ns = 0;
+            rc = server_tune_group(S, &ops[i], &q, &cfg, (int) k, &ns);
+            if (!rc && ns > 0)
+                yk_tune_server_sample(q.key, cand, ns);
+            if (rc || ops[i].actual == 0)
+                break;
+        }
+    }
+    if (classes)
+        *classes = decided;
     return rc;
 }
 
@@ -1815,6 +1953,8 @@ int yaksa_gb300_server_destroy(yaksa_gb300_server_t S)
             cudaFreeHost(S->req_nitems);
         if (S->cq)
             cudaFreeHost(S->cq);
+        if (S->req_busy)
+            cudaFreeHost(S->req_busy);
         if (S->ctl)
             cudaFreeHost(S->ctl);
     }
@@ -1827,6 +1967,153 @@ int yaksa_gb300_server_destroy(yaksa_gb300_server_t S)
 /* ------------------------------------------------------------------------- */
 /* serving loop: replay an arrival schedule through the plain or batched path */
 /* ------------------------------------------------------------------------- */
+
+/* The serving loop's graph lane (mode 2).  A request whose record (kind, buffers,
+ * count, type, offset, size, operator) repeats runs, from its second sight on, as the
+ * replay of a CUDA graph holding the launch captured at that sight: one graph launch
+ * and one event instead of the plan, the descriptor lookup, the launch-shape choice and
+ * the launch.  The first sight runs the plain path, which builds the type's
+ * descriptors, so nothing inside the capture allocates or synchronizes; the captured
+ * launch has the shape the autotuner had decided by then (the default while the class
+ * is still being timed).  Requests whose buffers need staging keep the plain path. */
+typedef struct {
+    yaksa_gb300_pup_t rec;
+    int used;
+    int seen;                   /* sights so far; -1: never captured */
+    cudaGraphExec_t exec;
+    yk_type *t;                 /* held while the graph exists */
+    uintptr_t actual;
+} yk_glane_ent;
+
+typedef struct {
+    yk_glane_ent *e;
+    size_t cap;                 /* a power of two, at least twice the requests */
+    cudaStream_t cs;            /* capture stream */
+} yk_glane;
+
+static uint64_t graph_captures, graph_replays;
+
+int yaksa_gb300_graph_lane_stats(uint64_t * captures, uint64_t * replays)
+{
+    *captures = __atomic_load_n(&graph_captures, __ATOMIC_RELAXED);
+    *replays = __atomic_load_n(&graph_replays, __ATOMIC_RELAXED);
+    return YAKSA_SUCCESS;
+}
+
+static int glane_same(const yaksa_gb300_pup_t * a, const yaksa_gb300_pup_t * b)
+{
+    return a->kind == b->kind && a->inbuf == b->inbuf && a->outbuf == b->outbuf &&
+        a->count == b->count && a->type == b->type && a->offset == b->offset &&
+        a->maxbytes == b->maxbytes && a->op == b->op;
+}
+
+static yk_glane_ent *glane_find(yk_glane * G, const yaksa_gb300_pup_t * o)
+{
+    const uint64_t w[8] = { (uint64_t) o->kind, (uint64_t) (uintptr_t) o->inbuf,
+        (uint64_t) (uintptr_t) o->outbuf, (uint64_t) o->count, (uint64_t) o->type,
+        (uint64_t) o->offset, (uint64_t) o->maxbytes, (uint64_t) o->op };
+    uint64_t h = 1469598103934665603ull;        /* FNV-1a over the record's words */
+    for (int i = 0; i < 8; i++)
+        h = (h ^ w[i]) * 1099511628211ull;
+    for (size_t i = (size_t) h & (G->cap - 1);; i = (i + 1) & (G->cap - 1)) {
+        yk_glane_ent *e = &G->e[i];
+        if (!e->used) {
+            e->used = 1;
+            e->rec = *o;
+            return e;
+        }
+        if (glane_same(&e->rec, o))
+            return e;
+    }
+}
+
+/* capture the request's launch into e->exec; e->seen = -1 when it never will be */
+static int glane_capture(yk_glane * G, yk_glane_ent * e, yaksa_gb300_pup_t * o, yaksa_info_t info)
+{
+    yk_type *t = yk_type_get(o->type);
+    if (!t)
+        return YAKSA_ERR__INTERNAL;
+    yk_plan p;
+    int rc = plan_op(o, t, info, &p);
+    if (rc)
+        return rc;
+    if (p.staged || p.b1 == p.b0) {
+        e->seen = -1;
+        return YAKSA_SUCCESS;
+    }
+    if (!G->cs && (rc = cuda_err(cudaStreamCreateWithFlags(&G->cs, cudaStreamNonBlocking),
+                                 "cudaStreamCreate")))
+        return rc;
+    rc = cuda_err(cudaStreamBeginCapture(G->cs, cudaStreamCaptureModeThreadLocal),
+                  "cudaStreamBeginCapture");
+    if (rc)
+        return rc;
+    const int erc = enqueue(&p, p.dtyped, p.dpacked, G->cs);
+    cudaGraph_t g = NULL;
+    cudaError_t ce = cudaStreamEndCapture(G->cs, &g);
+    if (erc || ce != cudaSuccess || !g) {
+        if (g)
+            cudaGraphDestroy(g);
+        cudaGetLastError();
+        e->seen = -1;
+        return erc;
+    }
+    ce = cudaGraphInstantiate(&e->exec, g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) {
+        cudaGetLastError();
+        e->exec = NULL;
+        e->seen = -1;
+        return YAKSA_SUCCESS;
+    }
+    yk_type_ref(t);
+    e->t = t;
+    e->actual = p.b1 - p.b0;
+    __atomic_add_fetch(&graph_captures, 1, __ATOMIC_RELAXED);
+    return YAKSA_SUCCESS;
+}
+
+/* mode 2's submission: a replay when the record was captured, else the plain path */
+static int glane_submit(yk_glane * G, yaksa_gb300_pup_t * o, yaksa_info_t info,
+                        yaksa_request_t * req)
+{
+    yk_glane_ent *e = glane_find(G, o);
+    int rc;
+    if (!e->exec && e->seen >= 0 && ++e->seen >= 2 && (rc = glane_capture(G, e, o, info)))
+        return rc;
+    if (e->exec) {
+        cudaStream_t s = lib_stream();
+        rc = cuda_err(cudaGraphLaunch(e->exec, s), "cudaGraphLaunch");
+        if (rc)
+            return rc;
+        __atomic_add_fetch(&graph_replays, 1, __ATOMIC_RELAXED);
+        o->actual = e->actual;
+        return complete(e->t, YK_MODE_NONBLOCKING, s, req);
+    }
+    uintptr_t actual = 0;
+    rc = o->kind != 0 && o->kind != 1 ? YAKSA_ERR__INTERNAL : o->kind == 0 ?
+        yaksa_ipack(o->inbuf, o->count, o->type, o->offset, o->outbuf, o->maxbytes, &actual, info,
+                    o->op, req) :
+        yaksa_iunpack(o->inbuf, o->maxbytes, o->outbuf, o->count, o->type, o->offset, &actual, info,
+                      o->op, req);
+    o->actual = actual;
+    return rc;
+}
+
+static void glane_free(yk_glane * G, int failed)
+{
+    if (failed)
+        cudaDeviceSynchronize();        /* replays may still run: none is destroyed live */
+    for (size_t i = 0; G->e && i < G->cap; i++) {
+        if (G->e[i].exec)
+            cudaGraphExecDestroy(G->e[i].exec);
+        if (G->e[i].t)
+            yk_type_unref(G->e[i].t);
+    }
+    free(G->e);
+    if (G->cs)
+        cudaStreamDestroy(G->cs);
+}
 
 static double now_s(void)
 {
@@ -1842,13 +2129,21 @@ int yaksa_gb300_serve_trace(yaksa_gb300_pup_t * ops, const double *arrival_s, in
     int rc = runtime_ready();
     if (rc)
         return rc;
-    if (mode == 1 && !server)
+    if ((mode == 1 && !server) || mode < 0 || mode > 2)
         return YAKSA_ERR__INTERNAL;
     uint64_t *handle = calloc(n > 0 ? n : 1, sizeof(uint64_t));
     char *state = calloc(n > 0 ? n : 1, 1);     /* 0 waiting, 1 in flight, 2 done */
-    if (!handle || !state) {
+    yk_glane G = { NULL, 0, NULL };
+    if (mode == 2) {
+        G.cap = 16;
+        while (G.cap < 2 * (size_t) (n > 0 ? n : 1))
+            G.cap *= 2;
+        G.e = calloc(G.cap, sizeof(yk_glane_ent));
+    }
+    if (!handle || !state || (mode == 2 && !G.e)) {
         free(handle);
         free(state);
+        free(G.e);
         return YAKSA_ERR__OUT_OF_MEM;
     }
     int next = 0, done = 0, oldest = 0;
@@ -1888,6 +2183,14 @@ int yaksa_gb300_serve_trace(yaksa_gb300_pup_t * ops, const double *arrival_s, in
                     done++;
                     continue;
                 }
+            } else if (mode == 2) {
+                yaksa_request_t req = YAKSA_REQUEST__NULL;
+                int r = glane_submit(&G, o, info, &req);
+                if (r) {
+                    rc = r;
+                    break;
+                }
+                handle[next] = req;
             } else {
                 yaksa_request_t req;
                 uintptr_t actual;
@@ -1949,6 +2252,8 @@ int yaksa_gb300_serve_trace(yaksa_gb300_pup_t * ops, const double *arrival_s, in
         pthread_mutex_unlock(&server->mu);
     }
     *makespan_s = last - t0;
+    if (mode == 2)
+        glane_free(&G, rc != 0);
     free(handle);
     free(state);
     return rc;

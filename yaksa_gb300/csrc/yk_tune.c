@@ -56,6 +56,10 @@ static const yk_tune_cfg cand_hidx_unpack[] = { {0, 0, 0}, {0, 8, 0}, {4, 0, 0},
     {0, 4, YK_VARIANT_BULK} };
 /* the typed operator kernel and the sorted-block kernels (default 16 CTAs per SM) */
 static const yk_tune_cfg cand_grid16[] = { {0, 0, 0}, {0, 8, 0}, {0, 32, 0} };
+/* the persistent server's cut of a request into work items: {largest item in KiB, least
+ * number of items} ({0, 0}: the server's own setting, 256 KiB and 128 by default) */
+static const yk_tune_cfg cand_server[] = { {0, 0, 0}, {1024, 128, 0}, {64, 128, 0}, {256, 32, 0},
+    {256, 512, 0} };
 
 #define YK_TUNE_PRELOAD 1024
 
@@ -104,6 +108,7 @@ static const yk_tune_cfg *family_cands(int family, int *n)
         case YK_TUNE_HIDX: return YK_C(cand_hidx);
         case YK_TUNE_HIDX_UNPACK: return YK_C(cand_hidx_unpack);
         case YK_TUNE_TYPED: case YK_TUNE_OWNER: return YK_C(cand_grid16);
+        case YK_TUNE_SERVER: return YK_C(cand_server);
         default: return YK_C(cand_batch);
     }
 #undef YK_C
@@ -167,10 +172,32 @@ static int log2u(uint64_t v)
 
 uint64_t yk_tune_key(int family, int depth, int vec, int dir, int wide, uint64_t units)
 {
-    /* nonzero by construction: family is 1..9 */
+    /* nonzero by construction: family is 1..10 */
     return ((uint64_t) family << 32) | ((uint64_t) (depth + 1) << 24) |
         ((uint64_t) vec << 16) | ((uint64_t) dir << 12) | ((uint64_t) wide << 8) |
         (uint64_t) log2u(units);
+}
+
+/* one timing sample of candidate c of slot s (ms); decides the class once every
+ * candidate has YK_TUNE_REPS samples */
+static void record_locked(slot_t * s, int c, float ms)
+{
+    if (s->done[c] == 0 || ms < s->fastest[c])
+        s->fastest[c] = ms;
+    s->done[c]++;
+    int all = 1;
+    for (int k = 0; k < s->ncand; k++)
+        all &= s->done[k] >= YK_TUNE_REPS;
+    if (all && s->best < 0) {
+        /* candidate 0 is the default shape: keep it unless another one's fastest sample
+         * beats it clearly (samples are noisy and taken with warm caches) */
+        int b = 0;
+        for (int k = 1; k < s->ncand; k++)
+            if (s->fastest[k] < YK_TUNE_MARGIN * s->fastest[0] && s->fastest[k] < s->fastest[b])
+                b = k;
+        s->best = b;
+        persist_locked(s);
+    }
 }
 
 static void drain_locked(void)
@@ -184,24 +211,7 @@ static void drain_locked(void)
             continue;
         float ms = 0;
         if (e == cudaSuccess && cudaEventElapsedTime(&ms, p->e0, p->e1) == cudaSuccess) {
-            slot_t *s = &T.slots[p->slot];
-            if (s->done[p->cand] == 0 || ms < s->fastest[p->cand])
-                s->fastest[p->cand] = ms;
-            s->done[p->cand]++;
-            int all = 1;
-            for (int c = 0; c < s->ncand; c++)
-                all &= s->done[c] >= YK_TUNE_REPS;
-            if (all && s->best < 0) {
-                /* candidate 0 is the default shape: keep it unless another one's fastest
-                 * sample beats it clearly (samples are noisy and taken with warm caches) */
-                int b = 0;
-                for (int c = 1; c < s->ncand; c++)
-                    if (s->fastest[c] < YK_TUNE_MARGIN * s->fastest[0] &&
-                        s->fastest[c] < s->fastest[b])
-                        b = c;
-                s->best = b;
-                persist_locked(s);
-            }
+            record_locked(&T.slots[p->slot], p->cand, ms);
         } else {
             cudaGetLastError();
         }
@@ -258,7 +268,14 @@ int yk_tune_begin(uint64_t key, int family, uint64_t units, void *stream, yk_tun
         pthread_mutex_unlock(&T.mu);
         return -1;
     }
-    drain_locked();
+    /* inside a stream capture: the decided shape (or the default), with no event work */
+    enum cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    const int capturing = cudaStreamIsCapturing(st, &cs) != cudaSuccess ||
+        cs != cudaStreamCaptureStatusNone;
+    if (capturing)
+        cudaGetLastError();
+    else
+        drain_locked();
     slot_t *s = slot_locked(key, family);
     if (!s) {
         pthread_mutex_unlock(&T.mu);
@@ -269,9 +286,7 @@ int yk_tune_begin(uint64_t key, int family, uint64_t units, void *stream, yk_tun
         pthread_mutex_unlock(&T.mu);
         return -1;
     }
-    enum cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    if (cudaStreamIsCapturing(st, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
-        cudaGetLastError();
+    if (capturing) {
         pthread_mutex_unlock(&T.mu);
         return -1;      /* no timing inside a capture: default shape */
     }
@@ -322,6 +337,54 @@ void yk_tune_end(int probe, void *stream)
     } else {
         T.probes[probe].armed = 1;
     }
+    pthread_mutex_unlock(&T.mu);
+}
+
+int yk_tune_server_cfg(uint64_t key, yk_tune_cfg * cfg)
+{
+    int n, decided = 0;
+    *cfg = family_cands(YK_TUNE_SERVER, &n)[0];
+    pthread_mutex_lock(&T.mu);
+    init_locked();
+    if (T.enabled) {
+        slot_t *s = slot_locked(key, YK_TUNE_SERVER);
+        if (s && s->best >= 0) {
+            *cfg = s->cand[s->best];
+            decided = 1;
+        }
+    }
+    pthread_mutex_unlock(&T.mu);
+    return decided;
+}
+
+int yk_tune_server_next(uint64_t key, yk_tune_cfg * cfg)
+{
+    int n, c = -1;
+    *cfg = family_cands(YK_TUNE_SERVER, &n)[0];
+    pthread_mutex_lock(&T.mu);
+    init_locked();
+    slot_t *s = T.enabled ? slot_locked(key, YK_TUNE_SERVER) : NULL;
+    if (s && s->best < 0) {
+        c = 0;
+        for (int k = 1; k < s->ncand; k++)
+            if (s->issued[k] < s->issued[c])
+                c = k;
+        s->issued[c]++;
+        *cfg = s->cand[c];
+    } else if (s) {
+        *cfg = s->cand[s->best];
+    }
+    pthread_mutex_unlock(&T.mu);
+    return c;
+}
+
+void yk_tune_server_sample(uint64_t key, int cand, double ns)
+{
+    pthread_mutex_lock(&T.mu);
+    init_locked();
+    slot_t *s = T.enabled ? slot_locked(key, YK_TUNE_SERVER) : NULL;
+    if (s && cand >= 0 && cand < s->ncand && ns > 0)
+        record_locked(s, cand, (float) (ns * 1e-6));
     pthread_mutex_unlock(&T.mu);
 }
 
