@@ -340,12 +340,25 @@ def suite_types(y, yk, np, rng_seed=7, scale=1):
         out[f"reduce_{base}"] = dict(
             mk=lambda L, offs=offs, h=h, nbk=nbk: L.type_create_indexed_block_array(nbk, 8, offs.ctypes.data, h),
             base=base, count=1, extent=(256 << 20) // scale, op=op, keep=(offs,), gran=0)
+    # operators on strided targets that do not overlap (the runtime-operator typed
+    # kernel): 4-element blocks at a stride of 6 elements, 64 MiB packed; double SUM, and
+    # long double SUM and PROD in binary128 (hosts whose long double is binary128 only).
+    # Named only, for profiling: they are not configs of the baseline.
+    for name, h, es, base, op in (("strided_sum", yk.TYPE_DOUBLE, 8, "double", yk.OP_SUM),
+                                  ("ldouble_sum", yk.TYPE_LONG_DOUBLE, 16, "ldouble", yk.OP_SUM),
+                                  ("ldouble_prod", yk.TYPE_LONG_DOUBLE, 16, "ldouble", yk.OP_PROD)):
+        nblk = (64 << 20) // (4 * es) // scale
+        out[name] = dict(mk=lambda L, nblk=nblk, es=es, h=h: L.type_create_hvector(nblk, 4, 6 * es, h),
+                         base=base, count=1, extent=nblk * 6 * es, op=op, gran=es, named_only=True)
     return out
 
 
 def suite_fill(np, rng, base, nbytes):
     if base == "double":
         return rng.standard_normal(nbytes // 8).view(np.uint8)
+    if base == "ldouble":
+        # the host's long double (binary128 where these workloads run)
+        return rng.standard_normal(nbytes // 16).astype(np.longdouble).view(np.uint8)
     if base == "int64":
         return rng.integers(-(1 << 63), (1 << 63) - 1, nbytes // 8, dtype=np.int64).view(np.uint8)
     if base == "uint32" or base == "int32":
