@@ -1122,6 +1122,34 @@ def run_halo(args, y, yk, torch, np, world, rank, dist):
                           "NVLink-C2C"}
     res["e2e_serial"] = {"value": step_bytes * world / results[False] / 1e9, "unit": "GB/s",
                          "note": "the six packs completed before the six unpacks, which read the send buffers"}
+    # the host link's own rate for the step's transfers: the row-touch instrument reads the
+    # six receive buffers and writes the six send buffers (12 MiB each way), both launches
+    # at once on two streams, GPU-timed; the e2e step moves the same bytes over the link
+    s_rd, s_wr = torch.cuda.Stream(), torch.cuda.Stream()
+    rd_rows = [yk.Rows(pk.data_ptr(), 1, 0, P // 16, 16, 16, 0) for pk in recv]
+    wr_rows = [yk.Rows(pk.data_ptr(), 1, 0, P // 16, 16, 16, 0) for pk in send]
+
+    def link_once():
+        e0 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        ends = []
+        for st, rows, w in ((s_rd, rd_rows, 0), (s_wr, wr_rows, 1)):
+            st.wait_event(e0)
+            h = ctypes.c_void_p(st.cuda_stream)
+            y.probe_rows(rows, w, ctypes.addressof(h))
+            e = torch.cuda.Event(enable_timing=True)
+            e.record(st)
+            ends.append(e)
+        torch.cuda.synchronize()
+        return max(e0.elapsed_time(e) for e in ends) * 1e-3
+    for _ in range(3):
+        link_once()
+    link_t = statistics.median(link_once() for _ in range(15))
+    link_gbps = step_bytes / link_t / 1e9
+    res["e2e"]["link_floor"] = {"GBps": link_gbps, "us": link_t * 1e6, "frac": res["e2e"]["value"] / link_gbps,
+                                "note": "plain 16-byte loads of the six pinned receive buffers and stores "
+                                        "into the six send buffers, at once (row-touch instrument, GPU-timed): "
+                                        "the host link's rate for the step's 12 MiB each way"}
     hsrc = src.cpu().pin_memory()
     hdst = torch.zeros_like(hsrc).pin_memory()
     e2e_h = e2e_run(hsrc, hdst, e_steps, True)
