@@ -195,6 +195,19 @@ int yaksa_gb300_debug_tma(int mode);
 int yaksa_gb300_debug_tma_stats(unsigned long long *launches, unsigned int *failures);
 int yaksa_gb300_debug_bulk_failures(unsigned int *n);
 
+/* Test hook (no counterpart in the reference): the L2-reduction form of unpacks whose
+ * targets overlap.  When the type is one level of equal blocks (indexed_block,
+ * hindexed_block, or indexed/hindexed with equal lengths) in any order, or a vector
+ * whose stride is under its block length, the operator
+ * is SUM, MAX, MIN, BAND, BOR or BXOR on a 4- or 8-byte integer type, and both buffers
+ * sit on the element size, each packed element is folded into its target by one
+ * reduction at L2 (red.global) instead of an ordered read-combine-write.  These
+ * operators are commutative and associative on integers, so the bytes equal the
+ * in-order result.  mode 0 never uses the form, 1 uses it wherever it applies (the
+ * default; YAKSA_GB300_L2_REDUCE=0 in the environment sets mode 0), -1 leaves the mode
+ * as it is.  *launches (if not NULL) receives the form's launches so far. */
+int yaksa_gb300_debug_l2_reduce(int mode, unsigned long long *launches);
+
 /* Test hook (no counterpart in the reference): the launch shape of contiguous-block
  * hindexed packs and unpacks.  variant < 0 lets the launch-shape autotuner choose (the
  * default).  variant 0 forces the shuffle-search kernel with `units` naming its shape

@@ -181,6 +181,7 @@ def load_library(path):
                            ("yaksa_gb300_pup_noalloc", [ctypes.POINTER(PupOp), _vp]),
                            ("yaksa_gb300_probe_rows", [ctypes.POINTER(Rows), ctypes.c_int, ctypes.c_int, _vp]),
                            ("yaksa_gb300_debug_hidx_shape", [ctypes.c_int, ctypes.c_int, ctypes.c_int]),
+                           ("yaksa_gb300_debug_l2_reduce", [ctypes.c_int, ctypes.POINTER(ctypes.c_ulonglong)]),
                            ("yaksa_gb300_graph_lane_stats", [ctypes.POINTER(_u64), ctypes.POINTER(_u64)]),
                            ("yaksa_gb300_serve_trace", [ctypes.POINTER(PupOp), ctypes.POINTER(ctypes.c_double),
                                                         ctypes.c_int, ctypes.c_int, _vp, _vp,

@@ -192,9 +192,29 @@ int yk_cuda_launch_pup_cfg(const yk_launch * l, void *stream, int units_per_thre
                            int ctas_per_sm);
 
 /* Ordered unpack for types whose targets may overlap: sorted-block owner-computes
- * kernel when the descriptor allows it, otherwise a single-warp ordered kernel. */
+ * kernel when the descriptor allows it, otherwise a single-warp ordered kernel.
+ * sorted_blocks & 3: 0 = any layout; 1 = one IDX level of sorted blocks; 2 = the same
+ * with both sides aligned to the element size.  YK_ORD_RED set: one IDX level of equal
+ * blocks in any order (or one VEC level), both sides aligned to the element size,
+ * under an operator that yk_red_applies() accepts -- the launch folds the elements in
+ * with L2 reductions. */
+#define YK_ORD_RED 4
 int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blocks, void *stream,
                                   int ctas_per_sm);
+/* launches of the L2-reduction form so far */
+unsigned long long yk_cuda_red_launches(void);
+
+/* Operators that an overlapping unpack may apply as L2 reductions, in any order: the
+ * integer operators whose result does not depend on the order of the contributions
+ * (addition modulo 2^n, max, min, and, or, xor), on 4- and 8-byte integers.  The
+ * launch also needs element-aligned sides, 32-bit positions and blocks under 2^32
+ * bytes. */
+static inline int yk_red_applies(int bt, uint64_t op)
+{
+    return (bt == YK_BT_I32 || bt == YK_BT_I64) &&
+        (op == 0 /* MAX */ || op == 1 /* MIN */ || op == 2 /* SUM */ || op == 5 /* BAND */ ||
+         op == 7 /* BOR */ || op == 9 /* BXOR */);
+}
 
 /* TMA form of a REPLACE launch over a regular nest (yk_tma.cu): 1 when it exists; the
  * launch returns -1 when it does not, else a cudaError_t value. */

@@ -19,6 +19,7 @@
  * multiplication recovers infinities with the algorithm of ISO C11 Annex G.5.1 (what
  * libgcc's __mulsc3/__muldc3 implement for the reference's `*=` on _Complex values).
  */
+#include <atomic>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "yk_desc.h"
@@ -1338,6 +1339,78 @@ yk_owner_chunk_kernel(const __grid_constant__ yk_launch L, int rshift)
     }
 }
 
+/* Reductions at L2 for the integer operators whose result does not depend on the order
+ * in which contributions arrive: SUM (addition modulo 2^n), MAX, MIN (signed, as the
+ * reference's unsigned handles alias the signed types), BAND, BOR and BXOR, on 4- and
+ * 8-byte integers.  The value is sent to the L2 with a reduction (red.global.*, the
+ * form an atomic whose result is unused compiles to), which reads, combines and writes
+ * the target element there. */
+template <int OP, typename T> __device__ __forceinline__ void yk_red(T *p, T v);
+template <int OP> __device__ __forceinline__ void yk_red(int32_t *p, int32_t v)
+{
+    unsigned int *q = (unsigned int *) p;
+    if constexpr (OP == OP_SUM) atomicAdd(q, (unsigned int) v);
+    else if constexpr (OP == OP_MAX) atomicMax((int *) p, (int) v);
+    else if constexpr (OP == OP_MIN) atomicMin((int *) p, (int) v);
+    else if constexpr (OP == OP_BAND) atomicAnd(q, (unsigned int) v);
+    else if constexpr (OP == OP_BOR) atomicOr(q, (unsigned int) v);
+    else atomicXor(q, (unsigned int) v);
+}
+template <int OP> __device__ __forceinline__ void yk_red(int64_t *p, int64_t v)
+{
+    unsigned long long *q = (unsigned long long *) p;
+    if constexpr (OP == OP_SUM) atomicAdd(q, (unsigned long long) v);
+    else if constexpr (OP == OP_MAX) atomicMax((long long *) p, (long long) v);
+    else if constexpr (OP == OP_MIN) atomicMin((long long *) p, (long long) v);
+    else if constexpr (OP == OP_BAND) atomicAnd(q, (unsigned long long) v);
+    else if constexpr (OP == OP_BOR) atomicOr(q, (unsigned long long) v);
+    else atomicXor(q, (unsigned long long) v);
+}
+
+/* Overlapping blocks of R bytes (one IDX level in any block order, or one VEC level
+ * whose stride is under its block) under one of those operators:
+ * every packed element in the range is folded into its target element by one L2
+ * reduction.  The operators are commutative and associative on integers, so the
+ * target ends equal to the reference's in-order application (src/backend/seq/
+ * genpup.py:119-211 with the operators of :302-327) whatever order the L2 applies the
+ * contributions in, and no lane reads the target or resolves which block comes first.
+ * Lane k of a warp takes packed element u0 + k, so the lanes of one block reduce into
+ * consecutive target elements (one L2 sector request per 32 bytes).  Both sides are
+ * aligned to the element size (checked on the host). */
+template <int BT, int OP, int K>
+__global__ void __launch_bounds__(YK_THREADS)
+yk_red_kernel(const __grid_constant__ yk_launch L)
+{
+    typedef typename yk_elem<BT>::T T;
+    constexpr uint32_t es = (uint32_t) sizeof(T);
+    constexpr int U = 4;        /* elements per lane, their loads issued together */
+    const yk_level & lv = L.desc.lv[0];
+    const uint32_t p0 = (uint32_t) L.p0;
+    const uint32_t nunits = (uint32_t) (L.nbytes / es);
+    const T *packed = (const T *) L.packed;     /* element 0 is packed byte p0 */
+    char *typed = L.typed + L.desc.base;
+    const uint32_t nthr = gridDim.x * YK_THREADS;
+    for (uint32_t u0 = blockIdx.x * YK_THREADS + threadIdx.x; u0 < nunits; u0 += U * nthr) {
+        int64_t x[U];
+        T in[U];
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            const uint32_t u = u0 + k * nthr;
+            if (u < nunits) {
+                const uint32_t p = p0 + u * es;
+                const uint32_t b = yk_div(p, lv);
+                const int64_t at = K == YK_LV_IDX ? __ldg(lv.disp + b) : (int64_t) b * lv.stride;
+                x[k] = at + (int64_t) (p - b * (uint32_t) lv.cps);
+                in[k] = __ldg(packed + u);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < U; k++)
+            if (u0 + k * nthr < nunits)
+                yk_red<OP>((T *) (typed + x[k]), in[k]);
+    }
+}
+
 /* Sorted blocks: descriptor = IDX(nblk, disp sorted ascending, cps = R) over a run of
  * R bytes of one base type.  Every target element that receives data gets exactly one
  * owner: the thread of its first in-range contributor, which applies the
@@ -2157,6 +2230,41 @@ extern "C" int yk_cuda_launch_runs_pack(const yk_launch * l, uint32_t run, void 
     return (int) cudaGetLastError();
 }
 
+/* yk_red_kernel for a 4- or 8-byte integer type and an operator that yk_red_applies()
+ * accepts; false when the launch does not fit it */
+template <int BT, int K>
+static bool yk_red_launch_bt(const yk_launch & c, cudaStream_t s, unsigned g)
+{
+    switch ((int) c.op) {
+#define YK_RD(O) case O: yk_red_kernel<BT, O, K><<<g, YK_THREADS, 0, s>>>(c); return true
+        YK_RD(OP_MAX); YK_RD(OP_MIN); YK_RD(OP_SUM); YK_RD(OP_BAND); YK_RD(OP_BOR); YK_RD(OP_BXOR);
+#undef YK_RD
+    }
+    return false;
+}
+
+static std::atomic<unsigned long long> yk_red_count(0);
+
+extern "C" unsigned long long yk_cuda_red_launches(void)
+{
+    return yk_red_count.load(std::memory_order_relaxed);
+}
+
+static bool yk_red_launch(const yk_launch & c, int bt, cudaStream_t s, int cap)
+{
+    const int k = c.desc.lv[0].kind;
+    if (c.use64 || c.desc.nlev != 1 || (k != YK_LV_IDX && k != YK_LV_VEC) ||
+        c.desc.lv[0].cps >= (1ull << 32) || !yk_red_applies(bt, c.op))
+        return false;
+    const uint64_t units = c.nbytes / (uint64_t) yk_bt_size(bt);
+    const unsigned g = yk_grid(units, (uint64_t) YK_THREADS * 4, cap > 0 ? cap : 8);
+    if (bt == YK_BT_I32)
+        return k == YK_LV_IDX ? yk_red_launch_bt<YK_BT_I32, YK_LV_IDX>(c, s, g) :
+            yk_red_launch_bt<YK_BT_I32, YK_LV_VEC>(c, s, g);
+    return k == YK_LV_IDX ? yk_red_launch_bt<YK_BT_I64, YK_LV_IDX>(c, s, g) :
+        yk_red_launch_bt<YK_BT_I64, YK_LV_VEC>(c, s, g);
+}
+
 extern "C" int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blocks, void *stream,
                                              int ctas_per_sm)
 {
@@ -2165,6 +2273,12 @@ extern "C" int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blo
         return 0;
     const yk_launch & c = *l;
     int bt = c.desc.leaf_type;
+    /* order-independent integer operators on aligned equal blocks: L2 reductions */
+    if ((sorted_blocks & YK_ORD_RED) && yk_red_launch(c, bt, s, ctas_per_sm)) {
+        yk_red_count.fetch_add(1, std::memory_order_relaxed);
+        return (int) cudaGetLastError();
+    }
+    sorted_blocks &= 3;
     bool typed_ok = sorted_blocks == 2 && (bt == YK_BT_I8 || bt == YK_BT_I16 || bt == YK_BT_I32 ||
                                            bt == YK_BT_I64 || bt == YK_BT_F32 || bt == YK_BT_F64 ||
                                            bt == YK_BT_C32 || bt == YK_BT_C64);

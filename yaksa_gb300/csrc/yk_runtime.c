@@ -51,6 +51,8 @@ static struct {
     int host_direct;            /* 0: host memory is never addressed in place, always
                                  * staged (YAKSA_GB300_HOST_DIRECT=0) */
     int tma_mode;               /* TMA forms: 0 off, 1 autotuner candidates, 2 forced */
+    int red_mode;               /* L2 reductions for order-independent integer operators
+                                 * on overlapping blocks: 0 off, 1 where they apply */
     int hidx_forced;            /* contiguous-block hindexed: 1 = hidx_cfg, 0 = autotuner */
     yk_tune_cfg hidx_cfg;
     /* library streams: requests that are not stream-ordered go round robin over
@@ -67,7 +69,7 @@ static struct {
     size_t nev, capev;
     /* counters (yaksa_gb300_stats) */
     uint64_t launches, staged_calls, direct_calls, memcpy_calls;
-} R = { .mu = PTHREAD_MUTEX_INITIALIZER, .tma_mode = -1 };
+} R = { .mu = PTHREAD_MUTEX_INITIALIZER, .tma_mode = -1, .red_mode = -1 };
 
 /* a library stream for a request that is not stream-ordered (round robin) */
 static cudaStream_t lib_stream(void)
@@ -121,6 +123,10 @@ static int runtime_ready(void)
             if (R.tma_mode < 0) {
                 const char *tm = getenv("YAKSA_GB300_TMA");
                 R.tma_mode = tm && tm[0] >= '0' && tm[0] <= '2' ? tm[0] - '0' : 1;
+            }
+            if (R.red_mode < 0) {
+                const char *rm = getenv("YAKSA_GB300_L2_REDUCE");
+                R.red_mode = !(rm && rm[0] == '0');
             }
             const char *hd = getenv("YAKSA_GB300_HOST_DIRECT");
             R.host_direct = !(hd && hd[0] == '0');
@@ -540,6 +546,19 @@ static int prepare_with(const yk_plan * p, char *typed, char *packed, yk_launch 
             if (es && (a % es) == 0 && (uint64_t) ddo->elem_align >= es)
                 *sorted = 2;
         }
+        if (__atomic_load_n(&R.red_mode, __ATOMIC_RELAXED) > 0 && ddo->idx_blocks &&
+            L->typed_op && L->desc.nlev == 1 && !L->use64 &&
+            (L->desc.lv[0].kind == YK_LV_IDX || L->desc.lv[0].kind == YK_LV_VEC) &&
+            L->desc.lv[0].cps < (1ull << 32) && yk_red_applies(L->desc.leaf_type, L->op)) {
+            /* equal blocks, in any order or at a stride under their length, under an
+             * order-independent integer operator: L2 reductions, when both sides sit on
+             * the element size */
+            uint64_t es = (uint64_t) yk_base_type_size(L->desc.leaf_type);
+            uint64_t a = (uint64_t) (uintptr_t) (typed + L->desc.base) | (uint64_t) (uintptr_t) packed |
+                b0 | (uint64_t) ddo->elem_align;
+            if (es && (a % es) == 0 && (uint64_t) ddo->elem_align >= es)
+                *sorted |= YK_ORD_RED;
+        }
         if (!L->typed_op && !*sorted)
             L->vec = (int) YK_MIN((uint64_t) L->vec, (uint64_t) ddo->vec_align);
     } else {
@@ -643,6 +662,17 @@ static int launch_prepared(const yk_plan * p, const yk_launch * L, int kind, int
 }
 
 /* TMA forms: 0 never, 1 as autotuner candidates (default), 2 always where one exists */
+int yaksa_gb300_debug_l2_reduce(int mode, unsigned long long *launches)
+{
+    if (mode > 1)
+        return YAKSA_ERR__INTERNAL;
+    if (mode >= 0)
+        __atomic_store_n(&R.red_mode, mode, __ATOMIC_RELAXED);
+    if (launches)
+        *launches = yk_cuda_red_launches();
+    return YAKSA_SUCCESS;
+}
+
 int yaksa_gb300_debug_tma(int mode)
 {
     if (mode < 0 || mode > 2)
@@ -1693,8 +1723,10 @@ static int server_plan(yaksa_gb300_pup_t * o, yaksa_info_t info, yk_srv_req * q)
         skind = YK_SRV_TYPED;
         gran = (uint64_t) L.vec;
     } else {
-        skind = sorted ? YK_SRV_OWNER : YK_SRV_ORDERED;
-        gran = sorted ? (uint64_t) yk_base_type_size(L.desc.leaf_type) : (uint64_t) L.vec;
+        /* the server's owner kernel needs sorted blocks; it has no L2-reduction form */
+        const int owner = (sorted & 3) != 0;
+        skind = owner ? YK_SRV_OWNER : YK_SRV_ORDERED;
+        gran = owner ? (uint64_t) yk_base_type_size(L.desc.leaf_type) : (uint64_t) L.vec;
     }
     q->L = L;
     q->skind = skind;
