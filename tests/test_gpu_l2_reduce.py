@@ -178,3 +178,36 @@ def test_red_extreme_values(cuda, prod, oracle):
             assert_same_bytes(host_of(cuda, t_p), t_o, f"{name} op {op}")
             prod.type_free(tp)
             oracle.type_free(to)
+
+
+def test_red_through_server(cuda, prod, oracle):
+    """The persistent server's reduction items: requests of about 0.5-1 MB, cut into many
+    items that run on different CTAs in any order, each against the oracle; the server
+    is destroyed before the library is used again."""
+    srv = yk.Server(prod)
+    try:
+        cases = [(yk.TYPE_INT64_T, 8, yk.OP_MAX, True), (yk.TYPE_UINT32_T, 4, yk.OP_BXOR, True),
+                 (yk.TYPE_INT32_T, 4, yk.OP_SUM, False), (yk.TYPE_INT64_T, 8, yk.OP_BAND, False)]
+        for k, (h, es, op, sort) in enumerate(cases):
+            rng = np.random.default_rng(900 + k)
+            offs = overlapping_offsets(rng, 1 << 14, 20000, sort)
+            tp = prod.type_create_indexed_block(8, offs, h)
+            to = oracle.type_create_indexed_block(8, offs, h)
+            lo, text = oracle.true_extent(to)
+            P = oracle.size(to)
+            typed0 = fill(rng, text, "int32")
+            packed0 = fill(rng, P, "int32")
+            t_o = typed0.copy()
+            oracle.unpack(packed0.ctypes.data, P, t_o.ctypes.data - lo, 1, to, 0, op=op)
+            t_p, p_p = dev_copy(cuda, typed0), dev_copy(cuda, packed0)
+            o = yk.unpack_op(p_p.data_ptr(), P, t_p.data_ptr() - lo, 1, tp, 0, op=op)
+            t = srv.submit(o)
+            assert t is not None
+            srv.wait(t)
+            assert o.actual == P
+            assert_same_bytes(host_of(cuda, t_p), t_o, f"server op {op}")
+            assert srv.stats()["items"] >= 2
+            prod.type_free(tp)
+            oracle.type_free(to)
+    finally:
+        srv.destroy()

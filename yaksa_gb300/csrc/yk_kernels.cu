@@ -1572,6 +1572,46 @@ __device__ void yk_srv_owner(const yk_launch & L, uint64_t ub, uint64_t ue)
     }
 }
 
+/* overlapping equal blocks under an order-independent integer operator (the launch
+ * form is yk_red_kernel): elements [ub, ue) of the request, each folded into its target
+ * by one L2 reduction */
+template <int BT, int OP>
+__device__ __forceinline__ void yk_srv_red_t(const yk_launch & L, uint64_t ub, uint64_t ue)
+{
+    typedef typename yk_elem<BT>::T T;
+    const yk_level & lv = L.desc.lv[0];
+    const uint64_t es = sizeof(T), p0 = L.p0;
+    char *typed = L.typed + L.desc.base;
+    for (uint64_t u = ub + threadIdx.x; u < ue; u += YK_THREADS) {
+        const uint64_t p = p0 + u * es;
+        const uint64_t b = yk_div(p, lv);
+        const int64_t at = lv.kind == YK_LV_IDX ? __ldg(lv.disp + b) : (int64_t) b * lv.stride;
+        const T v = *(const T *) (L.packed + (p - p0));
+        yk_red<OP>((T *) (typed + at + (int64_t) (p - b * lv.cps)), v);
+    }
+}
+
+template <int BT>
+__device__ __forceinline__ void yk_srv_red_bt(const yk_launch & L, uint64_t ub, uint64_t ue)
+{
+    switch ((int) L.op) {
+        case OP_MAX: yk_srv_red_t<BT, OP_MAX>(L, ub, ue); break;
+        case OP_MIN: yk_srv_red_t<BT, OP_MIN>(L, ub, ue); break;
+        case OP_SUM: yk_srv_red_t<BT, OP_SUM>(L, ub, ue); break;
+        case OP_BAND: yk_srv_red_t<BT, OP_BAND>(L, ub, ue); break;
+        case OP_BOR: yk_srv_red_t<BT, OP_BOR>(L, ub, ue); break;
+        case OP_BXOR: yk_srv_red_t<BT, OP_BXOR>(L, ub, ue); break;
+    }
+}
+
+__device__ void yk_srv_red(const yk_launch & L, uint64_t ub, uint64_t ue)
+{
+    if (L.desc.leaf_type == YK_BT_I32)
+        yk_srv_red_bt<YK_BT_I32>(L, ub, ue);
+    else if (L.desc.leaf_type == YK_BT_I64)
+        yk_srv_red_bt<YK_BT_I64>(L, ub, ue);
+}
+
 /* the whole request, in order, by warp 0 (targets that overlap arbitrarily) */
 __device__ void yk_srv_ordered(const yk_launch & L, uint64_t ub, uint64_t ue)
 {
@@ -1704,7 +1744,7 @@ __device__ __forceinline__ void yk_srv_item_done(const yk_server_args & A, uint3
 /* a record the GPU can act on: a known kind, a sane unit and an ordered range */
 __device__ __forceinline__ bool yk_item_ok(const yk_item & it, const yk_launch & L)
 {
-    if ((it.kind & ~YK_SRV_TIMED) > YK_SRV_HIDX || it.pe <= it.pb || it.pb < L.p0 ||
+    if ((it.kind & ~YK_SRV_TIMED) > YK_SRV_LAST || it.pe <= it.pb || it.pb < L.p0 ||
         it.pe > L.p0 + L.nbytes)
         return false;
     if (L.vec != 1 && L.vec != 2 && L.vec != 4 && L.vec != 8 && L.vec != 16)
@@ -1863,6 +1903,10 @@ yk_server_kernel(const __grid_constant__ yk_server_args A)
                 break;
             case YK_SRV_ORDERED:
                 yk_srv_ordered(sL, ub, ue);
+                break;
+            case YK_SRV_RED:
+                yk_srv_red(sL, (it.pb - sL.p0) / (uint64_t) yk_bt_size(sL.desc.leaf_type),
+                           (it.pe - sL.p0) / (uint64_t) yk_bt_size(sL.desc.leaf_type));
                 break;
             default:
 #define YK_SH(V) do { if (sL.dir == 0) yk_srv_hidx<V, 0>(sL, it.pb, it.pe); \
