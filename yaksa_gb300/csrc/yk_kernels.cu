@@ -1276,10 +1276,20 @@ yk_owner_lane_kernel(const __grid_constant__ yk_launch L, int rshift)
     }
 }
 
-/* The same for elements of 1, 2 or 4 bytes, one CW-byte packed chunk per lane (CW 8 or
- * 16): the chunk's elements share one block (blocks are a multiple of CW bytes long and
- * the range and the packed pointer sit on CW bytes, checked on the host), so its
- * displacement words and the packed load serve CW/es elements. */
+/* The same with one CW-byte packed chunk per lane (CW 8 or 16; elements of 1, 2 or 4
+ * bytes, or 8-byte elements other than double): the chunk's elements share one block
+ * (blocks are a multiple of CW bytes long and the range and the packed pointer sit on
+ * CW bytes, checked on the host), so its displacement words and the packed load serve
+ * CW/es elements.
+ *
+ * With at most four elements per chunk the fold has no loop for the common cases: the
+ * displacements of the next two blocks are loaded with the chunk's own, their
+ * contributions are loaded by predicated loads, and each is folded in by a select.  A
+ * warp then executes one instruction stream with all its lanes, instead of a branch
+ * per owner and a loop of dependent loads run by a few lanes (which left 12.8 of 32
+ * lanes active per instruction).  Only a third later block, rare at these shapes,
+ * takes the loop.  double keeps yk_owner_lane_kernel: there every fold is a DADD on
+ * GB300's narrow FP64 pipe, which the selects would spend on every lane. */
 template <int BT, int OP, int CW>
 __global__ void __launch_bounds__(YK_THREADS)
 yk_owner_chunk_kernel(const __grid_constant__ yk_launch L, int rshift)
@@ -1310,31 +1320,90 @@ yk_owner_chunk_kernel(const __grid_constant__ yk_launch L, int rshift)
         const int64_t x0 = d + (int64_t) (p & (R - 1));
         bool own[E];
         T out[E];
+        if constexpr (E <= 4) {
+            const int64_t dn2 = b + 2 < nblk ? __ldg(lv.disp + b + 2) : INT64_MAX;
+            bool h1[E], h2[E];
+            T c1[E], c2[E];
 #pragma unroll
-        for (int k = 0; k < E; k++) {
-            const int64_t x = x0 + (int64_t) k * es;
-            /* an earlier in-range block owns this element */
-            own[k] = !(b > 0 && x < dp + (int64_t) R && (b - 1) * R + (uint32_t) (x - dp) >= p0);
-            if (own[k])
-                out[k] = *(const T *) (typed + x);
-        }
-#pragma unroll
-        for (int k = 0; k < E; k++) {
-            if (!own[k])
-                continue;
-            const int64_t x = x0 + (int64_t) k * es;
-            yk_elem<BT>::op(OP, in.e[k], out[k]);
-            /* the blocks after this one that start at or before x, in block order */
-            int64_t dd = dn;
-            for (uint32_t bb = b + 1; bb < nblk && dd <= x;) {
-                const uint64_t pp = ((uint64_t) bb << rshift) + (uint64_t) (x - dd);
-                if (pp >= p1)
-                    break;
-                yk_elem<BT>::op(OP, __ldg(packed + ((uint32_t) pp - p0) / es), out[k]);
-                bb++;
-                dd = bb < nblk ? __ldg(lv.disp + bb) : INT64_MAX;
+            for (int k = 0; k < E; k++) {
+                const int64_t x = x0 + (int64_t) k * es;
+                /* an earlier in-range block owns this element */
+                own[k] = !(b > 0 && x < dp + (int64_t) R && (b - 1) * R + (uint32_t) (x - dp) >= p0);
+                if (own[k])
+                    out[k] = *(const T *) (typed + x);
+                /* the next two blocks' elements at x, when they exist and are in range (a
+                 * later block places x later in the packed stream still) */
+                h1[k] = false;
+                h2[k] = false;
+                c1[k] = c2[k] = T();
+                if (own[k] && dn <= x) {
+                    const uint64_t q1 = ((uint64_t) (b + 1) << rshift) + (uint64_t) (x - dn);
+                    if (q1 < p1) {
+                        h1[k] = true;
+                        c1[k] = __ldg(packed + ((uint32_t) q1 - p0) / es);
+                        if (dn2 <= x) {
+                            const uint64_t q2 = ((uint64_t) (b + 2) << rshift) + (uint64_t) (x - dn2);
+                            if (q2 < p1) {
+                                h2[k] = true;
+                                c2[k] = __ldg(packed + ((uint32_t) q2 - p0) / es);
+                            }
+                        }
+                    }
+                }
             }
-            *(T *) (typed + x) = out[k];
+#pragma unroll
+            for (int k = 0; k < E; k++) {
+                const int64_t x = x0 + (int64_t) k * es;
+                T v = out[k];
+                yk_elem<BT>::op(OP, in.e[k], v);
+                T t = v;
+                yk_elem<BT>::op(OP, c1[k], t);
+                v = h1[k] ? t : v;
+                t = v;
+                yk_elem<BT>::op(OP, c2[k], t);
+                v = h2[k] ? t : v;
+                if (h2[k]) {
+                    /* rare: the blocks after those, in block order */
+                    for (uint32_t bb = b + 3; bb < nblk; bb++) {
+                        const int64_t d3 = __ldg(lv.disp + bb);
+                        if (d3 > x)
+                            break;
+                        const uint64_t pp = ((uint64_t) bb << rshift) + (uint64_t) (x - d3);
+                        if (pp >= p1)
+                            break;
+                        yk_elem<BT>::op(OP, __ldg(packed + ((uint32_t) pp - p0) / es), v);
+                    }
+                }
+                if (own[k])
+                    *(T *) (typed + x) = v;
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < E; k++) {
+                const int64_t x = x0 + (int64_t) k * es;
+                /* an earlier in-range block owns this element */
+                own[k] = !(b > 0 && x < dp + (int64_t) R && (b - 1) * R + (uint32_t) (x - dp) >= p0);
+                if (own[k])
+                    out[k] = *(const T *) (typed + x);
+            }
+#pragma unroll
+            for (int k = 0; k < E; k++) {
+                if (!own[k])
+                    continue;
+                const int64_t x = x0 + (int64_t) k * es;
+                yk_elem<BT>::op(OP, in.e[k], out[k]);
+                /* the blocks after this one that start at or before x, in block order */
+                int64_t dd = dn;
+                for (uint32_t bb = b + 1; bb < nblk && dd <= x;) {
+                    const uint64_t pp = ((uint64_t) bb << rshift) + (uint64_t) (x - dd);
+                    if (pp >= p1)
+                        break;
+                    yk_elem<BT>::op(OP, __ldg(packed + ((uint32_t) pp - p0) / es), out[k]);
+                    bb++;
+                    dd = bb < nblk ? __ldg(lv.disp + bb) : INT64_MAX;
+                }
+                *(T *) (typed + x) = out[k];
+            }
         }
     }
 }
