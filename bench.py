@@ -377,7 +377,8 @@ SUITE_PROFILE = {("hindexed", "pack"): ("yk_hidx32_kernel_hindexed", "pack", 2),
                  ("hindexed", "unpack"): ("yk_hidx32_kernel_hindexed_unpack", "unpack", 2),
                  ("struct", "pack"): ("yk_runs_pack_kernel_struct", "pack", 2),
                  ("struct", "unpack"): ("yk_regular_kernel_struct", "unpack", 2),
-                 ("reduce_double", "unpack"): ("yk_owner_lane_kernel_reduce", "double_sum", 2),
+                 ("reduce_double", "unpack"): ("yk_owner_lane_kernel_reduce", "double_sum_full", 1),
+                 ("reduce_c_complex", "unpack"): ("yk_owner_chunk_kernel_reduce_complex", "complex_prod", 1),
                  ("reduce_uint32", "unpack"): ("yk_red_kernel_reduce", "uint32_bxor", 1),
                  ("reduce_int64", "unpack"): ("yk_red_kernel_reduce", "int64_max", 1)}
 
