@@ -211,3 +211,29 @@ def test_red_through_server(cuda, prod, oracle):
             oracle.type_free(to)
     finally:
         srv.destroy()
+
+
+@pytest.mark.parametrize("op", [yk.OP_SUM, yk.OP_BXOR])
+def test_red_not_sent_to_host_memory(cuda, prod, oracle, op):
+    """A typed buffer in pinned host memory, which the GPU addresses in place over the
+    C2C link: the reductions stay on device memory, so the owner kernels run, and the
+    bytes match the oracle."""
+    rng = np.random.default_rng(op + 300)
+    offs = overlapping_offsets(rng, 3000, 2000, True)
+    tp = prod.type_create_indexed_block(8, offs, yk.TYPE_INT32_T)
+    to = oracle.type_create_indexed_block(8, offs, yk.TYPE_INT32_T)
+    lo, text = oracle.true_extent(to)
+    P = oracle.size(to)
+    typed0 = fill(rng, text, "int32")
+    packed0 = fill(rng, P, "int32")
+    t_o = typed0.copy()
+    oracle.unpack(packed0.ctypes.data, P, t_o.ctypes.data - lo, 1, to, 0, op=op)
+    t_h = cuda.from_numpy(typed0.copy()).pin_memory()
+    p_p = dev_copy(cuda, packed0)
+    before = red_launches(prod)
+    prod.unpack(p_p.data_ptr(), P, t_h.data_ptr() - lo, 1, tp, 0, op=op)
+    cuda.cuda.synchronize()
+    assert red_launches(prod) - before == 0
+    assert_same_bytes(t_h.numpy(), t_o, f"host target op {op}")
+    prod.type_free(tp)
+    oracle.type_free(to)

@@ -356,6 +356,19 @@ static char *device_alias(const char *base, const char *probe, int host_hint, in
     }
 }
 
+/* 1 when p lies in device or managed memory: the reductions of yk_red_kernel are sent
+ * only there, never to host memory the GPU reaches over the C2C link */
+static int device_memory(const void *p)
+{
+    struct cudaPointerAttributes a;
+    memset(&a, 0, sizeof(a));
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
 static int pow2_of(uint64_t v)
 {
     int a = 16;
@@ -556,7 +569,7 @@ static int prepare_with(const yk_plan * p, char *typed, char *packed, yk_launch 
             uint64_t es = (uint64_t) yk_base_type_size(L->desc.leaf_type);
             uint64_t a = (uint64_t) (uintptr_t) (typed + L->desc.base) | (uint64_t) (uintptr_t) packed |
                 b0 | (uint64_t) ddo->elem_align;
-            if (es && (a % es) == 0 && (uint64_t) ddo->elem_align >= es)
+            if (es && (a % es) == 0 && (uint64_t) ddo->elem_align >= es && device_memory(typed))
                 *sorted |= YK_ORD_RED;
         }
         if (!L->typed_op && !*sorted)
