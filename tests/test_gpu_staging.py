@@ -33,3 +33,17 @@ def test_staging_ring(cuda):
     assert not bad, res
     # 17 single requests and 40 in flight, every one staged; none addressed in place
     assert res["staged_calls"] == 57 and res["direct_calls"] == 0, res
+
+
+def test_wait_kernel_hint(cuda):
+    """yaksa_init with yaksa_has_wait_kernel=true in a library told to stage every host
+    buffer: pageable and pinned host buffers are used in place (no staging ring, whose
+    pinned half would synchronize the device), and every result matches the oracle."""
+    env = dict(os.environ, YAKSA_GB300_HOST_DIRECT="0")
+    r = subprocess.run([sys.executable, os.path.join(HERE, "wait_kernel_child.py")], env=env,
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-4000:]
+    res = json.loads(r.stdout.strip().splitlines()[-1])
+    bad = [k for k, v in res.items() if v is False]
+    assert not bad, res
+    assert res["staged_calls"] == 0 and res["direct_calls"] == 4, res

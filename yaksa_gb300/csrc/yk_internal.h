@@ -112,7 +112,8 @@ uintptr_t yk_builtin_floor(yk_type * t, uintptr_t count, uintptr_t pos);
 void yk_iov_release(yk_type * t);
 
 /* GPU runtime (yk_runtime.c) */
-int yk_runtime_init(void);
+/* has_wait_kernel: the yaksa_has_wait_kernel hint of yaksa_init's info */
+int yk_runtime_init(int has_wait_kernel);
 void yk_runtime_finalize(void);
 int yk_pup(int dir, const void *packed_in, void *packed_out, char *typed, uintptr_t count,
            yk_type * t, uintptr_t offset, uintptr_t maxbytes, uintptr_t * actual,

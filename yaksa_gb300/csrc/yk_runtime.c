@@ -50,6 +50,11 @@ static struct {
     int host_ptr_ok;            /* registered host memory uses the host address */
     int host_direct;            /* 0: host memory is never addressed in place, always
                                  * staged (YAKSA_GB300_HOST_DIRECT=0) */
+    int has_wait_kernel;        /* yaksa_init's yaksa_has_wait_kernel hint: the caller may
+                                 * keep a kernel resident that waits on the host, so no
+                                 * call may synchronize the device (the reference:
+                                 * src/backend/src/yaksuri_progress.c:17-27,
+                                 * src/backend/cuda/hooks/yaksuri_cuda_init_hooks.c:14-64) */
     int tma_mode;               /* TMA forms: 0 off, 1 autotuner candidates, 2 forced */
     int red_mode;               /* L2 reductions for order-independent integer operators
                                  * on overlapping blocks: 0 off, 1 where they apply */
@@ -87,10 +92,11 @@ static int cuda_err(cudaError_t e, const char *what)
     return e == cudaErrorMemoryAllocation ? YAKSA_ERR__OUT_OF_MEM : YAKSA_ERR__INTERNAL;
 }
 
-int yk_runtime_init(void)
+int yk_runtime_init(int has_wait_kernel)
 {
     /* the GPU is brought up lazily at the first pack/unpack so that type
      * construction works on hosts without a GPU */
+    __atomic_store_n(&R.has_wait_kernel, has_wait_kernel ? 1 : 0, __ATOMIC_RELAXED);
     return YAKSA_SUCCESS;
 }
 
@@ -341,7 +347,7 @@ static char *device_alias(const char *base, const char *probe, int host_hint, in
         case cudaMemoryTypeManaged:
             return (char *) base;
         case cudaMemoryTypeHost:
-            if (!R.host_direct) {
+            if (!R.host_direct && !R.has_wait_kernel) {
                 *staged = 1;
                 return NULL;
             }
@@ -349,7 +355,10 @@ static char *device_alias(const char *base, const char *probe, int host_hint, in
                 return (char *) base + ((const char *) a.devicePointer - probe);
             return (char *) base;
         default:
-            if (R.pageable_access && R.host_direct)
+            /* with a wait kernel, pageable memory the GPU can reach is used in place even
+             * when staging was asked for: the reference likewise treats unregistered host
+             * buffers as registered then */
+            if (R.pageable_access && (R.host_direct || R.has_wait_kernel))
                 return (char *) base;
             *staged = 1;
             return NULL;
@@ -757,6 +766,7 @@ typedef struct {
     int nslabs;
     size_t slab;                /* bytes of one side (packed or typed) of one slab */
     char *dev, *host;           /* nslabs x 2 x (slab + 16) */
+    int host_pageable;          /* host half from malloc (a wait kernel), else pinned */
     cudaEvent_t ev_in[YK_STAGE_MAX_SLABS], ev_run[YK_STAGE_MAX_SLABS],
         ev_free[YK_STAGE_MAX_SLABS], ev_start, ev_end;
     cudaStream_t s_in, s_run, s_out;
@@ -785,7 +795,14 @@ static int stage_ready(void)
         ST.dev = NULL;
         return YAKSA_ERR__OUT_OF_MEM;
     }
-    if (yk_fail_injected() || cudaHostAlloc((void **) &ST.host, bytes, cudaHostAllocPortable) != cudaSuccess) {
+    /* with a wait kernel the host half is plain host memory: pinning it
+     * (cudaHostAlloc) would synchronize the device against that kernel */
+    ST.host_pageable = R.has_wait_kernel;
+    if (ST.host_pageable)
+        ST.host = yk_fail_injected() ? NULL : malloc(bytes);
+    else if (yk_fail_injected() || cudaHostAlloc((void **) &ST.host, bytes, cudaHostAllocPortable) != cudaSuccess)
+        ST.host = NULL;
+    if (!ST.host) {
         cudaFree(ST.dev);
         ST.dev = ST.host = NULL;
         return YAKSA_ERR__OUT_OF_MEM;
@@ -832,7 +849,10 @@ static void stage_finalize(void)
         cudaStreamDestroy(ST.s_run);
         cudaStreamDestroy(ST.s_out);
         cudaFree(ST.dev);
-        cudaFreeHost(ST.host);
+        if (ST.host_pageable)
+            free(ST.host);
+        else
+            cudaFreeHost(ST.host);
         ST.dev = ST.host = NULL;
         ST.ready = 0;
     }

@@ -251,7 +251,6 @@ static int add_int_alias(size_t sz, yaksa_type_t h)
 
 int yaksa_init(yaksa_info_t info)
 {
-    (void) info;
     int rc = YAKSA_SUCCESS;
     pthread_mutex_lock(&yk_init_mutex);
     if (yk_init_refs > 0) {
@@ -326,7 +325,7 @@ int yaksa_init(yaksa_info_t info)
     ADD_PAIR(YAKSA_TYPE__SHORT_INT, short, int_bt(sizeof(short)), int, int_bt(sizeof(int)));
     ADD_PAIR(YAKSA_TYPE__LONG_DOUBLE_INT, long double, YK_BT_LDOUBLE, int, int_bt(sizeof(int)));
 
-    rc = yk_runtime_init();
+    rc = yk_runtime_init(info ? ((yk_info *) info)->has_wait_kernel : 0);
     if (rc)
         goto fail_unlocked_rc;
     __atomic_store_n(&yk_init_refs, 1, __ATOMIC_RELEASE);
