@@ -733,6 +733,7 @@ static int build(yk_type * t, int typed, yk_devdesc * dd, int to_device)
     dd->may_overlap = check_overlap(&b, &span);
     dd->sorted_blocks = 0;
     dd->idx_blocks = 0;
+    dd->disp32 = 0;
     if (dd->may_overlap && typed && b.leaf == YK_LEAF_RUN && b.nlev == 1 &&
         b.lv[0].kind == YK_LV_VEC && b.lv[0].cps == b.run)
         dd->idx_blocks = 1;
@@ -743,6 +744,10 @@ static int build(yk_type * t, int typed, yk_devdesc * dd, int to_device)
         for (uint64_t j = 1; j < b.lv[0].count && sorted; j++)
             sorted = b.lv[0].disp[j] >= b.lv[0].disp[j - 1];
         dd->sorted_blocks = sorted;
+        /* sorted: the first and last displacements bound every target offset */
+        const uint64_t n = b.lv[0].count;
+        dd->disp32 = sorted && n > 0 && b.run < (1ull << 30) && b.lv[0].disp[0] >= INT32_MIN &&
+            b.lv[0].disp[n - 1] <= (int64_t) INT32_MAX - (int64_t) b.run;
     }
     dd->elem_span = span;
     int rc = upload(&b, dd, to_device);

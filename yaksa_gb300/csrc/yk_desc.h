@@ -200,6 +200,9 @@ int yk_cuda_launch_pup_cfg(const yk_launch * l, void *stream, int units_per_thre
  * under an operator that yk_red_applies() accepts -- the launch folds the elements in
  * with L2 reductions. */
 #define YK_ORD_RED 4
+/* set with sorted_blocks 2: every target offset (displacement + position in its block)
+ * fits in a signed 32-bit integer, so the chunk kernel may compute offsets in 32 bits */
+#define YK_ORD_D32 8
 int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blocks, void *stream,
                                   int ctas_per_sm);
 /* launches of the L2-reduction form so far */

@@ -20,6 +20,7 @@
  * libgcc's __mulsc3/__muldc3 implement for the reference's `*=` on _Complex values).
  */
 #include <atomic>
+#include <type_traits>
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "yk_desc.h"
@@ -1290,12 +1291,16 @@ yk_owner_lane_kernel(const __grid_constant__ yk_launch L, int rshift)
  * lanes active per instruction).  Only a third later block, rare at these shapes,
  * takes the loop.  double keeps yk_owner_lane_kernel: there every fold is a DADD on
  * GB300's narrow FP64 pipe, which the selects would spend on every lane. */
-template <int BT, int OP, int CW>
+template <int BT, int OP, int CW, bool D32>
 __global__ void __launch_bounds__(YK_THREADS)
 yk_owner_chunk_kernel(const __grid_constant__ yk_launch L, int rshift)
 {
     typedef typename yk_elem<BT>::T T;
     typedef typename yk_vec<CW>::T CT;
+    /* target offsets in 32 bits when the host found that every one fits (the
+     * displacements' low words are loaded), else in 64 bits */
+    typedef typename std::conditional<D32, int32_t, int64_t>::type OFF;
+    constexpr OFF OFF_MAX = D32 ? (OFF) INT32_MAX : (OFF) INT64_MAX;
     constexpr uint32_t es = (uint32_t) sizeof(T);
     constexpr int E = CW / (int) es;
     const uint32_t R = 1u << rshift;
@@ -1306,29 +1311,35 @@ yk_owner_chunk_kernel(const __grid_constant__ yk_launch L, int rshift)
     const CT *packedc = (const CT *) L.packed;  /* chunk 0 is byte p0 */
     const T *packed = (const T *) L.packed;
     char *typed = L.typed + L.desc.base;
+    auto disp = [&](uint32_t i) -> OFF {
+        if constexpr (D32)
+            return __ldg((const int32_t *) lv.disp + 2 * (size_t) i);   /* low word */
+        else
+            return __ldg(lv.disp + i);
+    };
     for (uint32_t u = blockIdx.x * YK_THREADS + threadIdx.x; u < nchunks; u += gridDim.x * YK_THREADS) {
         const uint32_t p = p0 + u * CW;
         const uint32_t b = p >> rshift;
-        const int64_t d = __ldg(lv.disp + b);
-        const int64_t dp = b > 0 ? __ldg(lv.disp + b - 1) : 0;
-        const int64_t dn = b + 1 < nblk ? __ldg(lv.disp + b + 1) : INT64_MAX;
+        const OFF d = disp(b);
+        const OFF dp = b > 0 ? disp(b - 1) : 0;
+        const OFF dn = b + 1 < nblk ? disp(b + 1) : OFF_MAX;
         union {
             CT w;
             T e[E];
         } in;
         in.w = __ldg(packedc + u);
-        const int64_t x0 = d + (int64_t) (p & (R - 1));
+        const OFF x0 = d + (OFF) (p & (R - 1));
         bool own[E];
         T out[E];
         if constexpr (E <= 4) {
-            const int64_t dn2 = b + 2 < nblk ? __ldg(lv.disp + b + 2) : INT64_MAX;
+            const OFF dn2 = b + 2 < nblk ? disp(b + 2) : OFF_MAX;
             bool h1[E], h2[E];
             T c1[E], c2[E];
 #pragma unroll
             for (int k = 0; k < E; k++) {
-                const int64_t x = x0 + (int64_t) k * es;
+                const OFF x = x0 + (OFF) (k * (int) es);
                 /* an earlier in-range block owns this element */
-                own[k] = !(b > 0 && x < dp + (int64_t) R && (b - 1) * R + (uint32_t) (x - dp) >= p0);
+                own[k] = !(b > 0 && x < dp + (OFF) R && (b - 1) * R + (uint32_t) (x - dp) >= p0);
                 if (own[k])
                     out[k] = *(const T *) (typed + x);
                 /* the next two blocks' elements at x, when they exist and are in range (a
@@ -1353,7 +1364,7 @@ yk_owner_chunk_kernel(const __grid_constant__ yk_launch L, int rshift)
             }
 #pragma unroll
             for (int k = 0; k < E; k++) {
-                const int64_t x = x0 + (int64_t) k * es;
+                const OFF x = x0 + (OFF) (k * (int) es);
                 T v = out[k];
                 yk_elem<BT>::op(OP, in.e[k], v);
                 T t = v;
@@ -1365,7 +1376,7 @@ yk_owner_chunk_kernel(const __grid_constant__ yk_launch L, int rshift)
                 if (h2[k]) {
                     /* rare: the blocks after those, in block order */
                     for (uint32_t bb = b + 3; bb < nblk; bb++) {
-                        const int64_t d3 = __ldg(lv.disp + bb);
+                        const OFF d3 = disp(bb);
                         if (d3 > x)
                             break;
                         const uint64_t pp = ((uint64_t) bb << rshift) + (uint64_t) (x - d3);
@@ -1380,9 +1391,9 @@ yk_owner_chunk_kernel(const __grid_constant__ yk_launch L, int rshift)
         } else {
 #pragma unroll
             for (int k = 0; k < E; k++) {
-                const int64_t x = x0 + (int64_t) k * es;
+                const OFF x = x0 + (OFF) (k * (int) es);
                 /* an earlier in-range block owns this element */
-                own[k] = !(b > 0 && x < dp + (int64_t) R && (b - 1) * R + (uint32_t) (x - dp) >= p0);
+                own[k] = !(b > 0 && x < dp + (OFF) R && (b - 1) * R + (uint32_t) (x - dp) >= p0);
                 if (own[k])
                     out[k] = *(const T *) (typed + x);
             }
@@ -1390,17 +1401,17 @@ yk_owner_chunk_kernel(const __grid_constant__ yk_launch L, int rshift)
             for (int k = 0; k < E; k++) {
                 if (!own[k])
                     continue;
-                const int64_t x = x0 + (int64_t) k * es;
+                const OFF x = x0 + (OFF) (k * (int) es);
                 yk_elem<BT>::op(OP, in.e[k], out[k]);
                 /* the blocks after this one that start at or before x, in block order */
-                int64_t dd = dn;
+                OFF dd = dn;
                 for (uint32_t bb = b + 1; bb < nblk && dd <= x;) {
                     const uint64_t pp = ((uint64_t) bb << rshift) + (uint64_t) (x - dd);
                     if (pp >= p1)
                         break;
                     yk_elem<BT>::op(OP, __ldg(packed + ((uint32_t) pp - p0) / es), out[k]);
                     bb++;
-                    dd = bb < nblk ? __ldg(lv.disp + bb) : INT64_MAX;
+                    dd = bb < nblk ? disp(bb) : OFF_MAX;
                 }
                 *(T *) (typed + x) = out[k];
             }
@@ -2246,18 +2257,21 @@ extern "C" int yk_cuda_launch_pup_cfg(const yk_launch * l, void *stream, int uni
  * 8-byte elements other than double; chunk = bytes per lane (0: the per-lane kernel) */
 template <int BT, int O>
 static bool yk_owner_chunk_launch(const yk_launch & c, int rshift, cudaStream_t s, unsigned g,
-                                  int chunk)
+                                  int chunk, bool d32)
 {
     if constexpr (sizeof(typename yk_elem<BT>::T) == 4 ||
                   (sizeof(typename yk_elem<BT>::T) == 8 && BT != YK_BT_F64)) {
         if (chunk == 16) {
-            yk_owner_chunk_kernel<BT, O, 16><<<g, YK_THREADS, 0, s>>>(c, rshift);
+            if (d32)
+                yk_owner_chunk_kernel<BT, O, 16, true><<<g, YK_THREADS, 0, s>>>(c, rshift);
+            else
+                yk_owner_chunk_kernel<BT, O, 16, false><<<g, YK_THREADS, 0, s>>>(c, rshift);
             return true;
         }
     }
     if constexpr (sizeof(typename yk_elem<BT>::T) < 8) {
         if (chunk == 8) {
-            yk_owner_chunk_kernel<BT, O, 8><<<g, YK_THREADS, 0, s>>>(c, rshift);
+            yk_owner_chunk_kernel<BT, O, 8, false><<<g, YK_THREADS, 0, s>>>(c, rshift);
             return true;
         }
     }
@@ -2268,10 +2282,11 @@ static bool yk_owner_chunk_launch(const yk_launch & c, int rshift, cudaStream_t 
 /* yk_owner_lane_kernel for (base type, operator) pairs in the operator table; false
  * when the pair has no instance (the caller falls back to the runtime-op kernels) */
 template <int BT>
-static bool yk_owner_lane_int(const yk_launch & c, int rshift, cudaStream_t s, unsigned g, int chunk)
+static bool yk_owner_lane_int(const yk_launch & c, int rshift, cudaStream_t s, unsigned g, int chunk,
+                              bool d32)
 {
     switch ((int) c.op) {
-#define YK_OL(O) case O: if (!yk_owner_chunk_launch<BT, O>(c, rshift, s, g, chunk))           \
+#define YK_OL(O) case O: if (!yk_owner_chunk_launch<BT, O>(c, rshift, s, g, chunk, d32))      \
                              yk_owner_lane_kernel<BT, O><<<g, YK_THREADS, 0, s>>>(c, rshift);  \
                          return true
         YK_OL(OP_MAX); YK_OL(OP_MIN); YK_OL(OP_SUM); YK_OL(OP_PROD); YK_OL(OP_LAND); YK_OL(OP_BAND);
@@ -2281,7 +2296,8 @@ static bool yk_owner_lane_int(const yk_launch & c, int rshift, cudaStream_t s, u
 }
 
 template <int BT>
-static bool yk_owner_lane_flt(const yk_launch & c, int rshift, cudaStream_t s, unsigned g, int chunk)
+static bool yk_owner_lane_flt(const yk_launch & c, int rshift, cudaStream_t s, unsigned g, int chunk,
+                              bool d32)
 {
     switch ((int) c.op) {
         YK_OL(OP_MAX); YK_OL(OP_MIN); YK_OL(OP_SUM); YK_OL(OP_PROD); YK_OL(OP_REPLACE);
@@ -2290,7 +2306,8 @@ static bool yk_owner_lane_flt(const yk_launch & c, int rshift, cudaStream_t s, u
 }
 
 template <int BT>
-static bool yk_owner_lane_cplx(const yk_launch & c, int rshift, cudaStream_t s, unsigned g, int chunk)
+static bool yk_owner_lane_cplx(const yk_launch & c, int rshift, cudaStream_t s, unsigned g, int chunk,
+                              bool d32)
 {
     switch ((int) c.op) {
         YK_OL(OP_SUM); YK_OL(OP_PROD); YK_OL(OP_REPLACE);
@@ -2299,7 +2316,8 @@ static bool yk_owner_lane_cplx(const yk_launch & c, int rshift, cudaStream_t s, 
     return false;
 }
 
-static bool yk_owner_lane_launch(const yk_launch & c, int bt, int rshift, cudaStream_t s, int cap)
+static bool yk_owner_lane_launch(const yk_launch & c, int bt, int rshift, cudaStream_t s, int cap,
+                                 bool d32)
 {
     const uint64_t es = (uint64_t) yk_bt_size(bt);
     /* chunks of CW bytes: blocks a multiple of CW bytes, range and packed pointer on CW
@@ -2319,14 +2337,14 @@ static bool yk_owner_lane_launch(const yk_launch & c, int bt, int rshift, cudaSt
     const uint64_t units = c.nbytes / (chunk ? (uint64_t) chunk : es);
     const unsigned g = yk_grid(units, YK_THREADS, cap > 0 ? cap : 16);
     switch (bt) {
-        case YK_BT_I8: return yk_owner_lane_int<YK_BT_I8>(c, rshift, s, g, chunk);
-        case YK_BT_I16: return yk_owner_lane_int<YK_BT_I16>(c, rshift, s, g, chunk);
-        case YK_BT_I32: return yk_owner_lane_int<YK_BT_I32>(c, rshift, s, g, chunk);
-        case YK_BT_I64: return yk_owner_lane_int<YK_BT_I64>(c, rshift, s, g, chunk);
-        case YK_BT_F32: return yk_owner_lane_flt<YK_BT_F32>(c, rshift, s, g, chunk);
-        case YK_BT_F64: return yk_owner_lane_flt<YK_BT_F64>(c, rshift, s, g, chunk);
-        case YK_BT_C32: return yk_owner_lane_cplx<YK_BT_C32>(c, rshift, s, g, chunk);
-        case YK_BT_C64: return yk_owner_lane_cplx<YK_BT_C64>(c, rshift, s, g, 0);
+        case YK_BT_I8: return yk_owner_lane_int<YK_BT_I8>(c, rshift, s, g, chunk, d32);
+        case YK_BT_I16: return yk_owner_lane_int<YK_BT_I16>(c, rshift, s, g, chunk, d32);
+        case YK_BT_I32: return yk_owner_lane_int<YK_BT_I32>(c, rshift, s, g, chunk, d32);
+        case YK_BT_I64: return yk_owner_lane_int<YK_BT_I64>(c, rshift, s, g, chunk, d32);
+        case YK_BT_F32: return yk_owner_lane_flt<YK_BT_F32>(c, rshift, s, g, chunk, d32);
+        case YK_BT_F64: return yk_owner_lane_flt<YK_BT_F64>(c, rshift, s, g, chunk, d32);
+        case YK_BT_C32: return yk_owner_lane_cplx<YK_BT_C32>(c, rshift, s, g, chunk, d32);
+        case YK_BT_C64: return yk_owner_lane_cplx<YK_BT_C64>(c, rshift, s, g, 0, d32);
     }
     return false;
 }
@@ -2391,6 +2409,7 @@ extern "C" int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blo
         yk_red_count.fetch_add(1, std::memory_order_relaxed);
         return (int) cudaGetLastError();
     }
+    const bool d32 = (sorted_blocks & YK_ORD_D32) != 0;
     sorted_blocks &= 3;
     bool typed_ok = sorted_blocks == 2 && (bt == YK_BT_I8 || bt == YK_BT_I16 || bt == YK_BT_I32 ||
                                            bt == YK_BT_I64 || bt == YK_BT_F32 || bt == YK_BT_F64 ||
@@ -2400,7 +2419,7 @@ extern "C" int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blo
     while (rshift < 31 && (1ull << rshift) < R)
         rshift++;
     if (typed_ok && !c.use64 && (1ull << rshift) == R &&
-        yk_owner_lane_launch(c, bt, rshift, s, ctas_per_sm)) {
+        yk_owner_lane_launch(c, bt, rshift, s, ctas_per_sm, d32)) {
         /* launched: power-of-two blocks, operator in the type's table */
     } else if (typed_ok) {
         uint64_t units = c.nbytes / (uint64_t) yk_bt_size(bt);

@@ -565,8 +565,11 @@ static int prepare_with(const yk_plan * p, char *typed, char *packed, yk_launch 
             uint64_t es = (uint64_t) yk_base_type_size(L->desc.leaf_type);
             uint64_t a = (uint64_t) (uintptr_t) (typed + L->desc.base) | (uint64_t) (uintptr_t) packed |
                 b0 | (uint64_t) ddo->elem_align;
-            if (es && (a % es) == 0 && (uint64_t) ddo->elem_align >= es)
+            if (es && (a % es) == 0 && (uint64_t) ddo->elem_align >= es) {
                 *sorted = 2;
+                if (ddo->disp32)
+                    *sorted |= YK_ORD_D32;
+            }
         }
         if (__atomic_load_n(&R.red_mode, __ATOMIC_RELAXED) > 0 && ddo->idx_blocks &&
             L->typed_op && L->desc.nlev == 1 && !L->use64 &&
