@@ -1248,9 +1248,9 @@ def main():
         lines = run_suite(args.steps)
         line["suite"] = lines
         line["suite_bit_exact"] = all(l["bit_exact"] for l in lines)
-    if not args.no_stream:
+    if rank == 0 and not args.no_stream:
         # the metric's second half: batched (persistent server) vs plain p50/p99 on the
-        # mixed request stream
+        # mixed request stream (rank 0 reports it; the other replicas have finished)
         r = run_stream(nreq=args.stream_requests, check=True)
         line["stream"] = {
             "workload": f"{r['requests']} pack/unpack requests, Poisson {r['rate_per_s']:.0f}/s, "
