@@ -683,6 +683,57 @@ yk_runs_pack_kernel(const __grid_constant__ yk_launch L, uint32_t R)
     }
 }
 
+/* The same pack with the packed side staged per warp: each lane still reads its run
+ * with 16-byte loads and puts its R bytes at lane * R in the warp's shared-memory tile;
+ * after __syncwarp the warp writes the tile's 32 * R packed bytes as 16-byte chunks at
+ * consecutive addresses.  The per-lane form writes R/4 pieces of 4 bytes at an R-byte
+ * stride, so each of its store instructions touches about R sectors for 128 bytes;
+ * here a store instruction fills whole sectors.  Only a warp, not the CTA, waits on the
+ * tile.  Needs the packed pointer on 16 bytes (checked by the launcher) and R a
+ * multiple of 4; a group of fewer than 32 elements writes its last bytes as 4-byte
+ * words. */
+template <int NV>
+__global__ void __launch_bounds__(YK_THREADS, 8)
+yk_runs_pack_warp_kernel(const __grid_constant__ yk_launch L, uint32_t R)
+{
+    __shared__ __align__(16) unsigned char stage[YK_THREADS / 32][32 * 48];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t E = L.desc.lv[0].stride;
+    const uint32_t nel = (uint32_t) (L.nbytes / R), e0 = (uint32_t) (L.p0 / R);
+    const char *tb = L.typed + L.desc.base;
+    const uint32_t nw4 = R / 4;      /* R <= 16 * NV */
+    unsigned char *st = stage[w];
+    const uint32_t gw = (blockIdx.x * YK_THREADS + threadIdx.x) >> 5;
+    const uint32_t nwarps = (gridDim.x * YK_THREADS) >> 5;
+    for (uint32_t i0 = gw * 32; i0 < nel; i0 += nwarps * 32) {
+        const uint32_t i = i0 + (uint32_t) lane;
+        const uint32_t n = min(32u, nel - i0);
+        if (i < nel) {
+            const char *src = tb + (int64_t) (e0 + i) * E;
+            union {
+                uint4 w[NV];
+                uint32_t u[4 * NV];
+            } v;
+#pragma unroll
+            for (int k = 0; k < NV; k++)
+                v.w[k] = yk_ldcg((const uint4 *) (src + 16 * k));
+            uint32_t *sw = (uint32_t *) (st + (uint32_t) lane * R);
+#pragma unroll
+            for (int j = 0; j < 4 * NV; j++)
+                if ((uint32_t) j < nw4)
+                    sw[j] = v.u[j];
+        }
+        __syncwarp();
+        char *dst = L.packed + (uint64_t) i0 * R;
+        const uint32_t nbytes = n * R, nch = nbytes / 16;
+        for (uint32_t c = (uint32_t) lane; c < nch; c += 32)
+            *(uint4 *) (dst + 16 * c) = *(const uint4 *) (st + 16 * c);
+        for (uint32_t q = nch * 16 + (uint32_t) lane * 4; q < nbytes; q += 128)
+            *(uint32_t *) (dst + q) = *(const uint32_t *) (st + q);
+        __syncwarp();
+    }
+}
+
 extern "C" int yk_cuda_launch_runs_pack(const yk_launch * l, uint32_t run, void *stream);
 
 template <typename IDX, int V, int DIR, int U>
@@ -2357,7 +2408,16 @@ extern "C" int yk_cuda_launch_runs_pack(const yk_launch * l, uint32_t run, void 
     const uint64_t nel = l->nbytes / run;
     const unsigned g = yk_grid(nel, YK_THREADS, 8);
     cudaStream_t s = (cudaStream_t) stream;
-    if (l->vec == 8)
+    static int warp_form = -1;
+    if (warp_form < 0) {
+        const char *e = getenv("YAKSA_GB300_RUNS_WARP");
+        warp_form = !(e && e[0] == '0');
+    }
+    if (warp_form && (uintptr_t) l->packed % 16 == 0 && run % 4 == 0 && run <= 32)
+        yk_runs_pack_warp_kernel<2><<<g, YK_THREADS, 0, s>>>(*l, run);
+    else if (warp_form && (uintptr_t) l->packed % 16 == 0 && run % 4 == 0 && run <= 48)
+        yk_runs_pack_warp_kernel<3><<<g, YK_THREADS, 0, s>>>(*l, run);
+    else if (l->vec == 8)
         yk_runs_pack_kernel<8><<<g, YK_THREADS, 0, s>>>(*l, run);
     else
         yk_runs_pack_kernel<4><<<g, YK_THREADS, 0, s>>>(*l, run);
