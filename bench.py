@@ -375,7 +375,7 @@ def suite_fill(np, rng, base, nbytes):
 # the DRAM bytes of a config's launch, and the full config's size over the captured case's
 SUITE_PROFILE = {("hindexed", "pack"): ("yk_hidx32_kernel_hindexed", "pack", 2),
                  ("hindexed", "unpack"): ("yk_hidx32_kernel_hindexed_unpack", "unpack", 2),
-                 ("struct", "pack"): ("yk_runs_pack_kernel_struct", "pack", 2),
+                 ("struct", "pack"): ("yk_runs_pack_warp_kernel_struct", "pack", 1),
                  ("struct", "unpack"): ("yk_regular_kernel_struct", "unpack", 2),
                  ("reduce_double", "unpack"): ("yk_owner_lane_kernel_reduce", "double_sum_full", 1),
                  ("reduce_c_complex", "unpack"): ("yk_owner_chunk_kernel_reduce_complex", "complex_prod", 1),
