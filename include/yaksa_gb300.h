@@ -70,8 +70,10 @@ int yaksa_gb300_graph_free(yaksa_gb300_graph_t graph);
  *           the GPU cannot address return YAKSA_ERR__NOT_SUPPORTED;
  *   test/wait: completion of a ticket (wait gives up with YAKSA_ERR__INTERNAL after
  *           20 s); progress: reclaims finished requests and keeps a kernel resident.
- * Resident CTAs that find no work for a few milliseconds leave; the next submit or
- * progress call relaunches them.  Requests in flight together must be independent. */
+ * Resident CTAs that find no work for 2 ms leave; the next submit or progress call
+ * relaunches them (about 30 us).  A device-wide synchronize (cudaDeviceSynchronize, or
+ * work on the legacy default stream) waits for resident CTAs, so it returns up to 2 ms
+ * after the server's last work.  Requests in flight together must be independent. */
 typedef struct yaksa_gb300_server_s *yaksa_gb300_server_t;
 int yaksa_gb300_server_create(uint32_t ring_requests, uint64_t budget_bytes,
                               yaksa_gb300_server_t * server);

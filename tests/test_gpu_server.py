@@ -130,6 +130,28 @@ def test_server_idle_exit_and_relaunch(cuda, prod, oracle):
     prod.type_free(t)
 
 
+def test_server_idle_exit_is_prompt(cuda, prod):
+    """A device-wide synchronize waits for resident CTAs, which leave after 2 ms without
+    work by the GPU's timer: it returns well before the old 4000-poll bound (about
+    50 ms at the measured 12.5 us per idle poll), every time."""
+    srv = yk.Server(prod)
+    t = prod.type_create_hvector(1 << 15, 4, 128, yk.TYPE_DOUBLE)    # 1 MiB packed
+    src = cuda.randn((1 << 15) * 16, dtype=cuda.float64, device="cuda")
+    out = cuda.zeros(1 << 17, dtype=cuda.float64, device="cuda")
+    cuda.cuda.synchronize()
+    waits = []
+    for rep in range(5):
+        tk = submit_all(srv, [yk.pack_op(src.data_ptr(), 1, t, 0, out.data_ptr(), 1 << 20)])[0]
+        srv.wait(tk)
+        t0 = time.perf_counter()
+        cuda.cuda.synchronize()
+        waits.append(time.perf_counter() - t0)
+    assert cuda.equal(out, src.view(-1, 16)[:, :4].reshape(-1))
+    assert max(waits) < 0.02, waits
+    srv.destroy()
+    prod.type_free(t)
+
+
 def test_server_admission_budget(cuda, prod, oracle):
     """A byte budget smaller than the queue refuses admission until requests finish."""
     srv = yk.Server(prod, ring_requests=8, budget_bytes=1 << 20)

@@ -171,8 +171,9 @@ typedef struct {
                                          * its record load to its last byte (GPU global
                                          * timer; the host zeroes it before publishing) */
     uint32_t qi, qr;            /* ring sizes */
-    uint32_t max_idle_spins;    /* bounded wait for new items */
-    uint32_t pad;
+    uint32_t max_idle_spins;    /* iteration bound on the wait for new items */
+    uint32_t idle_us;           /* a CTA that finds no item for this long leaves (GPU
+                                 * global timer); max_idle_spins bounds it regardless */
 } yk_server_args;
 
 int yk_cuda_server_launch(const yk_server_args * a, int ctas, void *stream);

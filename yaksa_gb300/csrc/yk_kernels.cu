@@ -1890,8 +1890,9 @@ __device__ __forceinline__ bool yk_item_ok(const yk_item & it, const yk_launch &
  * that never runs past the published count), stage the item's request record in shared
  * memory, process the item, and publish its completion.  A CTA tries its home lane
  * first, then the others in turn.  Every wait is bounded: a CTA that finds no new item
- * for max_idle_spins polls, or sees the stop flag, leaves; the host relaunches the
- * kernel when items are pending and no CTA is resident. */
+ * for idle_us microseconds of the GPU's global timer (or max_idle_spins polls), or sees
+ * the stop flag, leaves; the host relaunches the kernel when items are pending and no
+ * CTA is resident. */
 __global__ void __launch_bounds__(YK_THREADS, 6)
 yk_server_kernel(const __grid_constant__ yk_server_args A)
 {
@@ -1907,6 +1908,7 @@ yk_server_kernel(const __grid_constant__ yk_server_args A)
              * resident CTAs polling at full rate would load the C2C link the host's own
              * submissions cross */
             unsigned nap = 64;
+            const unsigned long long idle_t0 = yk_globaltimer();
             for (uint32_t spins = 0;; spins++) {
                 if (*A.stop) {
                     cmd = 2;
@@ -1941,7 +1943,8 @@ yk_server_kernel(const __grid_constant__ yk_server_args A)
                     }
                     continue;
                 }
-                if (spins >= A.max_idle_spins) {
+                if (spins >= A.max_idle_spins ||
+                    yk_globaltimer() - idle_t0 >= 1000ull * A.idle_us) {
                     cmd = 3;
                     break;
                 }

@@ -1639,7 +1639,13 @@ int yaksa_gb300_server_create(uint32_t ring_requests, uint64_t budget_bytes,
     S->args.req_busy = S->req_busy;
     S->args.qi = S->qi;
     S->args.qr = S->qr;
-    S->args.max_idle_spins = 4000;      /* ~8 ms without work at the 2 us poll interval */
+    /* Resident CTAs leave after 2 ms without work, by the GPU's global timer; a device-
+     * wide synchronize waits for them, so the window is kept short (a relaunch costs
+     * about 30 us).  The poll count bounds the wait as well: an idle poll measured
+     * about 12.5 us (the 2 us nap plus the C2C reads of the published count), so 4000
+     * polls are about 50 ms. */
+    S->args.idle_us = 2000;
+    S->args.max_idle_spins = 4000;
     *server = S;
     return YAKSA_SUCCESS;
 }
