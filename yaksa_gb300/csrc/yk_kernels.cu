@@ -1644,20 +1644,21 @@ __global__ void yk_ordered_warp_kernel(const __grid_constant__ yk_launch L)
 
 /* Each function processes the units [ub, ue) of one request with the CTA's threads. */
 template <int V, int DIR>
-__device__ __forceinline__ void yk_srv_regular(const yk_launch & L, uint64_t ub, uint64_t ue)
+__device__ __noinline__ void yk_srv_regular(const yk_launch & L, uint64_t ub, uint64_t ue)
 {
+    /* four units per thread, their loads issued together (the launch form's shape) */
     for (uint32_t t0 = (uint32_t) ub; t0 < (uint32_t) ue; t0 += YK_THREADS)
         yk_regular_dispatch<V, DIR, 1>(L, t0, (uint32_t) ue);
 }
 
 template <int V, int DIR>
-__device__ __forceinline__ void yk_srv_bytes(const yk_launch & L, uint64_t ub, uint64_t ue)
+__device__ __noinline__ void yk_srv_bytes(const yk_launch & L, uint64_t ub, uint64_t ue)
 {
     for (uint64_t t0 = ub; t0 < ue; t0 += YK_THREADS)
         yk_bytes_tile<uint64_t, V, DIR, 1>(L, t0, ue);
 }
 
-__device__ void yk_srv_typed(const yk_launch & L, uint64_t ub, uint64_t ue)
+__device__ __noinline__ void yk_srv_typed(const yk_launch & L, uint64_t ub, uint64_t ue)
 {
     const uint64_t g = (uint64_t) L.vec;
     const int op = (int) L.op;
@@ -1676,7 +1677,7 @@ __device__ void yk_srv_typed(const yk_launch & L, uint64_t ub, uint64_t ue)
     }
 }
 
-__device__ void yk_srv_owner(const yk_launch & L, uint64_t ub, uint64_t ue)
+__device__ __noinline__ void yk_srv_owner(const yk_launch & L, uint64_t ub, uint64_t ue)
 {
     const yk_level & lv = L.desc.lv[0];
     const int bt = L.desc.leaf_type;
@@ -1706,22 +1707,121 @@ __device__ void yk_srv_owner(const yk_launch & L, uint64_t ub, uint64_t ue)
     }
 }
 
+/* sorted blocks with both sides aligned to the element size (the launch form is
+ * yk_owner_lane_kernel): elements [ub, ue) of the request, two per thread, every load
+ * that does not depend on another issued first; the owner of a target element (its
+ * first in-range contributor) folds in the later blocks in block order. */
+template <int BT, int OP>
+__device__ __noinline__ void yk_srv_owner_t(const yk_launch & L, uint64_t ub, uint64_t ue)
+{
+    typedef typename yk_elem<BT>::T T;
+    constexpr uint64_t es = sizeof(T);
+    constexpr int U = 2;
+    constexpr int op = OP;
+    const yk_level & lv = L.desc.lv[0];
+    const uint64_t R = lv.cps, p0 = L.p0, p1 = L.p0 + L.nbytes, nblk = lv.count;
+    const T *packed = (const T *) L.packed;     /* element 0 is packed byte p0 */
+    char *typed = L.typed + L.desc.base;
+    for (uint64_t u0 = ub + threadIdx.x; u0 < ue; u0 += U * YK_THREADS) {
+        int64_t x[U], dn[U];
+        uint64_t b[U];
+        bool own[U], h1[U];
+        T in[U], out[U], in1[U];
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            const uint64_t u = u0 + (uint64_t) k * YK_THREADS;
+            own[k] = u < ue;
+            h1[k] = false;
+            if (!own[k])
+                continue;
+            const uint64_t p = p0 + u * es;
+            b[k] = yk_div(p, lv);
+            const int64_t d = __ldg(lv.disp + b[k]);
+            const int64_t dp = b[k] > 0 ? __ldg(lv.disp + b[k] - 1) : 0;
+            dn[k] = b[k] + 1 < nblk ? __ldg(lv.disp + b[k] + 1) : INT64_MAX;
+            in[k] = __ldg(packed + u);
+            x[k] = d + (int64_t) (p - b[k] * R);
+            /* an earlier in-range block owns this element */
+            if (b[k] > 0 && x[k] < dp + (int64_t) R && (b[k] - 1) * R + (uint64_t) (x[k] - dp) >= p0)
+                own[k] = false;
+        }
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            if (!own[k])
+                continue;
+            out[k] = *(const T *) (typed + x[k]);
+            if (dn[k] <= x[k]) {
+                const uint64_t pp = (b[k] + 1) * R + (uint64_t) (x[k] - dn[k]);
+                if (pp < p1) {
+                    h1[k] = true;
+                    in1[k] = __ldg(packed + (pp - p0) / es);
+                }
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            if (!own[k])
+                continue;
+            yk_elem<BT>::op(op, in[k], out[k]);
+            if (h1[k]) {
+                yk_elem<BT>::op(op, in1[k], out[k]);
+                /* rarer: the blocks after that, in block order */
+                for (uint64_t bb = b[k] + 2; bb < nblk; bb++) {
+                    const int64_t d2 = __ldg(lv.disp + bb);
+                    if (d2 > x[k])
+                        break;
+                    const uint64_t pp = bb * R + (uint64_t) (x[k] - d2);
+                    if (pp >= p1)
+                        break;  /* later blocks place x later still */
+                    yk_elem<BT>::op(op, __ldg(packed + (pp - p0) / es), out[k]);
+                }
+            }
+            *(T *) (typed + x[k]) = out[k];
+        }
+    }
+}
+
+/* a compile-time instance for complex-float PROD (600 against 510 GB/s on bursts of
+ * 16 MiB requests); every other aligned sorted-block request takes the generic item,
+ * double SUM included (its instance measured 579 against 624 GB/s at this kernel's
+ * register bound) */
+__device__ __noinline__ void yk_srv_owner_typed(const yk_launch & L, uint64_t ub, uint64_t ue)
+{
+    if (L.desc.leaf_type == YK_BT_C32 && (int) L.op == OP_PROD)
+        yk_srv_owner_t<YK_BT_C32, OP_PROD>(L, ub, ue);
+    else
+        yk_srv_owner(L, ub, ue);
+}
+
 /* overlapping equal blocks under an order-independent integer operator (the launch
  * form is yk_red_kernel): elements [ub, ue) of the request, each folded into its target
  * by one L2 reduction */
 template <int BT, int OP>
-__device__ __forceinline__ void yk_srv_red_t(const yk_launch & L, uint64_t ub, uint64_t ue)
+__device__ __noinline__ void yk_srv_red_t(const yk_launch & L, uint64_t ub, uint64_t ue)
 {
     typedef typename yk_elem<BT>::T T;
     const yk_level & lv = L.desc.lv[0];
     const uint64_t es = sizeof(T), p0 = L.p0;
     char *typed = L.typed + L.desc.base;
-    for (uint64_t u = ub + threadIdx.x; u < ue; u += YK_THREADS) {
-        const uint64_t p = p0 + u * es;
-        const uint64_t b = yk_div(p, lv);
-        const int64_t at = lv.kind == YK_LV_IDX ? __ldg(lv.disp + b) : (int64_t) b * lv.stride;
-        const T v = *(const T *) (L.packed + (p - p0));
-        yk_red<OP>((T *) (typed + at + (int64_t) (p - b * lv.cps)), v);
+    constexpr int U = 4;        /* elements per thread, their loads issued together */
+    for (uint64_t u0 = ub + threadIdx.x; u0 < ue; u0 += U * YK_THREADS) {
+        int64_t x[U];
+        T v[U];
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            const uint64_t u = u0 + (uint64_t) k * YK_THREADS;
+            if (u < ue) {
+                const uint64_t p = p0 + u * es;
+                const uint64_t b = yk_div(p, lv);
+                const int64_t at = lv.kind == YK_LV_IDX ? __ldg(lv.disp + b) : (int64_t) b * lv.stride;
+                x[k] = at + (int64_t) (p - b * lv.cps);
+                v[k] = *(const T *) (L.packed + (p - p0));
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < U; k++)
+            if (u0 + (uint64_t) k * YK_THREADS < ue)
+                yk_red<OP>((T *) (typed + x[k]), v[k]);
     }
 }
 
@@ -1738,7 +1838,7 @@ __device__ __forceinline__ void yk_srv_red_bt(const yk_launch & L, uint64_t ub, 
     }
 }
 
-__device__ void yk_srv_red(const yk_launch & L, uint64_t ub, uint64_t ue)
+__device__ __noinline__ void yk_srv_red(const yk_launch & L, uint64_t ub, uint64_t ue)
 {
     if (L.desc.leaf_type == YK_BT_I32)
         yk_srv_red_bt<YK_BT_I32>(L, ub, ue);
@@ -1747,7 +1847,7 @@ __device__ void yk_srv_red(const yk_launch & L, uint64_t ub, uint64_t ue)
 }
 
 /* the whole request, in order, by warp 0 (targets that overlap arbitrarily) */
-__device__ void yk_srv_ordered(const yk_launch & L, uint64_t ub, uint64_t ue)
+__device__ __noinline__ void yk_srv_ordered(const yk_launch & L, uint64_t ub, uint64_t ue)
 {
     if (threadIdx.x >= 32)
         return;
@@ -1800,7 +1900,7 @@ __device__ void yk_srv_ordered(const yk_launch & L, uint64_t ub, uint64_t ue)
 /* contiguous-block hindexed over the packed range [pb, pe): the CTA's warps split the
  * overlapping block groups (see yk_hidx_kernel) */
 template <int V, int DIR>
-__device__ void yk_srv_hidx(const yk_launch & L, uint64_t pb, uint64_t pe)
+__device__ __noinline__ void yk_srv_hidx(const yk_launch & L, uint64_t pb, uint64_t pe)
 {
     typedef typename yk_vec<V>::T VT;
     const yk_level *lv = &L.desc.lv[0];
@@ -1893,6 +1993,9 @@ __device__ __forceinline__ bool yk_item_ok(const yk_item & it, const yk_launch &
  * for idle_us microseconds of the GPU's global timer (or max_idle_spins polls), or sees
  * the stop flag, leaves; the host relaunches the kernel when items are pending and no
  * CTA is resident. */
+/* The item functions above are out of line (__noinline__): each gets the kernel's
+ * register budget to itself, so the loops of one item kind do not spill for the
+ * registers another kind needs (inlined, the kernel spilled up to 3 KB). */
 __global__ void __launch_bounds__(YK_THREADS, 6)
 yk_server_kernel(const __grid_constant__ yk_server_args A)
 {
@@ -2044,6 +2147,10 @@ yk_server_kernel(const __grid_constant__ yk_server_args A)
             case YK_SRV_RED:
                 yk_srv_red(sL, (it.pb - sL.p0) / (uint64_t) yk_bt_size(sL.desc.leaf_type),
                            (it.pe - sL.p0) / (uint64_t) yk_bt_size(sL.desc.leaf_type));
+                break;
+            case YK_SRV_OWNER_T:
+                yk_srv_owner_typed(sL, (it.pb - sL.p0) / (uint64_t) yk_bt_size(sL.desc.leaf_type),
+                                   (it.pe - sL.p0) / (uint64_t) yk_bt_size(sL.desc.leaf_type));
                 break;
             default:
 #define YK_SH(V) do { if (sL.dir == 0) yk_srv_hidx<V, 0>(sL, it.pb, it.pe); \

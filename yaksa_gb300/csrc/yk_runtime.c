@@ -1767,7 +1767,8 @@ static int server_plan(yaksa_gb300_pup_t * o, yaksa_info_t info, yk_srv_req * q)
     } else {
         /* L2 reductions where they apply; the owner items need sorted blocks */
         const int red = (sorted & YK_ORD_RED) != 0, owner = (sorted & 3) != 0;
-        skind = red ? YK_SRV_RED : owner ? YK_SRV_OWNER : YK_SRV_ORDERED;
+        skind = red ? YK_SRV_RED : (sorted & 3) == 2 ? YK_SRV_OWNER_T : owner ? YK_SRV_OWNER :
+            YK_SRV_ORDERED;
         gran = red || owner ? (uint64_t) yk_base_type_size(L.desc.leaf_type) : (uint64_t) L.vec;
     }
     q->L = L;
