@@ -557,6 +557,17 @@ static int hidx_has_table(const hlev * h)
     return h->kind == YK_LV_HIDX && h->count > 1 && h->count < 0xffffffffull;
 }
 
+/* an IDX level whose displacements all fit in 32 bits (it gets an int32 copy) */
+static int idx_fits32(const hlev * h)
+{
+    if (h->kind != YK_LV_IDX || !h->disp || !h->count)
+        return 0;
+    for (uint64_t j = 0; j < h->count; j++)
+        if (h->disp[j] < INT32_MIN || h->disp[j] > INT32_MAX)
+            return 0;
+    return 1;
+}
+
 static int upload(hbuild * b, yk_devdesc * dd, int to_device)
 {
     /* table sizes */
@@ -564,6 +575,8 @@ static int upload(hbuild * b, yk_devdesc * dd, int to_device)
     for (int i = 0; i < b->nlev; i++) {
         if (b->lv[i].disp)
             bytes += b->lv[i].count * sizeof(int64_t);
+        if (idx_fits32(&b->lv[i]))
+            bytes += (b->lv[i].count * sizeof(int32_t) + 7) & ~(size_t) 7;
         if (b->lv[i].pfx)
             bytes += (b->lv[i].count + 1) * sizeof(uint64_t);
         if (hidx_has_table(&b->lv[i]))
@@ -599,6 +612,15 @@ static int upload(hbuild * b, yk_devdesc * dd, int to_device)
             memcpy(host + pos, h->disp, h->count * sizeof(int64_t));
             l->disp = (const int64_t *) (dev + pos);
             pos += h->count * sizeof(int64_t);
+        }
+        if (idx_fits32(h)) {
+            /* the 32-bit copy right after the table: kernels that read one displacement
+             * per element move half the table bytes */
+            int32_t *d32 = (int32_t *) (host + pos);
+            for (uint64_t j = 0; j < h->count; j++)
+                d32[j] = (int32_t) h->disp[j];
+            l->has_d32 = 1;
+            pos += (h->count * sizeof(int32_t) + 7) & ~(size_t) 7;
         }
         if (h->pfx) {
             memcpy(host + pos, h->pfx, (h->count + 1) * sizeof(uint64_t));

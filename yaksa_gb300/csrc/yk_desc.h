@@ -59,7 +59,9 @@ enum {
 
 typedef struct {
     int32_t kind;
-    int32_t pad0;
+    int32_t has_d32;            /* IDX: an int32_t copy of disp[] follows it, at
+                                 * (const int32_t *) (disp + count) (every displacement
+                                 * fits in 32 bits) */
     uint64_t count;
     int64_t stride;             /* VEC: byte stride; HIDX: child extent */
     uint64_t cps;               /* packed bytes per digit (child packed size) */

@@ -1351,8 +1351,8 @@ yk_owner_chunk_kernel(const __grid_constant__ yk_launch L, int rshift)
 {
     typedef typename yk_elem<BT>::T T;
     typedef typename yk_vec<CW>::T CT;
-    /* target offsets in 32 bits when the host found that every one fits (the
-     * displacements' low words are loaded), else in 64 bits */
+    /* target offsets in 32 bits when the host found that every one fits (the level's
+     * 32-bit copy of the displacements is read), else in 64 bits */
     typedef typename std::conditional<D32, int32_t, int64_t>::type OFF;
     constexpr OFF OFF_MAX = D32 ? (OFF) INT32_MAX : (OFF) INT64_MAX;
     constexpr uint32_t es = (uint32_t) sizeof(T);
@@ -1367,7 +1367,7 @@ yk_owner_chunk_kernel(const __grid_constant__ yk_launch L, int rshift)
     char *typed = L.typed + L.desc.base;
     auto disp = [&](uint32_t i) -> OFF {
         if constexpr (D32)
-            return __ldg((const int32_t *) lv.disp + 2 * (size_t) i);   /* low word */
+            return __ldg((const int32_t *) (lv.disp + lv.count) + i);   /* the 32-bit copy */
         else
             return __ldg(lv.disp + i);
     };
@@ -1511,7 +1511,7 @@ template <int OP> __device__ __forceinline__ void yk_red(int64_t *p, int64_t v)
  * Lane k of a warp takes packed element u0 + k, so the lanes of one block reduce into
  * consecutive target elements (one L2 sector request per 32 bytes).  Both sides are
  * aligned to the element size (checked on the host). */
-template <int BT, int OP, int K>
+template <int BT, int OP, int K, bool D32>
 __global__ void __launch_bounds__(YK_THREADS)
 yk_red_kernel(const __grid_constant__ yk_launch L)
 {
@@ -1533,7 +1533,13 @@ yk_red_kernel(const __grid_constant__ yk_launch L)
             if (u < nunits) {
                 const uint32_t p = p0 + u * es;
                 const uint32_t b = yk_div(p, lv);
-                const int64_t at = K == YK_LV_IDX ? __ldg(lv.disp + b) : (int64_t) b * lv.stride;
+                int64_t at;
+                if constexpr (K != YK_LV_IDX)
+                    at = (int64_t) b * lv.stride;
+                else if constexpr (D32)
+                    at = __ldg((const int32_t *) (lv.disp + lv.count) + b);
+                else
+                    at = __ldg(lv.disp + b);
                 x[k] = at + (int64_t) (p - b * (uint32_t) lv.cps);
                 in[k] = __ldg(packed + u);
             }
@@ -2536,11 +2542,11 @@ extern "C" int yk_cuda_launch_runs_pack(const yk_launch * l, uint32_t run, void 
 
 /* yk_red_kernel for a 4- or 8-byte integer type and an operator that yk_red_applies()
  * accepts; false when the launch does not fit it */
-template <int BT, int K>
+template <int BT, int K, bool D32>
 static bool yk_red_launch_bt(const yk_launch & c, cudaStream_t s, unsigned g)
 {
     switch ((int) c.op) {
-#define YK_RD(O) case O: yk_red_kernel<BT, O, K><<<g, YK_THREADS, 0, s>>>(c); return true
+#define YK_RD(O) case O: yk_red_kernel<BT, O, K, D32><<<g, YK_THREADS, 0, s>>>(c); return true
         YK_RD(OP_MAX); YK_RD(OP_MIN); YK_RD(OP_SUM); YK_RD(OP_BAND); YK_RD(OP_BOR); YK_RD(OP_BXOR);
 #undef YK_RD
     }
@@ -2562,11 +2568,15 @@ static bool yk_red_launch(const yk_launch & c, int bt, cudaStream_t s, int cap)
         return false;
     const uint64_t units = c.nbytes / (uint64_t) yk_bt_size(bt);
     const unsigned g = yk_grid(units, (uint64_t) YK_THREADS * 4, cap > 0 ? cap : 8);
+    /* IDX: the 32-bit copy of the displacements when the level has one */
+    const bool d32 = k == YK_LV_IDX && c.desc.lv[0].has_d32;
     if (bt == YK_BT_I32)
-        return k == YK_LV_IDX ? yk_red_launch_bt<YK_BT_I32, YK_LV_IDX>(c, s, g) :
-            yk_red_launch_bt<YK_BT_I32, YK_LV_VEC>(c, s, g);
-    return k == YK_LV_IDX ? yk_red_launch_bt<YK_BT_I64, YK_LV_IDX>(c, s, g) :
-        yk_red_launch_bt<YK_BT_I64, YK_LV_VEC>(c, s, g);
+        return k != YK_LV_IDX ? yk_red_launch_bt<YK_BT_I32, YK_LV_VEC, false>(c, s, g) :
+            d32 ? yk_red_launch_bt<YK_BT_I32, YK_LV_IDX, true>(c, s, g) :
+            yk_red_launch_bt<YK_BT_I32, YK_LV_IDX, false>(c, s, g);
+    return k != YK_LV_IDX ? yk_red_launch_bt<YK_BT_I64, YK_LV_VEC, false>(c, s, g) :
+        d32 ? yk_red_launch_bt<YK_BT_I64, YK_LV_IDX, true>(c, s, g) :
+        yk_red_launch_bt<YK_BT_I64, YK_LV_IDX, false>(c, s, g);
 }
 
 extern "C" int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blocks, void *stream,
@@ -2582,7 +2592,7 @@ extern "C" int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blo
         yk_red_count.fetch_add(1, std::memory_order_relaxed);
         return (int) cudaGetLastError();
     }
-    const bool d32 = (sorted_blocks & YK_ORD_D32) != 0;
+    const bool d32 = (sorted_blocks & YK_ORD_D32) != 0 && l->desc.lv[0].has_d32;
     sorted_blocks &= 3;
     bool typed_ok = sorted_blocks == 2 && (bt == YK_BT_I8 || bt == YK_BT_I16 || bt == YK_BT_I32 ||
                                            bt == YK_BT_I64 || bt == YK_BT_F32 || bt == YK_BT_F64 ||
