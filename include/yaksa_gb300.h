@@ -58,7 +58,7 @@ int yaksa_gb300_graph_free(yaksa_gb300_graph_t graph);
 
 /* Request server (no counterpart in the reference, whose progress engine launches
  * one kernel per request chunk, src/backend/src/yaksuri_progress.c:2862-3088).  A
- * persistent kernel keeps six CTAs resident per SM and drains a work queue in
+ * persistent kernel keeps eight CTAs resident per SM and drains a work queue in
  * pinned, device-mapped host memory; requests are split into work items of up to
  * 256 KiB of packed bytes (YAKSA_GB300_SERVER_ITEM_KIB overrides it), and into at least
  * 128 items down to 32 KiB each (YAKSA_GB300_SERVER_MIN_ITEMS), so requests of any size
