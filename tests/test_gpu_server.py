@@ -310,3 +310,37 @@ def test_server_tune_decides_item_cuts_and_stays_exact(cuda, prod, oracle):
     for r in reqs:
         prod.type_free(r["tp"])
         oracle.type_free(r["to"])
+
+
+@pytest.mark.parametrize("fields,count", [
+    (([1, 3], [0, 8], ["TYPE_INT64_T", "TYPE_FLOAT"], 32), 300_001),    # 20-byte runs
+    (([3, 3], [0, 12], ["TYPE_INT32_T", "TYPE_FLOAT"], 32), 70_013),     # 24-byte runs
+    (([1, 7], [0, 8], ["TYPE_INT64_T", "TYPE_FLOAT"], 48), 50_021),      # 36-byte runs
+])
+def test_server_struct_like_packs(cuda, prod, oracle, fields, count):
+    """Packs of struct-like runs (17-47 bytes on 16-byte element starts) through the
+    server's warp-staged item: items of whole 32-element groups, a last group of fewer
+    than 32 elements, the packed bytes against the oracle."""
+    blens, displs, names, extent = fields
+    ts = [getattr(yk, n) for n in names]
+    sp = prod.type_create_struct(blens, displs, ts)
+    so = oracle.type_create_struct(blens, displs, ts)
+    tp, to = prod.type_create_resized(sp, 0, extent), oracle.type_create_resized(so, 0, extent)
+    rng = np.random.default_rng(count)
+    typed = rng.integers(0, 256, count * extent, dtype=np.uint8)
+    n = prod.size(tp) * count
+    exp = np.zeros(n, dtype=np.uint8)
+    oracle.pack(typed.ctypes.data, count, to, 0, exp.ctypes.data, n)
+    td = cuda.from_numpy(typed).cuda()
+    out = cuda.zeros(n, dtype=cuda.uint8, device="cuda")
+    cuda.cuda.synchronize()
+    srv = yk.Server(prod)
+    try:
+        tk = submit_all(srv, [yk.pack_op(td.data_ptr(), count, tp, 0, out.data_ptr(), n)])[0]
+        srv.wait(tk)
+        assert srv.stats()["items"] >= 2
+        assert np.array_equal(out.cpu().numpy(), exp)
+    finally:
+        srv.destroy()
+    for y, t in ((prod, tp), (prod, sp), (oracle, to), (oracle, so)):
+        y.type_free(t)

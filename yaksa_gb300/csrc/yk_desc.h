@@ -135,7 +135,7 @@ int yk_cuda_launch_batch(const yk_batch * b, int units_per_thread, int regular, 
  * Persistent request server: a device-visible work queue drained by resident CTAs.
  * ------------------------------------------------------------------------- */
 enum { YK_SRV_REGULAR = 0, YK_SRV_BYTES, YK_SRV_TYPED, YK_SRV_OWNER, YK_SRV_ORDERED, YK_SRV_HIDX,
-    YK_SRV_RED, YK_SRV_OWNER_T, YK_SRV_LAST = YK_SRV_OWNER_T };
+    YK_SRV_RED, YK_SRV_OWNER_T, YK_SRV_RUNS, YK_SRV_LAST = YK_SRV_RUNS };
 /* flag in yk_item.kind: the item's busy time is added to its request's req_busy */
 #define YK_SRV_TIMED 0x100u
 

@@ -1799,6 +1799,50 @@ __device__ __noinline__ void yk_srv_owner_typed(const yk_launch & L, uint64_t ub
         yk_srv_owner(L, ub, ue);
 }
 
+/* struct-like packs (the launch form is yk_runs_pack_warp_kernel): elements [ib, ie) of
+ * the request, ib a multiple of 32 (the host cuts these items in whole 32-element
+ * groups), each warp staging a group's runs in shared memory and writing its packed
+ * bytes as 16-byte chunks */
+static __shared__ __align__(16) unsigned char yk_srv_stage[YK_THREADS / 32][32 * 48];
+
+template <int NV>
+__device__ __noinline__ void yk_srv_runs(const yk_launch & L, uint64_t ib, uint64_t ie)
+{
+    const uint32_t R = (uint32_t) L.desc.run;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int64_t E = L.desc.lv[0].stride;
+    const uint32_t e0 = (uint32_t) (L.p0 / R), nw4 = R / 4;
+    const char *tb = L.typed + L.desc.base;
+    unsigned char *st = yk_srv_stage[w];
+    for (uint64_t i0 = ib + (uint64_t) w * 32; i0 < ie; i0 += (YK_THREADS / 32) * 32) {
+        const uint64_t i = i0 + (uint64_t) lane;
+        const uint32_t n = (uint32_t) min((uint64_t) 32, ie - i0);
+        if (i < ie) {
+            const char *src = tb + (int64_t) (e0 + i) * E;
+            union {
+                uint4 w[NV];
+                uint32_t u[4 * NV];
+            } v;
+#pragma unroll
+            for (int k = 0; k < NV; k++)
+                v.w[k] = yk_ldcg((const uint4 *) (src + 16 * k));
+            uint32_t *sw = (uint32_t *) (st + (uint32_t) lane * R);
+#pragma unroll
+            for (int j = 0; j < 4 * NV; j++)
+                if ((uint32_t) j < nw4)
+                    sw[j] = v.u[j];
+        }
+        __syncwarp();
+        char *dst = L.packed + i0 * R;
+        const uint32_t nbytes = n * R, nch = nbytes / 16;
+        for (uint32_t c = (uint32_t) lane; c < nch; c += 32)
+            *(uint4 *) (dst + 16 * c) = *(const uint4 *) (st + 16 * c);
+        for (uint32_t q = nch * 16 + (uint32_t) lane * 4; q < nbytes; q += 128)
+            *(uint32_t *) (dst + q) = *(const uint32_t *) (st + q);
+        __syncwarp();
+    }
+}
+
 /* overlapping equal blocks under an order-independent integer operator (the launch
  * form is yk_red_kernel): elements [ub, ue) of the request, each folded into its target
  * by one L2 reduction */
@@ -2155,6 +2199,12 @@ yk_server_kernel(const __grid_constant__ yk_server_args A)
             case YK_SRV_RED:
                 yk_srv_red(sL, (it.pb - sL.p0) / (uint64_t) yk_bt_size(sL.desc.leaf_type),
                            (it.pe - sL.p0) / (uint64_t) yk_bt_size(sL.desc.leaf_type));
+                break;
+            case YK_SRV_RUNS:
+                if (sL.desc.run <= 32)
+                    yk_srv_runs<2>(sL, (it.pb - sL.p0) / sL.desc.run, (it.pe - sL.p0) / sL.desc.run);
+                else
+                    yk_srv_runs<3>(sL, (it.pb - sL.p0) / sL.desc.run, (it.pe - sL.p0) / sL.desc.run);
                 break;
             case YK_SRV_OWNER_T:
                 yk_srv_owner_typed(sL, (it.pb - sL.p0) / (uint64_t) yk_bt_size(sL.desc.leaf_type),

@@ -1758,6 +1758,12 @@ static int server_plan(yaksa_gb300_pup_t * o, yaksa_info_t info, yk_srv_req * q)
         L.use64 = p.b1 > 0xffffffffull;
         skind = L.use64 ? YK_SRV_BYTES : YK_SRV_REGULAR;
         gran = (uint64_t) v;
+    } else if (kind == YK_X_BYTES && runs_pack_ok(&L) && (uintptr_t) L.packed % 16 == 0 &&
+               L.desc.run % 4 == 0 && L.desc.run <= 48) {
+        /* struct-like packs: the warp-staged form, items of whole 32-element groups so that
+         * each group's packed bytes start on 16 bytes */
+        skind = YK_SRV_RUNS;
+        gran = 32 * (uint64_t) L.desc.run;
     } else if (kind == YK_X_BYTES) {
         skind = L.hidx ? YK_SRV_HIDX : L.regular >= 0 ? YK_SRV_REGULAR : YK_SRV_BYTES;
         gran = (uint64_t) L.vec;
