@@ -112,6 +112,16 @@ def main():
     ip, io = prod.type_create_resized(cp, 0, 32), orc.type_create_resized(co, 0, 32)
     case("overlap_sum_typed_host", ip, io, 20000, "unpack", "host", "dev", op=yk.OP_SUM, kind=np.float64)
     case("overlap_replace_both_host", ip, io, 20000, "unpack", "host", "host")
+    # overlapping blocks of one indexed_block level under int64 SUM: the typed span is
+    # staged into device memory, where the L2-reduction form folds the blocks in
+    qoffs = sorted(rng.integers(0, 3000, 4000).tolist())
+    iq, iqo = both("type_create_indexed_block", 8, qoffs, yk.TYPE_INT64_T)
+    red0 = ctypes.c_ulonglong(0)
+    prod.lib.yaksa_gb300_debug_l2_reduce(-1, ctypes.byref(red0))
+    case("overlap_int_sum_typed_host", iq, iqo, 1, "unpack", "host", "dev", op=yk.OP_SUM)
+    red1 = ctypes.c_ulonglong(0)
+    prod.lib.yaksa_gb300_debug_l2_reduce(-1, ctypes.byref(red1))
+    out["l2_reduce_on_staged_span"] = red1.value > red0.value
     # hindexed in shuffled order with gaps
     nb = 40000
     blens = rng.integers(1, 40, nb)
@@ -142,7 +152,8 @@ def main():
     out["staged_calls"] = s1["staged_calls"] - s0["staged_calls"]
     out["direct_calls"] = s1["direct_calls"] - s0["direct_calls"]
     for y in (prod, orc):
-        for t in ((vp, wp, sp, rp, cp, ip, hp, bp) if y is prod else (vo, wo, so, ro, co, io, ho, bo)):
+        for t in ((vp, wp, sp, rp, cp, ip, iq, hp, bp) if y is prod else
+                  (vo, wo, so, ro, co, io, iqo, ho, bo)):
             y.type_free(t)
     print(json.dumps(out))
 

@@ -6,7 +6,10 @@ library first brings the GPU up, so the cases run in a child process
 (tests/staging_child.py) with a ring of 4 slabs of 64 KiB: 5 MiB requests take 80 chunks
 and wrap the ring, 40 nonblocking requests are in flight at once (more than the ring
 holds), the packed side, the typed side or both live in pageable or pinned host memory,
-one case unpacks with SUM through overlapping blocks into a staged typed buffer, and two
+two cases unpack with SUM through overlaps into a staged typed buffer (double over
+overlapping elements on the ordered kernel; int64 over overlapping indexed_block blocks,
+folded in by L2 reductions on the staged device copy, checked by the library's launch
+counter), and two
 cases have an element larger than a slab.  Every result is compared byte for byte with
 the oracle.
 """
@@ -31,8 +34,8 @@ def test_staging_ring(cuda):
     res = json.loads(r.stdout.strip().splitlines()[-1])
     bad = [k for k, v in res.items() if v is False]
     assert not bad, res
-    # 17 single requests and 40 in flight, every one staged; none addressed in place
-    assert res["staged_calls"] == 57 and res["direct_calls"] == 0, res
+    # 18 single requests and 40 in flight, every one staged; none addressed in place
+    assert res["staged_calls"] == 58 and res["direct_calls"] == 0, res
 
 
 def test_wait_kernel_hint(cuda):
