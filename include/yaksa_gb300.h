@@ -200,7 +200,8 @@ int yaksa_gb300_debug_bulk_failures(unsigned int *n);
 /* Test hook (no counterpart in the reference): the L2-reduction form of unpacks whose
  * targets overlap.  When the type is one level of equal blocks (indexed_block,
  * hindexed_block, or indexed/hindexed with equal lengths) in any order, or a vector
- * whose stride is under its block length, the operator
+ * whose stride is under its block length, or count > 1 elements of one contiguous run
+ * whose extent is shorter than the run, the operator
  * is SUM, MAX, MIN, BAND, BOR or BXOR on a 4- or 8-byte integer type, and both buffers
  * sit on the element size, each packed element is folded into its target by one
  * reduction at L2 (red.global) instead of an ordered read-combine-write.  These

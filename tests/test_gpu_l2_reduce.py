@@ -237,3 +237,26 @@ def test_red_not_sent_to_host_memory(cuda, prod, oracle, op):
     assert_same_bytes(t_h.numpy(), t_o, f"host target op {op}")
     prod.type_free(tp)
     oracle.type_free(to)
+
+
+@pytest.mark.parametrize("op", [yk.OP_SUM, yk.OP_MAX, yk.OP_BXOR])
+def test_red_overlapping_elements(cuda, prod, oracle, op):
+    """count > 1 elements whose extent is shorter than their span (8 int64 each, extent
+    32 bytes): the overlap comes from the element level of the launch, which the
+    reduction form takes as one VEC level over a run."""
+    cp, co = prod.type_create_contig(8, yk.TYPE_INT64_T), oracle.type_create_contig(8, yk.TYPE_INT64_T)
+    tp, to = prod.type_create_resized(cp, 0, 32), oracle.type_create_resized(co, 0, 32)
+    count = 5000
+    rng = np.random.default_rng(op + 11)
+    typed0 = fill(rng, 32 * (count - 1) + 64, "int64")
+    packed0 = fill(rng, 64 * count, "int64")
+    t_o = typed0.copy()
+    oracle.unpack(packed0.ctypes.data, packed0.nbytes, t_o.ctypes.data, count, to, 0, op=op)
+    t_p, p_p = dev_copy(cuda, typed0), dev_copy(cuda, packed0)
+    before = red_launches(prod)
+    prod.unpack(p_p.data_ptr(), packed0.nbytes, t_p.data_ptr(), count, tp, 0, op=op)
+    cuda.cuda.synchronize()
+    assert red_launches(prod) - before == 1
+    assert_same_bytes(host_of(cuda, t_p), t_o, f"overlapping elements op {op}")
+    for y, t in ((prod, tp), (prod, cp), (oracle, to), (oracle, co)):
+        y.type_free(t)

@@ -754,14 +754,9 @@ static int build(yk_type * t, int typed, yk_devdesc * dd, int to_device)
     int64_t span = 0;
     dd->may_overlap = check_overlap(&b, &span);
     dd->sorted_blocks = 0;
-    dd->idx_blocks = 0;
     dd->disp32 = 0;
     if (dd->may_overlap && typed && b.leaf == YK_LEAF_RUN && b.nlev == 1 &&
-        b.lv[0].kind == YK_LV_VEC && b.lv[0].cps == b.run)
-        dd->idx_blocks = 1;
-    if (dd->may_overlap && typed && b.leaf == YK_LEAF_RUN && b.nlev == 1 &&
         b.lv[0].kind == YK_LV_IDX && b.lv[0].cps == b.run) {
-        dd->idx_blocks = 1;
         int sorted = 1;
         for (uint64_t j = 1; j < b.lv[0].count && sorted; j++)
             sorted = b.lv[0].disp[j] >= b.lv[0].disp[j - 1];

@@ -32,8 +32,6 @@ typedef struct {
     int unit;                   /* typed: gcd of element sizes (work-unit granule) */
     int may_overlap;            /* some typed-side bytes are reached twice */
     int sorted_blocks;          /* owner-computes ordered unpack applies */
-    int idx_blocks;             /* one IDX level of equal blocks over a run in any order,
-                                 * or one VEC level over its run */
     int disp32;                 /* sorted blocks: every target offset fits in 32 bits */
     int64_t elem_span;          /* bytes one element touches (element-level overlap test) */
     uint64_t table_bytes;

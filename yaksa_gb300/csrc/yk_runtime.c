@@ -571,8 +571,11 @@ static int prepare_with(const yk_plan * p, char *typed, char *packed, yk_launch 
                     *sorted |= YK_ORD_D32;
             }
         }
-        if (__atomic_load_n(&R.red_mode, __ATOMIC_RELAXED) > 0 && ddo->idx_blocks &&
-            L->typed_op && L->desc.nlev == 1 && !L->use64 &&
+        /* one level whose every step is one run of the base type: the type's own IDX or
+         * VEC level, or (count > 1) the element level over a type that is one run */
+        if (__atomic_load_n(&R.red_mode, __ATOMIC_RELAXED) > 0 &&
+            L->typed_op && L->desc.nlev == 1 && !L->use64 && L->desc.leaf == YK_LEAF_RUN &&
+            L->desc.lv[0].cps == L->desc.run &&
             (L->desc.lv[0].kind == YK_LV_IDX || L->desc.lv[0].kind == YK_LV_VEC) &&
             L->desc.lv[0].cps < (1ull << 32) && yk_red_applies(L->desc.leaf_type, L->op)) {
             /* equal blocks, in any order or at a stride under their length, under an
