@@ -1341,10 +1341,13 @@ yk_owner_lane_kernel(const __grid_constant__ yk_launch L, int rshift)
  * per owner and a loop of dependent loads run by a few lanes (which left 12.8 of 32
  * lanes active per instruction).  Only a third later block, rare at these shapes,
  * takes the loop.  double keeps yk_owner_lane_kernel: there every fold is a DADD on
- * GB300's narrow FP64 pipe, which the selects would spend on every lane. */
-/* complex float: bounded to the 32 registers of full occupancy, with a 32-byte spill in
- * the 32-bit-offset form; at 40 registers (6 CTAs per SM) the complex PROD config took
- * 180.2 us, at 32 (8 per SM) 170.0 us */
+ * GB300's narrow FP64 pipe, which the selects would spend on every lane.
+ *
+ * D32: offsets and ownership tests in 32 bits on the level's 32-bit copy of the
+ * displacements, where the host found that every target offset fits.  Complex float is
+ * bounded to the 32 registers of full occupancy, with a 32-byte spill in the D32 form:
+ * at 40 registers (6 CTAs per SM) the complex PROD config took 180.2 us, at 32 (8 per
+ * SM) 170.0 us. */
 template <int BT, int OP, int CW, bool D32>
 __global__ void __launch_bounds__(YK_THREADS, (BT == YK_BT_C32 ? 7 : 1))
 yk_owner_chunk_kernel(const __grid_constant__ yk_launch L, int rshift)
