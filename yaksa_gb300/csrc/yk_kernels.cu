@@ -1250,11 +1250,15 @@ yk_owner_typed_kernel(const __grid_constant__ yk_launch L)
  * or before x, in block order.  Lanes of one block read the same displacement words
  * (one broadcast per warp), packed elements are read contiguously across the warp and
  * each block's target run is read and written by consecutive lanes. */
-template <int BT, int OP>
+template <int BT, int OP, bool D32>
 __global__ void __launch_bounds__(YK_THREADS)
 yk_owner_lane_kernel(const __grid_constant__ yk_launch L, int rshift)
 {
     typedef typename yk_elem<BT>::T T;
+    /* D32: offsets in 32 bits on the level's 32-bit copy of the displacements, where the
+     * host found that every target offset fits (as in yk_owner_chunk_kernel) */
+    typedef typename std::conditional<D32, int32_t, int64_t>::type OFF;
+    constexpr OFF OFF_MAX = D32 ? (OFF) INT32_MAX : (OFF) INT64_MAX;
     constexpr uint32_t es = (uint32_t) sizeof(T);
     /* elements per lane, loads issued together (complex pairs keep one, within the
      * register budget of full occupancy) */
@@ -1267,10 +1271,16 @@ yk_owner_lane_kernel(const __grid_constant__ yk_launch L, int rshift)
     const T *packed = (const T *) L.packed;     /* element 0 is packed byte p0 */
     char *typed = L.typed + L.desc.base;
     const uint32_t nthr = gridDim.x * YK_THREADS;
+    auto disp = [&](uint32_t i) -> OFF {
+        if constexpr (D32)
+            return __ldg((const int32_t *) (lv.disp + lv.count) + i);   /* the 32-bit copy */
+        else
+            return __ldg(lv.disp + i);
+    };
     for (uint32_t u0 = blockIdx.x * YK_THREADS + threadIdx.x; u0 < nunits; u0 += U * nthr) {
         /* every load that does not depend on another first: the block's displacement,
          * its predecessor's and successor's, and the packed element */
-        int64_t x[U], dn[U];
+        OFF x[U], dn[U];
         uint32_t b[U];
         bool own[U];
         T in[U], out[U], in1[U];
@@ -1282,13 +1292,13 @@ yk_owner_lane_kernel(const __grid_constant__ yk_launch L, int rshift)
                 continue;
             const uint32_t p = p0 + u * es;
             b[k] = p >> rshift;
-            const int64_t d = __ldg(lv.disp + b[k]);
-            const int64_t dp = b[k] > 0 ? __ldg(lv.disp + b[k] - 1) : 0;
-            dn[k] = b[k] + 1 < nblk ? __ldg(lv.disp + b[k] + 1) : INT64_MAX;
+            const OFF d = disp(b[k]);
+            const OFF dp = b[k] > 0 ? disp(b[k] - 1) : 0;
+            dn[k] = b[k] + 1 < nblk ? disp(b[k] + 1) : OFF_MAX;
             in[k] = __ldg(packed + u);
-            x[k] = d + (int64_t) (p & (R - 1));
+            x[k] = d + (OFF) (p & (R - 1));
             /* an earlier in-range block owns this element */
-            if (b[k] > 0 && x[k] < dp + (int64_t) R && (b[k] - 1) * R + (uint32_t) (x[k] - dp) >= p0)
+            if (b[k] > 0 && x[k] < dp + (OFF) R && (b[k] - 1) * R + (uint32_t) (x[k] - dp) >= p0)
                 own[k] = false;
         }
         /* then the target element and the next block's contribution, if any */
@@ -1302,7 +1312,7 @@ yk_owner_lane_kernel(const __grid_constant__ yk_launch L, int rshift)
                 if (pp < p1)
                     in1[k] = __ldg(packed + ((uint32_t) pp - p0) / es);
                 else
-                    dn[k] = INT64_MAX;
+                    dn[k] = OFF_MAX;
             }
         }
 #pragma unroll
@@ -1314,7 +1324,7 @@ yk_owner_lane_kernel(const __grid_constant__ yk_launch L, int rshift)
                 yk_elem<BT>::op(OP, in1[k], out[k]);
                 /* rarer: the blocks after that, in block order */
                 for (uint32_t bb = b[k] + 2; bb < nblk; bb++) {
-                    const int64_t d2 = __ldg(lv.disp + bb);
+                    const OFF d2 = disp(bb);
                     if (d2 > x[k])
                         break;
                     const uint64_t pp = ((uint64_t) bb << rshift) + (uint64_t) (x[k] - d2);
@@ -2511,8 +2521,12 @@ static bool yk_owner_lane_int(const yk_launch & c, int rshift, cudaStream_t s, u
                               bool d32)
 {
     switch ((int) c.op) {
-#define YK_OL(O) case O: if (!yk_owner_chunk_launch<BT, O>(c, rshift, s, g, chunk, d32))      \
-                             yk_owner_lane_kernel<BT, O><<<g, YK_THREADS, 0, s>>>(c, rshift);  \
+#define YK_OL(O) case O: if (!yk_owner_chunk_launch<BT, O>(c, rshift, s, g, chunk, d32)) {    \
+                             if (d32)                                                          \
+                                 yk_owner_lane_kernel<BT, O, true><<<g, YK_THREADS, 0, s>>>(c, rshift); \
+                             else                                                              \
+                                 yk_owner_lane_kernel<BT, O, false><<<g, YK_THREADS, 0, s>>>(c, rshift); \
+                         }                                                                     \
                          return true
         YK_OL(OP_MAX); YK_OL(OP_MIN); YK_OL(OP_SUM); YK_OL(OP_PROD); YK_OL(OP_LAND); YK_OL(OP_BAND);
         YK_OL(OP_LOR); YK_OL(OP_BOR); YK_OL(OP_LXOR); YK_OL(OP_BXOR); YK_OL(OP_REPLACE);
