@@ -689,7 +689,8 @@ static int launch_prepared(const yk_plan * p, const yk_launch * L, int kind, int
     return cuda_err((cudaError_t) e, "kernel launch");
 }
 
-/* TMA forms: 0 never, 1 as autotuner candidates (default), 2 always where one exists */
+/* L2-reduction form of overlapping unpacks: 0 never, 1 where it applies (default), a
+ * negative mode leaves it as it is; *launches receives the form's launches so far */
 int yaksa_gb300_debug_l2_reduce(int mode, unsigned long long *launches)
 {
     if (mode > 1)
@@ -701,6 +702,7 @@ int yaksa_gb300_debug_l2_reduce(int mode, unsigned long long *launches)
     return YAKSA_SUCCESS;
 }
 
+/* TMA forms: 0 never, 1 as autotuner candidates (default), 2 always where one exists */
 int yaksa_gb300_debug_tma(int mode)
 {
     if (mode < 0 || mode > 2)
