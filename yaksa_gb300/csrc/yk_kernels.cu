@@ -2593,11 +2593,11 @@ extern "C" int yk_cuda_launch_runs_pack(const yk_launch * l, uint32_t run, void 
     const uint64_t nel = l->nbytes / run;
     const unsigned g = yk_grid(nel, YK_THREADS, 8);
     cudaStream_t s = (cudaStream_t) stream;
-    static int warp_form = -1;
-    if (warp_form < 0) {
+    /* read once; the initialisation of a function-local static is thread-safe */
+    static const bool warp_form = [] {
         const char *e = getenv("YAKSA_GB300_RUNS_WARP");
-        warp_form = !(e && e[0] == '0');
-    }
+        return !(e && e[0] == '0');
+    }();
     if (warp_form && (uintptr_t) l->packed % 16 == 0 && run % 4 == 0 && run <= 32)
         yk_runs_pack_warp_kernel<2><<<g, YK_THREADS, 0, s>>>(*l, run);
     else if (warp_form && (uintptr_t) l->packed % 16 == 0 && run % 4 == 0 && run <= 48)

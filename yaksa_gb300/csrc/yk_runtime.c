@@ -58,7 +58,8 @@ static struct {
     int tma_mode;               /* TMA forms: 0 off, 1 autotuner candidates, 2 forced */
     int red_mode;               /* L2 reductions for order-independent integer operators
                                  * on overlapping blocks: 0 off, 1 where they apply */
-    int hidx_forced;            /* contiguous-block hindexed: 1 = hidx_cfg, 0 = autotuner */
+    int runs_pack;              /* one-thread-per-element packs of 17..47-byte runs */
+    int hidx_forced;           /* contiguous-block hindexed: 1 = hidx_cfg, 0 = autotuner */
     yk_tune_cfg hidx_cfg;
     /* library streams: requests that are not stream-ordered go round robin over
      * these, so independent requests (whose order the API leaves open) overlap on the
@@ -134,6 +135,8 @@ static int runtime_ready(void)
                 const char *rm = getenv("YAKSA_GB300_L2_REDUCE");
                 R.red_mode = !(rm && rm[0] == '0');
             }
+            const char *rp = getenv("YAKSA_GB300_RUNS_PACK");
+            R.runs_pack = !(rp && rp[0] == '0');
             const char *hd = getenv("YAKSA_GB300_HOST_DIRECT");
             R.host_direct = !(hd && hd[0] == '0');
             const char *ns = getenv("YAKSA_GB300_LIB_STREAMS");
@@ -608,13 +611,8 @@ static int prepare(const yk_plan * p, char *typed, char *packed, yk_launch * L, 
  * YAKSA_GB300_RUNS_PACK=0 in the environment keeps such packs on the byte kernels. */
 static int runs_pack_ok(const yk_launch * L)
 {
-    static int on = -1;
-    if (on < 0) {
-        const char *e = getenv("YAKSA_GB300_RUNS_PACK");
-        on = !(e && e[0] == '0');
-    }
     const uint64_t r = L->desc.run;
-    return on && L->dir == 0 && !L->typed_op && !L->use64 && L->regular == 1 &&
+    return R.runs_pack && L->dir == 0 && !L->typed_op && !L->use64 && L->regular == 1 &&
         L->desc.leaf == YK_LEAF_RUN && L->desc.lv[0].kind == YK_LV_VEC && L->desc.lv[0].cps == r &&
         r > 16 && r < 48 && r % 16 && (L->vec == 4 || L->vec == 8) && r % (uint64_t) L->vec == 0 &&
         L->desc.lv[0].stride > 0 && L->desc.lv[0].stride % 16 == 0 &&
