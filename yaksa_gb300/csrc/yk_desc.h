@@ -106,7 +106,8 @@ typedef struct {
                                  * with 32-bit positions; -1: any other shape */
     int32_t hidx;               /* 1: one HIDX level of contiguous blocks over its run */
     int32_t ldouble;            /* 1: the type holds long double (binary128 operators) */
-    int32_t pad_ld;
+    int32_t form;               /* server items of sorted blocks (YK_SRV_OWNER_T): the
+                                 * launch form the host chose, YK_FORM_* below */
 } yk_launch;
 
 #define YK_REGULAR_MAX 3
@@ -208,6 +209,14 @@ int yk_cuda_launch_pup_cfg(const yk_launch * l, void *stream, int units_per_thre
 #define YK_ORD_D32 8
 int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blocks, void *stream,
                                   int ctas_per_sm);
+/* The sorted-block kernel form of an aligned typed unpack (sorted_blocks 2, 32-bit
+ * positions, blocks of a power-of-two byte length): log2 of the block length in bits
+ * 0-7, the bytes per lane of the chunk form (8 or 16; 0 for one element per lane) in
+ * bits 8-15, YK_FORM_D32 for 32-bit target offsets, and YK_FORM_POW2 set.  0: no such
+ * form (the generic kernels apply). */
+#define YK_FORM_D32 (1 << 16)
+#define YK_FORM_POW2 (1 << 17)
+int yk_cuda_owner_form(const yk_launch * l, int sorted_blocks);
 /* launches of the L2-reduction form so far */
 unsigned long long yk_cuda_red_launches(void);
 

@@ -19,232 +19,7 @@
  * multiplication recovers infinities with the algorithm of ISO C11 Annex G.5.1 (what
  * libgcc's __mulsc3/__muldc3 implement for the reference's `*=` on _Complex values).
  */
-#include <atomic>
-#include <type_traits>
-#include <cuda_runtime.h>
-#include <stdint.h>
-#include "yk_desc.h"
-#include "yk_locate.h"
-#include "yk_quad.h"
-
-#define YK_THREADS 256
-#define YK_UNROLL 4
-
-extern "C" int yk_cuda_num_sms(void);
-extern "C" void yk_tma_count_launch(void);
-
-/* address decomposition shared with the host (yk_locate.h) */
-/* ------------------------------------------------------------------------- */
-
-__device__ __forceinline__ uint32_t yk_div(uint32_t n, const yk_level & l) { return yk_div32(n, &l); }
-__device__ __forceinline__ uint64_t yk_div(uint64_t n, const yk_level & l) { return yk_div64(n, &l); }
-
-template <typename IDX>
-__device__ __forceinline__ int64_t yk_locate(const yk_desc & d, IDX p, int *bt, uint64_t * inseg);
-template <>
-__device__ __forceinline__ int64_t yk_locate<uint32_t>(const yk_desc & d, uint32_t p, int *bt,
-                                                       uint64_t * inseg)
-{
-    return yk_locate32(&d, p, bt, inseg);
-}
-template <>
-__device__ __forceinline__ int64_t yk_locate<uint64_t>(const yk_desc & d, uint64_t p, int *bt,
-                                                       uint64_t * inseg)
-{
-    return yk_locate64(&d, p, bt, inseg);
-}
-
-/* ------------------------------------------------------------------------- */
-/* REPLACE: byte movement in V-byte units                                    */
-/* ------------------------------------------------------------------------- */
-
-template <int V> struct yk_vec;
-template <> struct yk_vec<1> { typedef uint8_t T; };
-template <> struct yk_vec<2> { typedef uint16_t T; };
-template <> struct yk_vec<4> { typedef uint32_t T; };
-template <> struct yk_vec<8> { typedef uint2 T; };
-template <> struct yk_vec<16> { typedef uint4 T; };
-
-/* Loads cached in L2 only: the strided side is read once, so it does not displace L1.
- * (An isolated 8-byte run still costs a whole 128-byte line from L2 on GB300, whatever
- * the cache operator or prefetch-size qualifier; measured for every documented form.) */
-__device__ __forceinline__ uint8_t yk_ldcg(const uint8_t * p)
-{
-    uint16_t v;
-    asm volatile ("ld.global.cg.u8 %0, [%1];" : "=h"(v) : "l"(p));
-    return (uint8_t) v;
-}
-
-__device__ __forceinline__ uint16_t yk_ldcg(const uint16_t * p)
-{
-    uint16_t v;
-    asm volatile ("ld.global.cg.u16 %0, [%1];" : "=h"(v) : "l"(p));
-    return v;
-}
-
-__device__ __forceinline__ uint32_t yk_ldcg(const uint32_t * p)
-{
-    uint32_t v;
-    asm volatile ("ld.global.cg.u32 %0, [%1];" : "=r"(v) : "l"(p));
-    return v;
-}
-
-__device__ __forceinline__ uint2 yk_ldcg(const uint2 * p)
-{
-    uint2 v;
-    asm volatile ("ld.global.cg.v2.u32 {%0, %1}, [%2];" : "=r"(v.x), "=r"(v.y) : "l"(p));
-    return v;
-}
-
-__device__ __forceinline__ uint4 yk_ldcg(const uint4 * p)
-{
-    uint4 v;
-    asm volatile ("ld.global.cg.v4.u32 {%0, %1, %2, %3}, [%4];"
-                  : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w) : "l"(p));
-    return v;
-}
-
-/* One tile: units t0 + k * YK_THREADS + threadIdx.x, k < U, of a request with
- * `nunits` V-byte units.  All U addresses are computed first and all U loads issued
- * before any store, so every thread keeps U independent memory requests in flight.
- * Loads use ld.global.cg (cache in L2 only): an L1-allocating load of an isolated
- * 8-byte run fills a 128-byte line, which is 16x the useful DRAM traffic for runs
- * at a large stride. */
-template <typename IDX, int V, int DIR, int U>
-__device__ __forceinline__ void yk_bytes_tile(const yk_launch & L, IDX t0, IDX nunits)
-{
-    typedef typename yk_vec<V>::T VT;
-    const IDX p0 = (IDX) L.p0;
-    VT *packed = (VT *) L.packed;
-    char *typed = L.typed;
-    int64_t off[U];
-    VT v[U];
-#pragma unroll
-    for (int k = 0; k < U; k++) {
-        IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
-        if (u < nunits)
-            off[k] = yk_locate<IDX>(L.desc, p0 + u * (IDX) V, nullptr, nullptr);
-    }
-    if (DIR == 0) {
-#pragma unroll
-        for (int k = 0; k < U; k++) {
-            IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
-            if (u < nunits)
-                v[k] = yk_ldcg((const VT *) (typed + off[k]));
-        }
-#pragma unroll
-        for (int k = 0; k < U; k++) {
-            IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
-            if (u < nunits)
-                packed[u] = v[k];
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < U; k++) {
-            IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
-            if (u < nunits)
-                v[k] = yk_ldcg((const VT *) (packed + u));
-        }
-#pragma unroll
-        for (int k = 0; k < U; k++) {
-            IDX u = t0 + (IDX) (k * YK_THREADS + threadIdx.x);
-            if (u < nunits)
-                *(VT *) (typed + off[k]) = v[k];
-        }
-    }
-}
-
-/* Regular nests (NL strided levels over one contiguous run, 32-bit positions): the
- * decomposition unrolls at compile time into NL multiply-high/shift/multiply-add steps
- * with no table loads, which keeps the kernel near 32 registers and lets eight
- * 256-thread CTAs share an SM (full occupancy, the most loads in flight). */
-/* the few fields of a regular request a tile needs, held in registers */
-struct yk_rt {
-    char *typed;                /* typed pointer + descriptor base */
-    char *packed;
-    uint32_t p0;
-    uint32_t m[YK_REGULAR_MAX];
-    uint32_t cps[YK_REGULAR_MAX];
-    uint32_t sh1[YK_REGULAR_MAX], sh2[YK_REGULAR_MAX];
-    int64_t stride[YK_REGULAR_MAX];
-};
-
-template <int NL>
-__device__ __forceinline__ void yk_rt_load(yk_rt & t, const yk_launch & L)
-{
-    t.typed = L.typed + L.desc.base;
-    t.packed = L.packed;
-    t.p0 = (uint32_t) L.p0;
-#pragma unroll
-    for (int i = 0; i < NL; i++) {
-        t.m[i] = L.desc.lv[i].m32;
-        t.cps[i] = (uint32_t) L.desc.lv[i].cps;
-        t.sh1[i] = L.desc.lv[i].l ? 1u : 0u;
-        t.sh2[i] = L.desc.lv[i].l ? (uint32_t) L.desc.lv[i].l - 1u : 0u;
-        t.stride[i] = L.desc.lv[i].stride;
-    }
-}
-
-template <int V, int DIR, int U, int NL>
-__device__ __forceinline__ void yk_regular_tile(const yk_launch & L, uint32_t t0, uint32_t nunits)
-{
-    typedef typename yk_vec<V>::T VT;
-    yk_rt rt;
-    yk_rt_load<NL>(rt, L);
-    VT *packed = (VT *) rt.packed;
-    char *typed = rt.typed;
-    int64_t off[U];
-    VT v[U];
-#pragma unroll
-    for (int k = 0; k < U; k++) {
-        uint32_t u = t0 + (uint32_t) (k * YK_THREADS + threadIdx.x);
-        uint32_t r = rt.p0 + u * (uint32_t) V;
-        int64_t o = 0;
-#pragma unroll
-        for (int i = 0; i < NL; i++) {
-            uint32_t t = __umulhi(rt.m[i], r);
-            uint32_t q = (t + ((r - t) >> rt.sh1[i])) >> rt.sh2[i];
-            r -= q * rt.cps[i];
-            o += (int64_t) q * rt.stride[i];
-        }
-        off[k] = o + (int64_t) r;
-    }
-    if (DIR == 0) {
-#pragma unroll
-        for (int k = 0; k < U; k++)
-            if (t0 + (uint32_t) (k * YK_THREADS + threadIdx.x) < nunits)
-                v[k] = yk_ldcg((const VT *) (typed + off[k]));
-#pragma unroll
-        for (int k = 0; k < U; k++) {
-            uint32_t u = t0 + (uint32_t) (k * YK_THREADS + threadIdx.x);
-            if (u < nunits)
-                packed[u] = v[k];
-        }
-    } else {
-#pragma unroll
-        for (int k = 0; k < U; k++) {
-            uint32_t u = t0 + (uint32_t) (k * YK_THREADS + threadIdx.x);
-            if (u < nunits)
-                v[k] = yk_ldcg((const VT *) (packed + u));
-        }
-#pragma unroll
-        for (int k = 0; k < U; k++)
-            if (t0 + (uint32_t) (k * YK_THREADS + threadIdx.x) < nunits)
-                *(VT *) (typed + off[k]) = v[k];
-    }
-}
-
-template <int V, int DIR, int U>
-__device__ __forceinline__ void yk_regular_dispatch(const yk_launch & L, uint32_t t0,
-                                                    uint32_t nunits)
-{
-    switch (L.regular) {
-        case 0: yk_regular_tile<V, DIR, U, 0>(L, t0, nunits); break;
-        case 1: yk_regular_tile<V, DIR, U, 1>(L, t0, nunits); break;
-        case 2: yk_regular_tile<V, DIR, U, 2>(L, t0, nunits); break;
-        default: yk_regular_tile<V, DIR, U, 3>(L, t0, nunits); break;
-    }
-}
+#include "yk_device.cuh"
 
 template <int V, int DIR, int U>
 __global__ void __launch_bounds__(YK_THREADS, (U == 1 ? 8 : 4))
@@ -358,113 +133,14 @@ yk_hidx_kernel(const __grid_constant__ yk_launch L)
     }
 }
 
-/* The same walk for requests under 4 GiB, in packed positions relative to each group's
- * first byte: 32-bit search keys (one shuffle per step instead of two) and per-lane
- * state small enough for every warp slot of the SM to stay resident.  Lane k keeps its
- * block's start relative to the group (0 for a block that starts before the range) and
- * the typed offset of relative position 0 in that block, so a unit's typed offset is one
- * shuffle and one add.
- *
- * The kernel is latency-bound (random block starts, a few KiB per group), so each warp
- * keeps as much in flight as its registers allow: the four index words of its next
- * group are loaded while the current group is walked, and U units per lane move per
- * step.  A pack finds the units' typed offsets first and then loads them; an unpack
- * loads its contiguous packed units first (no offsets needed) and locates each unit
- * only to store it, so no offsets are live across the load.  MINB CTAs of the block
- * size are meant to stay resident; the autotuner chooses among the shapes. */
+/* yk_hidx32_groups over the whole request, MINB CTAs of the block size resident */
 template <int V, int DIR, int U, int MINB, bool PF>
 __global__ void __launch_bounds__(YK_THREADS, MINB)
 yk_hidx32_kernel(const __grid_constant__ yk_launch L)
 {
-    typedef typename yk_vec<V>::T VT;
-    const yk_level *lv = &L.desc.lv[0];
-    const uint64_t p0 = L.p0, p1 = L.p0 + L.nbytes;
-    const int lane = threadIdx.x & 31;
-    const uint64_t warp = ((uint64_t) blockIdx.x * YK_THREADS + threadIdx.x) >> 5;
-    const uint64_t nwarps = ((uint64_t) gridDim.x * YK_THREADS) >> 5;
-    char *typed = L.typed + L.desc.base;
-    const uint64_t jb = yk_hidx_block(lv, p0), je = yk_hidx_block(lv, p1 - 1);
-    const uint64_t ngroups = (je - jb + 32) / 32;
-    /* the index words of the group a warp takes next: its first block's packed start,
-     * the end of its last block, and this lane's block start and displacement */
-    uint64_t f_first = 0, f_end = 0, f_bp = 0;
-    int64_t f_disp = 0;
-    auto fetch = [&](uint64_t gg) {
-        const uint64_t j0 = jb + gg * 32, jl = j0 + (uint64_t) lane;
-        const uint64_t jend = min(j0 + 32, je + 1);
-        f_first = __ldg(lv->pfx + j0);
-        f_end = __ldg(lv->pfx + jend);
-        if (jl < jend) {
-            f_bp = __ldg(lv->pfx + jl);
-            f_disp = __ldg(lv->disp + jl);
-        }
-    };
-    if (PF && warp < ngroups)
-        fetch(warp);
-    for (uint64_t g = warp; g < ngroups; g += nwarps) {
-        const uint64_t j0 = jb + g * 32;
-        const uint64_t jl = j0 + (uint64_t) lane;
-        const uint64_t jend = min(j0 + 32, je + 1);
-        if (!PF)
-            fetch(g);
-        const uint64_t gs = max(f_first, p0);
-        const uint32_t n = (uint32_t) (min(f_end, p1) - gs);
-        uint32_t my_rel = 0xffffffffu;
-        int64_t my_adj = 0;
-        if (jl < jend) {
-            my_rel = f_bp <= gs ? 0u : (uint32_t) (f_bp - gs);
-            my_adj = f_disp - ((int64_t) f_bp - (int64_t) gs);
-        }
-        if (PF && g + nwarps < ngroups)
-            fetch(g + nwarps);
-        VT *pk = (VT *) (L.packed + (gs - p0));
-        for (uint32_t base = 0; base < n; base += 32u * V * U) {
-            if (DIR == 0) {
-                int64_t off[U];
-#pragma unroll
-                for (int k = 0; k < U; k++) {
-                    const uint32_t r = base + (uint32_t) (k * 32 + lane) * V;
-                    int idx = 0;
-#pragma unroll
-                    for (int step = 16; step > 0; step >>= 1) {
-                        const uint32_t c = __shfl_sync(0xffffffffu, my_rel, idx + step);
-                        if (c <= r)
-                            idx += step;
-                    }
-                    off[k] = __shfl_sync(0xffffffffu, my_adj, idx) + (int64_t) r;
-                }
-                VT v[U];
-#pragma unroll
-                for (int k = 0; k < U; k++)
-                    if (base + (uint32_t) (k * 32 + lane) * V < n)
-                        v[k] = yk_ldcg((const VT *) (typed + off[k]));
-#pragma unroll
-                for (int k = 0; k < U; k++)
-                    if (base + (uint32_t) (k * 32 + lane) * V < n)
-                        pk[base / V + (uint32_t) (k * 32 + lane)] = v[k];
-            } else {
-                VT v[U];
-#pragma unroll
-                for (int k = 0; k < U; k++)
-                    if (base + (uint32_t) (k * 32 + lane) * V < n)
-                        v[k] = yk_ldcg(pk + base / V + (uint32_t) (k * 32 + lane));
-#pragma unroll
-                for (int k = 0; k < U; k++) {
-                    const uint32_t r = base + (uint32_t) (k * 32 + lane) * V;
-                    int idx = 0;
-#pragma unroll
-                    for (int step = 16; step > 0; step >>= 1) {
-                        const uint32_t c = __shfl_sync(0xffffffffu, my_rel, idx + step);
-                        if (c <= r)
-                            idx += step;
-                    }
-                    const int64_t off = __shfl_sync(0xffffffffu, my_adj, idx) + (int64_t) r;
-                    if (r < n)
-                        *(VT *) (typed + off) = v[k];
-                }
-            }
-        }
-    }
+    yk_hidx32_groups<V, DIR, U, PF>(L, L.p0, L.p0 + L.nbytes,
+                                    ((uint64_t) blockIdx.x * YK_THREADS + threadIdx.x) >> 5,
+                                    ((uint64_t) gridDim.x * YK_THREADS) >> 5);
 }
 
 
@@ -683,55 +359,14 @@ yk_runs_pack_kernel(const __grid_constant__ yk_launch L, uint32_t R)
     }
 }
 
-/* The same pack with the packed side staged per warp: each lane still reads its run
- * with 16-byte loads and puts its R bytes at lane * R in the warp's shared-memory tile;
- * after __syncwarp the warp writes the tile's 32 * R packed bytes as 16-byte chunks at
- * consecutive addresses.  The per-lane form writes R/4 pieces of 4 bytes at an R-byte
- * stride, so each of its store instructions touches about R sectors for 128 bytes;
- * here a store instruction fills whole sectors.  Only a warp, not the CTA, waits on the
- * tile.  Needs the packed pointer on 16 bytes (checked by the launcher) and R a
- * multiple of 4; a group of fewer than 32 elements writes its last bytes as 4-byte
- * words. */
+/* yk_runs_pack_groups over the whole request, each warp with its own stage */
 template <int NV>
 __global__ void __launch_bounds__(YK_THREADS, 8)
 yk_runs_pack_warp_kernel(const __grid_constant__ yk_launch L, uint32_t R)
 {
     __shared__ __align__(16) unsigned char stage[YK_THREADS / 32][32 * 48];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int64_t E = L.desc.lv[0].stride;
-    const uint32_t nel = (uint32_t) (L.nbytes / R), e0 = (uint32_t) (L.p0 / R);
-    const char *tb = L.typed + L.desc.base;
-    const uint32_t nw4 = R / 4;      /* R <= 16 * NV */
-    unsigned char *st = stage[w];
-    const uint32_t gw = (blockIdx.x * YK_THREADS + threadIdx.x) >> 5;
-    const uint32_t nwarps = (gridDim.x * YK_THREADS) >> 5;
-    for (uint32_t i0 = gw * 32; i0 < nel; i0 += nwarps * 32) {
-        const uint32_t i = i0 + (uint32_t) lane;
-        const uint32_t n = min(32u, nel - i0);
-        if (i < nel) {
-            const char *src = tb + (int64_t) (e0 + i) * E;
-            union {
-                uint4 w[NV];
-                uint32_t u[4 * NV];
-            } v;
-#pragma unroll
-            for (int k = 0; k < NV; k++)
-                v.w[k] = yk_ldcg((const uint4 *) (src + 16 * k));
-            uint32_t *sw = (uint32_t *) (st + (uint32_t) lane * R);
-#pragma unroll
-            for (int j = 0; j < 4 * NV; j++)
-                if ((uint32_t) j < nw4)
-                    sw[j] = v.u[j];
-        }
-        __syncwarp();
-        char *dst = L.packed + (uint64_t) i0 * R;
-        const uint32_t nbytes = n * R, nch = nbytes / 16;
-        for (uint32_t c = (uint32_t) lane; c < nch; c += 32)
-            *(uint4 *) (dst + 16 * c) = *(const uint4 *) (st + 16 * c);
-        for (uint32_t q = nch * 16 + (uint32_t) lane * 4; q < nbytes; q += 128)
-            *(uint32_t *) (dst + q) = *(const uint32_t *) (st + q);
-        __syncwarp();
-    }
+    yk_runs_pack_groups<NV>(L, R, stage[threadIdx.x >> 5], ((blockIdx.x * YK_THREADS + threadIdx.x) >> 5) * 32,
+                            (uint32_t) (L.nbytes / R), ((gridDim.x * YK_THREADS) >> 5) * 32);
 }
 
 extern "C" int yk_cuda_launch_runs_pack(const yk_launch * l, uint32_t run, void *stream);
@@ -775,328 +410,6 @@ yk_batch_kernel(const __grid_constant__ yk_batch B)
     }
 }
 
-/* ------------------------------------------------------------------------- */
-/* elementwise operators                                                     */
-/* ------------------------------------------------------------------------- */
-
-enum { OP_MAX = 0, OP_MIN = 1, OP_SUM = 2, OP_PROD = 3, OP_LAND = 4, OP_BAND = 5, OP_LOR = 6,
-    OP_BOR = 7, OP_LXOR = 8, OP_BXOR = 9, OP_REPLACE = 10 };
-
-template <typename T> __device__ __forceinline__ T yk_ld(const char *p)
-{
-    if (((uintptr_t) p & (sizeof(T) - 1)) == 0)
-        return *(const T *) p;
-    T v;
-    char *q = (char *) &v;
-#pragma unroll
-    for (int i = 0; i < (int) sizeof(T); i++)
-        q[i] = p[i];
-    return v;
-}
-
-template <typename T> __device__ __forceinline__ void yk_st(char *p, T v)
-{
-    if (((uintptr_t) p & (sizeof(T) - 1)) == 0) {
-        *(T *) p = v;
-        return;
-    }
-    const char *q = (const char *) &v;
-#pragma unroll
-    for (int i = 0; i < (int) sizeof(T); i++)
-        p[i] = q[i];
-}
-
-/* integer operators; returns false when op is outside the type's table */
-template <typename S, typename U>
-__device__ __forceinline__ bool yk_int_op(int op, S in, S & out)
-{
-    switch (op) {
-        case OP_REPLACE:
-            out = in;
-            return true;
-        case OP_MAX:
-            out = (in < out) ? out : in;
-            return true;
-        case OP_MIN:
-            out = (in < out) ? in : out;
-            return true;
-        case OP_SUM:
-            out = (S) (U) ((U) out + (U) in);
-            return true;
-        case OP_PROD:
-            out = (S) (U) ((U) out * (U) in);
-            return true;
-        case OP_LAND:
-            out = (S) (out && in);
-            return true;
-        case OP_LOR:
-            out = (S) (out || in);
-            return true;
-        case OP_LXOR:
-            out = (S) (!out != !in);
-            return true;
-        case OP_BAND:
-            out = (S) (out & in);
-            return true;
-        case OP_BOR:
-            out = (S) (out | in);
-            return true;
-        case OP_BXOR:
-            out = (S) (out ^ in);
-            return true;
-    }
-    return false;
-}
-
-__device__ __forceinline__ float yk_add(float a, float b) { return __fadd_rn(a, b); }
-__device__ __forceinline__ double yk_add(double a, double b) { return __dadd_rn(a, b); }
-__device__ __forceinline__ float yk_sub(float a, float b) { return __fsub_rn(a, b); }
-__device__ __forceinline__ double yk_sub(double a, double b) { return __dsub_rn(a, b); }
-__device__ __forceinline__ float yk_mul(float a, float b) { return __fmul_rn(a, b); }
-__device__ __forceinline__ double yk_mul(double a, double b) { return __dmul_rn(a, b); }
-
-template <typename F>
-__device__ __forceinline__ bool yk_flt_op(int op, F in, F & out)
-{
-    switch (op) {
-        case OP_REPLACE:
-            out = in;
-            return true;
-        case OP_MAX:
-            out = (in < out) ? out : in;
-            return true;
-        case OP_MIN:
-            out = (in > out) ? out : in;
-            return true;
-        case OP_SUM:
-            out = yk_add(out, in);
-            return true;
-        case OP_PROD:
-            out = yk_mul(out, in);
-            return true;
-    }
-    return false;
-}
-
-/* (a + ib) * (c + id) with the infinity recovery of ISO C11 Annex G.5.1 */
-template <typename F>
-__device__ __forceinline__ void yk_cmul(F a, F b, F c, F d, F & x, F & y)
-{
-    F ac = yk_mul(a, c), bd = yk_mul(b, d), ad = yk_mul(a, d), bc = yk_mul(b, c);
-    x = yk_sub(ac, bd);
-    y = yk_add(ad, bc);
-    if (isnan(x) && isnan(y)) {
-        bool recalc = false;
-        const F one = (F) 1, zero = (F) 0;
-        if (isinf(a) || isinf(b)) {
-            a = copysign(isinf(a) ? one : zero, a);
-            b = copysign(isinf(b) ? one : zero, b);
-            if (isnan(c))
-                c = copysign(zero, c);
-            if (isnan(d))
-                d = copysign(zero, d);
-            recalc = true;
-        }
-        if (isinf(c) || isinf(d)) {
-            c = copysign(isinf(c) ? one : zero, c);
-            d = copysign(isinf(d) ? one : zero, d);
-            if (isnan(a))
-                a = copysign(zero, a);
-            if (isnan(b))
-                b = copysign(zero, b);
-            recalc = true;
-        }
-        if (!recalc && (isinf(ac) || isinf(bd) || isinf(ad) || isinf(bc))) {
-            if (isnan(a))
-                a = copysign(zero, a);
-            if (isnan(b))
-                b = copysign(zero, b);
-            if (isnan(c))
-                c = copysign(zero, c);
-            if (isnan(d))
-                d = copysign(zero, d);
-            recalc = true;
-        }
-        if (recalc) {
-            const F inf = (F) INFINITY;
-            x = yk_mul(inf, yk_sub(yk_mul(a, c), yk_mul(b, d)));
-            y = yk_mul(inf, yk_add(yk_mul(a, d), yk_mul(b, c)));
-        }
-    }
-}
-
-template <typename F>
-__device__ __forceinline__ bool yk_cplx_op(int op, const F in[2], F out[2])
-{
-    switch (op) {
-        case OP_REPLACE:
-            out[0] = in[0];
-            out[1] = in[1];
-            return true;
-        case OP_SUM:
-            out[0] = yk_add(out[0], in[0]);
-            out[1] = yk_add(out[1], in[1]);
-            return true;
-        case OP_PROD:{
-                F x, y;
-                yk_cmul(out[0], out[1], in[0], in[1], x, y);
-                out[0] = x;
-                out[1] = y;
-                return true;
-            }
-    }
-    return false;
-}
-
-__device__ __forceinline__ yk_u128 yk_ldq(const char *p)
-{
-    return ((yk_u128) yk_ld<uint64_t>(p + 8) << 64) | (yk_u128) yk_ld<uint64_t>(p);
-}
-
-__device__ __forceinline__ void yk_stq(char *p, yk_u128 v)
-{
-    yk_st<uint64_t>(p, (uint64_t) v);
-    yk_st<uint64_t>(p + 8, (uint64_t) (v >> 64));
-}
-
-/* long double and long double complex in binary128: `out = out op in` as the
- * reference's seq loops compute it (MAX and MIN are the selects of the float types) */
-__device__ __forceinline__ void yk_q_apply(int bt, int op, char *dst, const char *src)
-{
-    if (bt == YK_BT_LDOUBLE) {
-        const yk_u128 in = yk_ldq(src), out = yk_ldq(dst);
-        yk_u128 r;
-        switch (op) {
-            case OP_REPLACE: r = in; break;
-            case OP_MAX: r = yk_q_lt(in, out) ? out : in; break;
-            case OP_MIN: r = yk_q_lt(out, in) ? out : in; break;
-            case OP_SUM: r = yk_q_add(out, in); break;
-            case OP_PROD: r = yk_q_mul(out, in); break;
-            default: return;
-        }
-        yk_stq(dst, r);
-        return;
-    }
-    const yk_u128 ir = yk_ldq(src), ii = yk_ldq(src + 16);
-    yk_u128 orr = yk_ldq(dst), oi = yk_ldq(dst + 16);
-    switch (op) {
-        case OP_REPLACE:
-            orr = ir;
-            oi = ii;
-            break;
-        case OP_SUM:
-            orr = yk_q_add(orr, ir);
-            oi = yk_q_add(oi, ii);
-            break;
-        case OP_PROD:
-            yk_q_cmul(orr, oi, ir, ii, &orr, &oi);
-            break;
-        default:
-            return;
-    }
-    yk_stq(dst, orr);
-    yk_stq(dst + 16, oi);
-}
-
-/* apply op to one element of base type bt; `dst` is updated in place from `src`.
- * LD: the instance for types that hold long double, with the binary128 operators;
- * the other instance moves long double bytes for REPLACE only (the host sends every
- * long double operator to the LD instances), which keeps the 128-bit arithmetic out
- * of the register budget of the common kernels. */
-template <bool LD>
-__device__ __forceinline__ void yk_apply(int bt, int op, char *dst, const char *src)
-{
-    switch (bt) {
-        case YK_BT_BOOL:{
-                if (op != OP_REPLACE && op != OP_LAND && op != OP_LOR && op != OP_LXOR)
-                    return;
-                uint8_t i = yk_ld<uint8_t>(src), o = yk_ld<uint8_t>(dst);
-                uint8_t r = op == OP_REPLACE ? i : op == OP_LAND ? (uint8_t) (o && i) :
-                    op == OP_LOR ? (uint8_t) (o || i) : (uint8_t) (!o != !i);
-                yk_st<uint8_t>(dst, r);
-                return;
-            }
-        case YK_BT_I8:{
-                int8_t i = yk_ld<int8_t>(src), o = yk_ld<int8_t>(dst);
-                if (yk_int_op<int8_t, uint8_t>(op, i, o))
-                    yk_st<int8_t>(dst, o);
-                return;
-            }
-        case YK_BT_I16:{
-                int16_t i = yk_ld<int16_t>(src), o = yk_ld<int16_t>(dst);
-                if (yk_int_op<int16_t, uint16_t>(op, i, o))
-                    yk_st<int16_t>(dst, o);
-                return;
-            }
-        case YK_BT_I32:{
-                int32_t i = yk_ld<int32_t>(src), o = yk_ld<int32_t>(dst);
-                if (yk_int_op<int32_t, uint32_t>(op, i, o))
-                    yk_st<int32_t>(dst, o);
-                return;
-            }
-        case YK_BT_I64:{
-                int64_t i = yk_ld<int64_t>(src), o = yk_ld<int64_t>(dst);
-                if (yk_int_op<int64_t, uint64_t>(op, i, o))
-                    yk_st<int64_t>(dst, o);
-                return;
-            }
-        case YK_BT_F32:{
-                float i = yk_ld<float>(src), o = yk_ld<float>(dst);
-                if (yk_flt_op<float>(op, i, o))
-                    yk_st<float>(dst, o);
-                return;
-            }
-        case YK_BT_F64:{
-                double i = yk_ld<double>(src), o = yk_ld<double>(dst);
-                if (yk_flt_op<double>(op, i, o))
-                    yk_st<double>(dst, o);
-                return;
-            }
-        case YK_BT_C32:{
-                float i[2] = { yk_ld<float>(src), yk_ld<float>(src + 4) };
-                float o[2] = { yk_ld<float>(dst), yk_ld<float>(dst + 4) };
-                if (yk_cplx_op<float>(op, i, o)) {
-                    yk_st<float>(dst, o[0]);
-                    yk_st<float>(dst + 4, o[1]);
-                }
-                return;
-            }
-        case YK_BT_C64:{
-                double i[2] = { yk_ld<double>(src), yk_ld<double>(src + 8) };
-                double o[2] = { yk_ld<double>(dst), yk_ld<double>(dst + 8) };
-                if (yk_cplx_op<double>(op, i, o)) {
-                    yk_st<double>(dst, o[0]);
-                    yk_st<double>(dst + 8, o[1]);
-                }
-                return;
-            }
-        case YK_BT_LDOUBLE: case YK_BT_CLDOUBLE:
-            if (LD) {
-                yk_q_apply(bt, op, dst, src);
-            } else if (op == OP_REPLACE) {
-                yk_stq(dst, yk_ldq(src));
-                if (bt == YK_BT_CLDOUBLE)
-                    yk_stq(dst + 16, yk_ldq(src + 16));
-            }
-            return;
-        default:
-            /* CHAR/WCHAR only have REPLACE, which never reaches the typed kernel */
-            return;
-    }
-}
-
-__host__ __device__ __forceinline__ int yk_bt_size(int bt)
-{
-    switch (bt) {
-        case YK_BT_BOOL: case YK_BT_CHAR: case YK_BT_I8: return 1;
-        case YK_BT_I16: return 2;
-        case YK_BT_WCHAR: case YK_BT_I32: case YK_BT_F32: return 4;
-        case YK_BT_I64: case YK_BT_F64: case YK_BT_C32: return 8;
-        case YK_BT_C64: case YK_BT_LDOUBLE: return 16;
-        case YK_BT_CLDOUBLE: return 32;
-        default: return 1;
-    }
-}
 
 /* Operators: one work unit = `vec` bytes (the gcd of the element sizes); the unit
  * that starts an element applies op to that whole element. */
@@ -1127,53 +440,6 @@ yk_typed_kernel(const __grid_constant__ yk_launch L)
 /* ------------------------------------------------------------------------- */
 /* ordered unpack for overlapping targets                                    */
 /* ------------------------------------------------------------------------- */
-
-/* element types in registers, for the typed ordered-unpack kernel */
-template <int BT> struct yk_elem;
-template <> struct yk_elem<YK_BT_I8> {
-    typedef int8_t T;
-    static __device__ __forceinline__ bool op(int o, T in, T & out) { return yk_int_op<int8_t, uint8_t>(o, in, out); }
-};
-template <> struct yk_elem<YK_BT_I16> {
-    typedef int16_t T;
-    static __device__ __forceinline__ bool op(int o, T in, T & out) { return yk_int_op<int16_t, uint16_t>(o, in, out); }
-};
-template <> struct yk_elem<YK_BT_I32> {
-    typedef int32_t T;
-    static __device__ __forceinline__ bool op(int o, T in, T & out) { return yk_int_op<int32_t, uint32_t>(o, in, out); }
-};
-template <> struct yk_elem<YK_BT_I64> {
-    typedef int64_t T;
-    static __device__ __forceinline__ bool op(int o, T in, T & out) { return yk_int_op<int64_t, uint64_t>(o, in, out); }
-};
-template <> struct yk_elem<YK_BT_F32> {
-    typedef float T;
-    static __device__ __forceinline__ bool op(int o, T in, T & out) { return yk_flt_op<float>(o, in, out); }
-};
-template <> struct yk_elem<YK_BT_F64> {
-    typedef double T;
-    static __device__ __forceinline__ bool op(int o, T in, T & out) { return yk_flt_op<double>(o, in, out); }
-};
-template <> struct yk_elem<YK_BT_C32> {
-    typedef float2 T;
-    static __device__ __forceinline__ bool op(int o, T in, T & out)
-    {
-        float a[2] = { in.x, in.y }, b[2] = { out.x, out.y };
-        bool r = yk_cplx_op<float>(o, a, b);
-        out = make_float2(b[0], b[1]);
-        return r;
-    }
-};
-template <> struct yk_elem<YK_BT_C64> {
-    typedef double2 T;
-    static __device__ __forceinline__ bool op(int o, T in, T & out)
-    {
-        double a[2] = { in.x, in.y }, b[2] = { out.x, out.y };
-        bool r = yk_cplx_op<double>(o, a, b);
-        out = make_double2(b[0], b[1]);
-        return r;
-    }
-};
 
 /* Sorted blocks, typed: the same ownership rule as yk_owner_kernel below, with U
  * elements per thread and every index and data load issued before the ordered
@@ -1242,119 +508,17 @@ yk_owner_typed_kernel(const __grid_constant__ yk_launch L)
     }
 }
 
-/* Sorted blocks of a power-of-two byte length R, one packed element per lane (32-bit
- * positions), operator fixed at compile time.  The ownership rule of yk_owner_kernel
- * below: element x = disp[b] + j of block b belongs to b unless block b-1 covers x from
- * a position inside the range; no earlier block can cover x when b-1 does not, because
- * the displacements ascend.  The owner folds in the blocks b+1, b+2, ... that start at
- * or before x, in block order.  Lanes of one block read the same displacement words
- * (one broadcast per warp), packed elements are read contiguously across the warp and
- * each block's target run is read and written by consecutive lanes. */
+/* yk_owner_lane_units over the whole request, grid-stride */
 template <int BT, int OP, bool D32>
 __global__ void __launch_bounds__(YK_THREADS)
 yk_owner_lane_kernel(const __grid_constant__ yk_launch L, int rshift)
 {
-    typedef typename yk_elem<BT>::T T;
-    /* D32: offsets in 32 bits on the level's 32-bit copy of the displacements, where the
-     * host found that every target offset fits (as in yk_owner_chunk_kernel) */
-    typedef typename std::conditional<D32, int32_t, int64_t>::type OFF;
-    constexpr OFF OFF_MAX = D32 ? (OFF) INT32_MAX : (OFF) INT64_MAX;
-    constexpr uint32_t es = (uint32_t) sizeof(T);
-    /* elements per lane, loads issued together (complex pairs keep one, within the
-     * register budget of full occupancy) */
-    constexpr int U = (BT == YK_BT_C32 || BT == YK_BT_C64) ? 1 : 2;
-    const uint32_t R = 1u << rshift;
-    const yk_level & lv = L.desc.lv[0];
-    const uint32_t p0 = (uint32_t) L.p0, p1 = (uint32_t) (L.p0 + L.nbytes);
-    const uint32_t nblk = (uint32_t) lv.count;
-    const uint32_t nunits = (uint32_t) (L.nbytes / es);
-    const T *packed = (const T *) L.packed;     /* element 0 is packed byte p0 */
-    char *typed = L.typed + L.desc.base;
-    const uint32_t nthr = gridDim.x * YK_THREADS;
-    auto disp = [&](uint32_t i) -> OFF {
-        if constexpr (D32)
-            return __ldg((const int32_t *) (lv.disp + lv.count) + i);   /* the 32-bit copy */
-        else
-            return __ldg(lv.disp + i);
-    };
-    for (uint32_t u0 = blockIdx.x * YK_THREADS + threadIdx.x; u0 < nunits; u0 += U * nthr) {
-        /* every load that does not depend on another first: the block's displacement,
-         * its predecessor's and successor's, and the packed element */
-        OFF x[U], dn[U];
-        uint32_t b[U];
-        bool own[U];
-        T in[U], out[U], in1[U];
-#pragma unroll
-        for (int k = 0; k < U; k++) {
-            const uint32_t u = u0 + k * nthr;
-            own[k] = u < nunits;
-            if (!own[k])
-                continue;
-            const uint32_t p = p0 + u * es;
-            b[k] = p >> rshift;
-            const OFF d = disp(b[k]);
-            const OFF dp = b[k] > 0 ? disp(b[k] - 1) : 0;
-            dn[k] = b[k] + 1 < nblk ? disp(b[k] + 1) : OFF_MAX;
-            in[k] = __ldg(packed + u);
-            x[k] = d + (OFF) (p & (R - 1));
-            /* an earlier in-range block owns this element */
-            if (b[k] > 0 && x[k] < dp + (OFF) R && (b[k] - 1) * R + (uint32_t) (x[k] - dp) >= p0)
-                own[k] = false;
-        }
-        /* then the target element and the next block's contribution, if any */
-#pragma unroll
-        for (int k = 0; k < U; k++) {
-            if (!own[k])
-                continue;
-            out[k] = *(const T *) (typed + x[k]);
-            if (dn[k] <= x[k]) {
-                const uint64_t pp = ((uint64_t) (b[k] + 1) << rshift) + (uint64_t) (x[k] - dn[k]);
-                if (pp < p1)
-                    in1[k] = __ldg(packed + ((uint32_t) pp - p0) / es);
-                else
-                    dn[k] = OFF_MAX;
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < U; k++) {
-            if (!own[k])
-                continue;
-            yk_elem<BT>::op(OP, in[k], out[k]);
-            if (dn[k] <= x[k]) {
-                yk_elem<BT>::op(OP, in1[k], out[k]);
-                /* rarer: the blocks after that, in block order */
-                for (uint32_t bb = b[k] + 2; bb < nblk; bb++) {
-                    const OFF d2 = disp(bb);
-                    if (d2 > x[k])
-                        break;
-                    const uint64_t pp = ((uint64_t) bb << rshift) + (uint64_t) (x[k] - d2);
-                    if (pp >= p1)
-                        break;  /* later blocks place x later still */
-                    yk_elem<BT>::op(OP, __ldg(packed + ((uint32_t) pp - p0) / es), out[k]);
-                }
-            }
-            *(T *) (typed + x[k]) = out[k];
-        }
-    }
+    yk_owner_lane_units<BT, OP, D32>(L, rshift, blockIdx.x * YK_THREADS + threadIdx.x,
+                                     (uint32_t) (L.nbytes / sizeof(typename yk_elem<BT>::T)),
+                                     gridDim.x * YK_THREADS);
 }
 
-/* The same with one CW-byte packed chunk per lane (CW 8 or 16; elements of 1, 2 or 4
- * bytes, or 8-byte elements other than double): the chunk's elements share one block
- * (blocks are a multiple of CW bytes long and the range and the packed pointer sit on
- * CW bytes, checked on the host), so its displacement words and the packed load serve
- * CW/es elements.
- *
- * With at most four elements per chunk the fold has no loop for the common cases: the
- * displacements of the next two blocks are loaded with the chunk's own, their
- * contributions are loaded by predicated loads, and each is folded in by a select.  A
- * warp then executes one instruction stream with all its lanes, instead of a branch
- * per owner and a loop of dependent loads run by a few lanes (which left 12.8 of 32
- * lanes active per instruction).  Only a third later block, rare at these shapes,
- * takes the loop.  double keeps yk_owner_lane_kernel: there every fold is a DADD on
- * GB300's narrow FP64 pipe, which the selects would spend on every lane.
- *
- * D32: offsets and ownership tests in 32 bits on the level's 32-bit copy of the
- * displacements, where the host found that every target offset fits.  Complex float is
+/* yk_owner_chunk_units over the whole request, grid-stride.  Complex float is
  * bounded to the 32 registers of full occupancy, with a 32-byte spill in the D32 form:
  * at 40 registers (6 CTAs per SM) the complex PROD config took 180.2 us, at 32 (8 per
  * SM) 170.0 us. */
@@ -1362,206 +526,19 @@ template <int BT, int OP, int CW, bool D32>
 __global__ void __launch_bounds__(YK_THREADS, (BT == YK_BT_C32 ? 7 : 1))
 yk_owner_chunk_kernel(const __grid_constant__ yk_launch L, int rshift)
 {
-    typedef typename yk_elem<BT>::T T;
-    typedef typename yk_vec<CW>::T CT;
-    /* target offsets in 32 bits when the host found that every one fits (the level's
-     * 32-bit copy of the displacements is read), else in 64 bits */
-    typedef typename std::conditional<D32, int32_t, int64_t>::type OFF;
-    constexpr OFF OFF_MAX = D32 ? (OFF) INT32_MAX : (OFF) INT64_MAX;
-    constexpr uint32_t es = (uint32_t) sizeof(T);
-    constexpr int E = CW / (int) es;
-    const uint32_t R = 1u << rshift;
-    const yk_level & lv = L.desc.lv[0];
-    const uint32_t p0 = (uint32_t) L.p0, p1 = (uint32_t) (L.p0 + L.nbytes);
-    const uint32_t nblk = (uint32_t) lv.count;
-    const uint32_t nchunks = (uint32_t) (L.nbytes / CW);
-    const CT *packedc = (const CT *) L.packed;  /* chunk 0 is byte p0 */
-    const T *packed = (const T *) L.packed;
-    char *typed = L.typed + L.desc.base;
-    auto disp = [&](uint32_t i) -> OFF {
-        if constexpr (D32)
-            return __ldg((const int32_t *) (lv.disp + lv.count) + i);   /* the 32-bit copy */
-        else
-            return __ldg(lv.disp + i);
-    };
-    for (uint32_t u = blockIdx.x * YK_THREADS + threadIdx.x; u < nchunks; u += gridDim.x * YK_THREADS) {
-        const uint32_t p = p0 + u * CW;
-        const uint32_t b = p >> rshift;
-        const OFF d = disp(b);
-        const OFF dp = b > 0 ? disp(b - 1) : 0;
-        const OFF dn = b + 1 < nblk ? disp(b + 1) : OFF_MAX;
-        union {
-            CT w;
-            T e[E];
-        } in;
-        in.w = __ldg(packedc + u);
-        const OFF x0 = d + (OFF) (p & (R - 1));
-        bool own[E];
-        T out[E];
-        if constexpr (E <= 4) {
-            const OFF dn2 = b + 2 < nblk ? disp(b + 2) : OFF_MAX;
-            bool h1[E], h2[E];
-            T c1[E], c2[E];
-#pragma unroll
-            for (int k = 0; k < E; k++) {
-                const OFF x = x0 + (OFF) (k * (int) es);
-                /* an earlier in-range block owns this element */
-                own[k] = !(b > 0 && x < dp + (OFF) R && (b - 1) * R + (uint32_t) (x - dp) >= p0);
-                if (own[k])
-                    out[k] = *(const T *) (typed + x);
-                /* the next two blocks' elements at x, when they exist and are in range (a
-                 * later block places x later in the packed stream still) */
-                h1[k] = false;
-                h2[k] = false;
-                c1[k] = c2[k] = T();
-                if (own[k] && dn <= x) {
-                    const uint64_t q1 = ((uint64_t) (b + 1) << rshift) + (uint64_t) (x - dn);
-                    if (q1 < p1) {
-                        h1[k] = true;
-                        c1[k] = __ldg(packed + ((uint32_t) q1 - p0) / es);
-                        if (dn2 <= x) {
-                            const uint64_t q2 = ((uint64_t) (b + 2) << rshift) + (uint64_t) (x - dn2);
-                            if (q2 < p1) {
-                                h2[k] = true;
-                                c2[k] = __ldg(packed + ((uint32_t) q2 - p0) / es);
-                            }
-                        }
-                    }
-                }
-            }
-#pragma unroll
-            for (int k = 0; k < E; k++) {
-                const OFF x = x0 + (OFF) (k * (int) es);
-                T v = out[k];
-                yk_elem<BT>::op(OP, in.e[k], v);
-                T t = v;
-                yk_elem<BT>::op(OP, c1[k], t);
-                v = h1[k] ? t : v;
-                t = v;
-                yk_elem<BT>::op(OP, c2[k], t);
-                v = h2[k] ? t : v;
-                if (h2[k]) {
-                    /* rare: the blocks after those, in block order */
-                    for (uint32_t bb = b + 3; bb < nblk; bb++) {
-                        const OFF d3 = disp(bb);
-                        if (d3 > x)
-                            break;
-                        const uint64_t pp = ((uint64_t) bb << rshift) + (uint64_t) (x - d3);
-                        if (pp >= p1)
-                            break;
-                        yk_elem<BT>::op(OP, __ldg(packed + ((uint32_t) pp - p0) / es), v);
-                    }
-                }
-                if (own[k])
-                    *(T *) (typed + x) = v;
-            }
-        } else {
-#pragma unroll
-            for (int k = 0; k < E; k++) {
-                const OFF x = x0 + (OFF) (k * (int) es);
-                /* an earlier in-range block owns this element */
-                own[k] = !(b > 0 && x < dp + (OFF) R && (b - 1) * R + (uint32_t) (x - dp) >= p0);
-                if (own[k])
-                    out[k] = *(const T *) (typed + x);
-            }
-#pragma unroll
-            for (int k = 0; k < E; k++) {
-                if (!own[k])
-                    continue;
-                const OFF x = x0 + (OFF) (k * (int) es);
-                yk_elem<BT>::op(OP, in.e[k], out[k]);
-                /* the blocks after this one that start at or before x, in block order */
-                OFF dd = dn;
-                for (uint32_t bb = b + 1; bb < nblk && dd <= x;) {
-                    const uint64_t pp = ((uint64_t) bb << rshift) + (uint64_t) (x - dd);
-                    if (pp >= p1)
-                        break;
-                    yk_elem<BT>::op(OP, __ldg(packed + ((uint32_t) pp - p0) / es), out[k]);
-                    bb++;
-                    dd = bb < nblk ? disp(bb) : OFF_MAX;
-                }
-                *(T *) (typed + x) = out[k];
-            }
-        }
-    }
+    yk_owner_chunk_units<BT, OP, CW, D32>(L, rshift, blockIdx.x * YK_THREADS + threadIdx.x,
+                                          (uint32_t) (L.nbytes / CW), gridDim.x * YK_THREADS);
 }
 
-/* Reductions at L2 for the integer operators whose result does not depend on the order
- * in which contributions arrive: SUM (addition modulo 2^n), MAX, MIN (signed, as the
- * reference's unsigned handles alias the signed types), BAND, BOR and BXOR, on 4- and
- * 8-byte integers.  The value is sent to the L2 with a reduction (red.global.*, the
- * form an atomic whose result is unused compiles to), which reads, combines and writes
- * the target element there. */
-template <int OP, typename T> __device__ __forceinline__ void yk_red(T *p, T v);
-template <int OP> __device__ __forceinline__ void yk_red(int32_t *p, int32_t v)
-{
-    unsigned int *q = (unsigned int *) p;
-    if constexpr (OP == OP_SUM) atomicAdd(q, (unsigned int) v);
-    else if constexpr (OP == OP_MAX) atomicMax((int *) p, (int) v);
-    else if constexpr (OP == OP_MIN) atomicMin((int *) p, (int) v);
-    else if constexpr (OP == OP_BAND) atomicAnd(q, (unsigned int) v);
-    else if constexpr (OP == OP_BOR) atomicOr(q, (unsigned int) v);
-    else atomicXor(q, (unsigned int) v);
-}
-template <int OP> __device__ __forceinline__ void yk_red(int64_t *p, int64_t v)
-{
-    unsigned long long *q = (unsigned long long *) p;
-    if constexpr (OP == OP_SUM) atomicAdd(q, (unsigned long long) v);
-    else if constexpr (OP == OP_MAX) atomicMax((long long *) p, (long long) v);
-    else if constexpr (OP == OP_MIN) atomicMin((long long *) p, (long long) v);
-    else if constexpr (OP == OP_BAND) atomicAnd(q, (unsigned long long) v);
-    else if constexpr (OP == OP_BOR) atomicOr(q, (unsigned long long) v);
-    else atomicXor(q, (unsigned long long) v);
-}
 
-/* Overlapping blocks of R bytes (one IDX level in any block order, or one VEC level
- * whose stride is under its block) under one of those operators:
- * every packed element in the range is folded into its target element by one L2
- * reduction.  The operators are commutative and associative on integers, so the
- * target ends equal to the reference's in-order application (src/backend/seq/
- * genpup.py:119-211 with the operators of :302-327) whatever order the L2 applies the
- * contributions in, and no lane reads the target or resolves which block comes first.
- * Lane k of a warp takes packed element u0 + k, so the lanes of one block reduce into
- * consecutive target elements (one L2 sector request per 32 bytes).  Both sides are
- * aligned to the element size (checked on the host). */
+/* yk_red_units over the whole request, grid-stride */
 template <int BT, int OP, int K, bool D32>
 __global__ void __launch_bounds__(YK_THREADS)
 yk_red_kernel(const __grid_constant__ yk_launch L)
 {
-    typedef typename yk_elem<BT>::T T;
-    constexpr uint32_t es = (uint32_t) sizeof(T);
-    constexpr int U = 4;        /* elements per lane, their loads issued together */
-    const yk_level & lv = L.desc.lv[0];
-    const uint32_t p0 = (uint32_t) L.p0;
-    const uint32_t nunits = (uint32_t) (L.nbytes / es);
-    const T *packed = (const T *) L.packed;     /* element 0 is packed byte p0 */
-    char *typed = L.typed + L.desc.base;
-    const uint32_t nthr = gridDim.x * YK_THREADS;
-    for (uint32_t u0 = blockIdx.x * YK_THREADS + threadIdx.x; u0 < nunits; u0 += U * nthr) {
-        int64_t x[U];
-        T in[U];
-#pragma unroll
-        for (int k = 0; k < U; k++) {
-            const uint32_t u = u0 + k * nthr;
-            if (u < nunits) {
-                const uint32_t p = p0 + u * es;
-                const uint32_t b = yk_div(p, lv);
-                int64_t at;
-                if constexpr (K != YK_LV_IDX)
-                    at = (int64_t) b * lv.stride;
-                else if constexpr (D32)
-                    at = __ldg((const int32_t *) (lv.disp + lv.count) + b);
-                else
-                    at = __ldg(lv.disp + b);
-                x[k] = at + (int64_t) (p - b * (uint32_t) lv.cps);
-                in[k] = __ldg(packed + u);
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < U; k++)
-            if (u0 + k * nthr < nunits)
-                yk_red<OP>((T *) (typed + x[k]), in[k]);
-    }
+    yk_red_units<BT, OP, K, D32>(L, blockIdx.x * YK_THREADS + threadIdx.x,
+                                 (uint32_t) (L.nbytes / sizeof(typename yk_elem<BT>::T)),
+                                 gridDim.x * YK_THREADS);
 }
 
 /* Sorted blocks: descriptor = IDX(nblk, disp sorted ascending, cps = R) over a run of
@@ -1657,608 +634,6 @@ __global__ void yk_ordered_warp_kernel(const __grid_constant__ yk_launch L)
     }
 }
 
-/* ------------------------------------------------------------------------- */
-/* persistent request server                                                 */
-/* ------------------------------------------------------------------------- */
-
-/* Each function processes the units [ub, ue) of one request with the CTA's threads. */
-template <int V, int DIR>
-__device__ __noinline__ void yk_srv_regular(const yk_launch & L, uint64_t ub, uint64_t ue)
-{
-    /* four units per thread, their loads issued together (the launch form's shape) */
-    for (uint32_t t0 = (uint32_t) ub; t0 < (uint32_t) ue; t0 += YK_THREADS)
-        yk_regular_dispatch<V, DIR, 1>(L, t0, (uint32_t) ue);
-}
-
-template <int V, int DIR>
-__device__ __noinline__ void yk_srv_bytes(const yk_launch & L, uint64_t ub, uint64_t ue)
-{
-    for (uint64_t t0 = ub; t0 < ue; t0 += YK_THREADS)
-        yk_bytes_tile<uint64_t, V, DIR, 1>(L, t0, ue);
-}
-
-__device__ __noinline__ void yk_srv_typed(const yk_launch & L, uint64_t ub, uint64_t ue)
-{
-    const uint64_t g = (uint64_t) L.vec;
-    const int op = (int) L.op;
-    for (uint64_t u = ub + threadIdx.x; u < ue; u += YK_THREADS) {
-        int bt;
-        uint64_t inseg;
-        int64_t off = yk_locate<uint64_t>(L.desc, L.p0 + u * g, &bt, &inseg);
-        if (inseg % (uint64_t) yk_bt_size(bt))
-            continue;
-        char *t = L.typed + off;
-        char *p = L.packed + u * g;
-        if (L.dir == 0)
-            yk_apply<false>(bt, op, p, t);
-        else
-            yk_apply<false>(bt, op, t, p);
-    }
-}
-
-__device__ __noinline__ void yk_srv_owner(const yk_launch & L, uint64_t ub, uint64_t ue)
-{
-    const yk_level & lv = L.desc.lv[0];
-    const int bt = L.desc.leaf_type;
-    const uint64_t es = (uint64_t) yk_bt_size(bt), R = lv.cps;
-    const uint64_t p0 = L.p0, p1 = L.p0 + L.nbytes;
-    const int op = (int) L.op;
-    for (uint64_t u = ub + threadIdx.x; u < ue; u += YK_THREADS) {
-        uint64_t p = p0 + u * es;
-        uint64_t b = yk_div(p, lv);
-        uint64_t j = p - b * R;
-        int64_t x = __ldg(lv.disp + b) + (int64_t) j;
-        if (b > 0) {
-            int64_t dprev = __ldg(lv.disp + b - 1);
-            if (x < dprev + (int64_t) R && (b - 1) * R + (uint64_t) (x - dprev) >= p0)
-                continue;
-        }
-        char *t = L.typed + L.desc.base + x;
-        for (uint64_t bb = b; bb < lv.count; bb++) {
-            int64_t db = __ldg(lv.disp + bb);
-            if (db > x)
-                break;
-            uint64_t pp = bb * R + (uint64_t) (x - db);
-            if (pp >= p1)
-                break;
-            yk_apply<false>(bt, op, t, L.packed + (pp - p0));
-        }
-    }
-}
-
-/* sorted blocks with both sides aligned to the element size (the launch form is
- * yk_owner_lane_kernel): elements [ub, ue) of the request, two per thread, every load
- * that does not depend on another issued first; the owner of a target element (its
- * first in-range contributor) folds in the later blocks in block order. */
-template <int BT, int OP>
-__device__ __noinline__ void yk_srv_owner_t(const yk_launch & L, uint64_t ub, uint64_t ue)
-{
-    typedef typename yk_elem<BT>::T T;
-    constexpr uint64_t es = sizeof(T);
-    constexpr int U = 2;
-    constexpr int op = OP;
-    const yk_level & lv = L.desc.lv[0];
-    const uint64_t R = lv.cps, p0 = L.p0, p1 = L.p0 + L.nbytes, nblk = lv.count;
-    const T *packed = (const T *) L.packed;     /* element 0 is packed byte p0 */
-    char *typed = L.typed + L.desc.base;
-    for (uint64_t u0 = ub + threadIdx.x; u0 < ue; u0 += U * YK_THREADS) {
-        int64_t x[U], dn[U];
-        uint64_t b[U];
-        bool own[U], h1[U];
-        T in[U], out[U], in1[U];
-#pragma unroll
-        for (int k = 0; k < U; k++) {
-            const uint64_t u = u0 + (uint64_t) k * YK_THREADS;
-            own[k] = u < ue;
-            h1[k] = false;
-            if (!own[k])
-                continue;
-            const uint64_t p = p0 + u * es;
-            b[k] = yk_div(p, lv);
-            const int64_t d = __ldg(lv.disp + b[k]);
-            const int64_t dp = b[k] > 0 ? __ldg(lv.disp + b[k] - 1) : 0;
-            dn[k] = b[k] + 1 < nblk ? __ldg(lv.disp + b[k] + 1) : INT64_MAX;
-            in[k] = __ldg(packed + u);
-            x[k] = d + (int64_t) (p - b[k] * R);
-            /* an earlier in-range block owns this element */
-            if (b[k] > 0 && x[k] < dp + (int64_t) R && (b[k] - 1) * R + (uint64_t) (x[k] - dp) >= p0)
-                own[k] = false;
-        }
-#pragma unroll
-        for (int k = 0; k < U; k++) {
-            if (!own[k])
-                continue;
-            out[k] = *(const T *) (typed + x[k]);
-            if (dn[k] <= x[k]) {
-                const uint64_t pp = (b[k] + 1) * R + (uint64_t) (x[k] - dn[k]);
-                if (pp < p1) {
-                    h1[k] = true;
-                    in1[k] = __ldg(packed + (pp - p0) / es);
-                }
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < U; k++) {
-            if (!own[k])
-                continue;
-            yk_elem<BT>::op(op, in[k], out[k]);
-            if (h1[k]) {
-                yk_elem<BT>::op(op, in1[k], out[k]);
-                /* rarer: the blocks after that, in block order */
-                for (uint64_t bb = b[k] + 2; bb < nblk; bb++) {
-                    const int64_t d2 = __ldg(lv.disp + bb);
-                    if (d2 > x[k])
-                        break;
-                    const uint64_t pp = bb * R + (uint64_t) (x[k] - d2);
-                    if (pp >= p1)
-                        break;  /* later blocks place x later still */
-                    yk_elem<BT>::op(op, __ldg(packed + (pp - p0) / es), out[k]);
-                }
-            }
-            *(T *) (typed + x[k]) = out[k];
-        }
-    }
-}
-
-/* a compile-time instance for complex-float PROD (600 against 510 GB/s on bursts of
- * 16 MiB requests); every other aligned sorted-block request takes the generic item,
- * double SUM included (its instance measured 579 against 624 GB/s at this kernel's
- * register bound) */
-__device__ __noinline__ void yk_srv_owner_typed(const yk_launch & L, uint64_t ub, uint64_t ue)
-{
-    if (L.desc.leaf_type == YK_BT_C32 && (int) L.op == OP_PROD)
-        yk_srv_owner_t<YK_BT_C32, OP_PROD>(L, ub, ue);
-    else
-        yk_srv_owner(L, ub, ue);
-}
-
-/* struct-like packs (the launch form is yk_runs_pack_warp_kernel): elements [ib, ie) of
- * the request, ib a multiple of 32 (the host cuts these items in whole 32-element
- * groups), each warp staging a group's runs in shared memory and writing its packed
- * bytes as 16-byte chunks */
-static __shared__ __align__(16) unsigned char yk_srv_stage[YK_THREADS / 32][32 * 48];
-
-template <int NV>
-__device__ __noinline__ void yk_srv_runs(const yk_launch & L, uint64_t ib, uint64_t ie)
-{
-    const uint32_t R = (uint32_t) L.desc.run;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int64_t E = L.desc.lv[0].stride;
-    const uint32_t e0 = (uint32_t) (L.p0 / R), nw4 = R / 4;
-    const char *tb = L.typed + L.desc.base;
-    unsigned char *st = yk_srv_stage[w];
-    for (uint64_t i0 = ib + (uint64_t) w * 32; i0 < ie; i0 += (YK_THREADS / 32) * 32) {
-        const uint64_t i = i0 + (uint64_t) lane;
-        const uint32_t n = (uint32_t) min((uint64_t) 32, ie - i0);
-        if (i < ie) {
-            const char *src = tb + (int64_t) (e0 + i) * E;
-            union {
-                uint4 w[NV];
-                uint32_t u[4 * NV];
-            } v;
-#pragma unroll
-            for (int k = 0; k < NV; k++)
-                v.w[k] = yk_ldcg((const uint4 *) (src + 16 * k));
-            uint32_t *sw = (uint32_t *) (st + (uint32_t) lane * R);
-#pragma unroll
-            for (int j = 0; j < 4 * NV; j++)
-                if ((uint32_t) j < nw4)
-                    sw[j] = v.u[j];
-        }
-        __syncwarp();
-        char *dst = L.packed + i0 * R;
-        const uint32_t nbytes = n * R, nch = nbytes / 16;
-        for (uint32_t c = (uint32_t) lane; c < nch; c += 32)
-            *(uint4 *) (dst + 16 * c) = *(const uint4 *) (st + 16 * c);
-        for (uint32_t q = nch * 16 + (uint32_t) lane * 4; q < nbytes; q += 128)
-            *(uint32_t *) (dst + q) = *(const uint32_t *) (st + q);
-        __syncwarp();
-    }
-}
-
-/* overlapping equal blocks under an order-independent integer operator (the launch
- * form is yk_red_kernel): elements [ub, ue) of the request, each folded into its target
- * by one L2 reduction */
-template <int BT, int OP>
-__device__ __noinline__ void yk_srv_red_t(const yk_launch & L, uint64_t ub, uint64_t ue)
-{
-    typedef typename yk_elem<BT>::T T;
-    const yk_level & lv = L.desc.lv[0];
-    const uint64_t es = sizeof(T), p0 = L.p0;
-    char *typed = L.typed + L.desc.base;
-    constexpr int U = 4;        /* elements per thread, their loads issued together */
-    for (uint64_t u0 = ub + threadIdx.x; u0 < ue; u0 += U * YK_THREADS) {
-        int64_t x[U];
-        T v[U];
-#pragma unroll
-        for (int k = 0; k < U; k++) {
-            const uint64_t u = u0 + (uint64_t) k * YK_THREADS;
-            if (u < ue) {
-                const uint64_t p = p0 + u * es;
-                const uint64_t b = yk_div(p, lv);
-                const int64_t at = lv.kind == YK_LV_IDX ? __ldg(lv.disp + b) : (int64_t) b * lv.stride;
-                x[k] = at + (int64_t) (p - b * lv.cps);
-                v[k] = *(const T *) (L.packed + (p - p0));
-            }
-        }
-#pragma unroll
-        for (int k = 0; k < U; k++)
-            if (u0 + (uint64_t) k * YK_THREADS < ue)
-                yk_red<OP>((T *) (typed + x[k]), v[k]);
-    }
-}
-
-template <int BT>
-__device__ __forceinline__ void yk_srv_red_bt(const yk_launch & L, uint64_t ub, uint64_t ue)
-{
-    switch ((int) L.op) {
-        case OP_MAX: yk_srv_red_t<BT, OP_MAX>(L, ub, ue); break;
-        case OP_MIN: yk_srv_red_t<BT, OP_MIN>(L, ub, ue); break;
-        case OP_SUM: yk_srv_red_t<BT, OP_SUM>(L, ub, ue); break;
-        case OP_BAND: yk_srv_red_t<BT, OP_BAND>(L, ub, ue); break;
-        case OP_BOR: yk_srv_red_t<BT, OP_BOR>(L, ub, ue); break;
-        case OP_BXOR: yk_srv_red_t<BT, OP_BXOR>(L, ub, ue); break;
-    }
-}
-
-__device__ __noinline__ void yk_srv_red(const yk_launch & L, uint64_t ub, uint64_t ue)
-{
-    if (L.desc.leaf_type == YK_BT_I32)
-        yk_srv_red_bt<YK_BT_I32>(L, ub, ue);
-    else if (L.desc.leaf_type == YK_BT_I64)
-        yk_srv_red_bt<YK_BT_I64>(L, ub, ue);
-}
-
-/* the whole request, in order, by warp 0 (targets that overlap arbitrarily) */
-__device__ __noinline__ void yk_srv_ordered(const yk_launch & L, uint64_t ub, uint64_t ue)
-{
-    if (threadIdx.x >= 32)
-        return;
-    const int lane = threadIdx.x;
-    const uint64_t g = (uint64_t) L.vec;
-    for (uint64_t c0 = ub; c0 < ue; c0 += 32) {
-        uint64_t u = c0 + (uint64_t) lane;
-        bool active = u < ue;
-        int bt = YK_BT_NONE;
-        uint64_t inseg = 0;
-        int64_t off = 0;
-        int len = 0;
-        if (active) {
-            off = yk_locate<uint64_t>(L.desc, L.p0 + u * g, &bt, &inseg);
-            if (L.typed_op) {
-                int es = yk_bt_size(bt);
-                if (inseg % (uint64_t) es)
-                    active = false;
-                else
-                    len = es;
-            } else {
-                len = (int) g;
-            }
-        }
-        bool conflict = false;
-        for (int k = 0; k < 31; k++) {
-            int64_t ooff = __shfl_sync(0xffffffffu, off, k);
-            int olen = __shfl_sync(0xffffffffu, active ? len : 0, k);
-            if (k < lane && active && olen && off < ooff + olen && ooff < off + len)
-                conflict = true;
-        }
-        bool serial = __any_sync(0xffffffffu, conflict);
-        for (int k = 0; k < 32; k++) {
-            if ((!serial || k == lane) && active) {
-                char *t = L.typed + off;
-                char *p = L.packed + u * g;
-                if (L.typed_op)
-                    yk_apply<false>(bt, (int) L.op, t, p);
-                else
-                    for (int i = 0; i < len; i++)
-                        t[i] = p[i];
-            }
-            __syncwarp();
-            if (!serial)
-                break;
-        }
-    }
-}
-
-/* contiguous-block hindexed over the packed range [pb, pe): the CTA's warps split the
- * overlapping block groups (see yk_hidx_kernel) */
-template <int V, int DIR>
-__device__ __noinline__ void yk_srv_hidx(const yk_launch & L, uint64_t pb, uint64_t pe)
-{
-    typedef typename yk_vec<V>::T VT;
-    const yk_level *lv = &L.desc.lv[0];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    char *typed = L.typed + L.desc.base;
-    VT *packed = (VT *) L.packed;
-    const uint64_t jb = yk_hidx_block(lv, pb), je = yk_hidx_block(lv, pe - 1);
-    const uint64_t ngroups = (je - jb + 32) / 32;
-    for (uint64_t gi = (uint64_t) w; gi < ngroups; gi += YK_THREADS / 32) {
-        const uint64_t j0 = jb + gi * 32, jl = j0 + (uint64_t) lane;
-        const uint64_t my_pfx = jl <= je ? __ldg(lv->pfx + jl) : ~(uint64_t) 0;
-        const int64_t my_disp = jl <= je ? __ldg(lv->disp + jl) : 0;
-        uint64_t start = max(__shfl_sync(0xffffffffu, my_pfx, 0), pb);
-        uint64_t end = min(__ldg(lv->pfx + min(j0 + 32, je + 1)), pe);
-        for (uint64_t base = start; base < end; base += (uint64_t) 32 * V) {
-            const uint64_t p = base + (uint64_t) lane * V;
-            int idx = 0;
-#pragma unroll
-            for (int step = 16; step > 0; step >>= 1) {
-                uint64_t c = __shfl_sync(0xffffffffu, my_pfx, idx + step);
-                if (c <= p)
-                    idx += step;
-            }
-            const uint64_t bp = __shfl_sync(0xffffffffu, my_pfx, idx);
-            const int64_t bd = __shfl_sync(0xffffffffu, my_disp, idx);
-            if (p < end) {
-                char *t = typed + bd + (int64_t) (p - bp);
-                VT *q = packed + (p - L.p0) / V;
-                if (DIR == 0)
-                    *q = yk_ldcg((const VT *) t);
-                else
-                    *(VT *) t = yk_ldcg((const VT *) q);
-            }
-        }
-    }
-}
-
-__device__ __forceinline__ uint64_t yk_ld_acquire_sys(const volatile uint64_t * p)
-{
-    uint64_t v;
-    asm volatile ("ld.acquire.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-
-/* host-written queue data is read at system scope: never from a stale cached copy */
-__device__ __forceinline__ uint64_t yk_ld_sys(const void *p)
-{
-    uint64_t v;
-    asm volatile ("ld.relaxed.sys.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
-    return v;
-}
-
-/* An item of request slot `slot` is finished: count it into the request's completion
- * word; the CTA that finishes the request's last item appends slot + 1 to the completion
- * queue, so the host learns of completions without scanning every request in flight.
- * The item's bytes are made visible to the host first. */
-__device__ __forceinline__ unsigned long long yk_globaltimer(void)
-{
-    unsigned long long t;
-    asm volatile ("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-__device__ __forceinline__ void yk_srv_item_done(const yk_server_args & A, uint32_t slot)
-{
-    __threadfence_system();
-    const unsigned long long old = atomicAdd_system(&A.req_done[slot], 1ull);
-    if (old + 1 == yk_ld_sys(A.req_nitems + slot)) {
-        const unsigned long long pos = atomicAdd(A.cq_tail, 1ull);
-        asm volatile ("st.release.sys.global.u64 [%0], %1;"
-                      :: "l"(A.cq + pos % A.qr), "l"((unsigned long long) slot + 1ull) : "memory");
-    }
-}
-
-/* a record the GPU can act on: a known kind, a sane unit and an ordered range */
-__device__ __forceinline__ bool yk_item_ok(const yk_item & it, const yk_launch & L)
-{
-    if ((it.kind & ~YK_SRV_TIMED) > YK_SRV_LAST || it.pe <= it.pb || it.pb < L.p0 ||
-        it.pe > L.p0 + L.nbytes)
-        return false;
-    if (L.vec != 1 && L.vec != 2 && L.vec != 4 && L.vec != 8 && L.vec != 16)
-        return false;
-    return L.dir == 0 || L.dir == 1;
-}
-
-/* Resident CTAs claim work items one at a time (a compare-and-swap on a lane's counter
- * that never runs past the published count), stage the item's request record in shared
- * memory, process the item, and publish its completion.  A CTA tries its home lane
- * first, then the others in turn.  Every wait is bounded: a CTA that finds no new item
- * for idle_us microseconds of the GPU's global timer (or max_idle_spins polls), or sees
- * the stop flag, leaves; the host relaunches the kernel when items are pending and no
- * CTA is resident. */
-/* The item functions above are out of line (__noinline__): each gets the kernel's
- * register budget to itself, so the loops of one item kind do not spill for the
- * registers another kind needs (inlined, the kernel spilled up to 3 KB).  That lets the
- * kernel run at 32 registers, eight resident CTAs per SM like the launch kernels: on the
- * mixed request stream 817 GB/s of capacity against 702-769 at six. */
-__global__ void __launch_bounds__(YK_THREADS, 8)
-yk_server_kernel(const __grid_constant__ yk_server_args A)
-{
-    __shared__ yk_launch sL;
-    __shared__ uint64_t s_item;
-    __shared__ int s_cmd;
-    __shared__ yk_item s_it;
-    uint64_t pub = 0;           /* thread 0: last published count read from the host */
-    for (;;) {
-        if (threadIdx.x == 0) {
-            int cmd = 0;
-            /* idle polls of the host-mapped counter back off from 64 ns to 2 us: many
-             * resident CTAs polling at full rate would load the C2C link the host's own
-             * submissions cross */
-            unsigned nap = 64;
-            const unsigned long long idle_t0 = yk_globaltimer();
-            for (uint32_t spins = 0;; spins++) {
-                if (*A.stop) {
-                    cmd = 2;
-                    break;
-                }
-                /* the published count only grows: re-read it from host memory only when
-                 * every lane has caught up with the copy held here */
-                bool pending = false;
-                for (int pass = 0; pass < 2 && !pending; pass++) {
-                    if (pass == 1)
-                        pub = yk_ld_acquire_sys(A.items_published);
-                    for (uint32_t i = 0; i < YK_SRV_LANES && cmd == 0; i++) {
-                        const uint32_t lane = (blockIdx.x + i) % YK_SRV_LANES;
-                        unsigned long long *ctr = A.next_item + lane * YK_SRV_LANE_STRIDE;
-                        const unsigned long long c = *(volatile unsigned long long *) ctr;
-                        const unsigned long long t = c * YK_SRV_LANES + lane;
-                        if (t >= pub)
-                            continue;
-                        pending = true;
-                        if (atomicCAS(ctr, c, c + 1) == c) {
-                            s_item = t;
-                            cmd = 1;
-                        }
-                    }
-                }
-                if (cmd == 1)
-                    break;
-                if (pending) {
-                    if (spins >= 64u * A.max_idle_spins) {
-                        cmd = 3;        /* hard bound: leave; the host relaunches */
-                        break;
-                    }
-                    continue;
-                }
-                if (spins >= A.max_idle_spins ||
-                    yk_globaltimer() - idle_t0 >= 1000ull * A.idle_us) {
-                    cmd = 3;
-                    break;
-                }
-                __nanosleep(nap);
-                nap = nap < 2048 ? 2 * nap : 2048;
-            }
-            if (cmd == 1) {
-                /* the item carries its own sequence number: re-read (bounded) until the
-                 * host's write is the one seen */
-                const yk_item *src = &A.items[s_item % A.qi];
-                uint64_t w[4];
-                uint32_t tries = 0;
-                do {
-                    for (int i = 0; i < 4; i++)
-                        w[i] = yk_ld_sys((const uint64_t *) src + i);
-                } while (w[0] != s_item && ++tries < 1000);
-                if (w[0] != s_item)
-                    cmd = 4;
-                uint64_t *dst = (uint64_t *) &s_it;
-                for (int i = 0; i < 4; i++)
-                    dst[i] = w[i];
-            }
-            s_cmd = cmd;
-        }
-        __syncthreads();
-        int cmd = s_cmd;
-        if (cmd == 2 || cmd == 3) {
-            if (threadIdx.x == 0)
-                atomicAdd((unsigned int *) &A.status[cmd == 2 ? 1 : 0], 1u);
-            return;
-        }
-        if (cmd == 1) {
-            /* request record -> shared memory (8-byte words, system-scope loads) */
-            const uint64_t *src = (const uint64_t *) (A.reqs + (s_it.req % A.qr));
-            uint64_t *dst = (uint64_t *) &sL;
-            for (uint32_t i = threadIdx.x; i < sizeof(yk_launch) / 8; i += YK_THREADS)
-                dst[i] = yk_ld_sys(src + i);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0 && cmd == 1 && !yk_item_ok(s_it, sL))
-            s_cmd = 4;
-        __syncthreads();
-        cmd = s_cmd;
-        if (cmd == 4) {
-            /* unusable item: count it, mark it done, move on (never loop on it) */
-            if (threadIdx.x == 0) {
-                atomicAdd((unsigned int *) &A.status[2], 1u);
-                /* counted for its request only when the item record itself was current;
-                 * otherwise the request stays incomplete and the host's bounded wait
-                 * reports the error */
-                if (s_it.seq == s_item)
-                    yk_srv_item_done(A, s_it.req % A.qr);
-            }
-            __syncthreads();
-            continue;
-        }
-        const yk_item it = s_it;
-        const bool timed = (it.kind & YK_SRV_TIMED) != 0;
-        const unsigned long long tb = timed && threadIdx.x == 0 ? yk_globaltimer() : 0ull;
-        const uint64_t g = (uint64_t) sL.vec;
-        const uint64_t ub = (it.pb - sL.p0) / g, ue = (it.pe - sL.p0) / g;
-        switch (it.kind & ~YK_SRV_TIMED) {
-            case YK_SRV_REGULAR:
-#define YK_SV(V) do { if (sL.dir == 0) yk_srv_regular<V, 0>(sL, ub, ue); \
-                      else yk_srv_regular<V, 1>(sL, ub, ue); } while (0)
-                switch (sL.vec) {
-                    case 16: YK_SV(16); break;
-                    case 8: YK_SV(8); break;
-                    case 4: YK_SV(4); break;
-                    case 2: YK_SV(2); break;
-                    default: YK_SV(1); break;
-                }
-#undef YK_SV
-                break;
-            case YK_SRV_BYTES:
-#define YK_SB(V) do { if (sL.dir == 0) yk_srv_bytes<V, 0>(sL, ub, ue); \
-                      else yk_srv_bytes<V, 1>(sL, ub, ue); } while (0)
-                switch (sL.vec) {
-                    case 16: YK_SB(16); break;
-                    case 8: YK_SB(8); break;
-                    case 4: YK_SB(4); break;
-                    case 2: YK_SB(2); break;
-                    default: YK_SB(1); break;
-                }
-#undef YK_SB
-                break;
-            case YK_SRV_TYPED:
-                yk_srv_typed(sL, ub, ue);
-                break;
-            case YK_SRV_OWNER:
-                yk_srv_owner(sL, (it.pb - sL.p0) / (uint64_t) yk_bt_size(sL.desc.leaf_type),
-                             (it.pe - sL.p0) / (uint64_t) yk_bt_size(sL.desc.leaf_type));
-                break;
-            case YK_SRV_ORDERED:
-                yk_srv_ordered(sL, ub, ue);
-                break;
-            case YK_SRV_RED:
-                yk_srv_red(sL, (it.pb - sL.p0) / (uint64_t) yk_bt_size(sL.desc.leaf_type),
-                           (it.pe - sL.p0) / (uint64_t) yk_bt_size(sL.desc.leaf_type));
-                break;
-            case YK_SRV_RUNS:
-                if (sL.desc.run <= 32)
-                    yk_srv_runs<2>(sL, (it.pb - sL.p0) / sL.desc.run, (it.pe - sL.p0) / sL.desc.run);
-                else
-                    yk_srv_runs<3>(sL, (it.pb - sL.p0) / sL.desc.run, (it.pe - sL.p0) / sL.desc.run);
-                break;
-            case YK_SRV_OWNER_T:
-                yk_srv_owner_typed(sL, (it.pb - sL.p0) / (uint64_t) yk_bt_size(sL.desc.leaf_type),
-                                   (it.pe - sL.p0) / (uint64_t) yk_bt_size(sL.desc.leaf_type));
-                break;
-            default:
-#define YK_SH(V) do { if (sL.dir == 0) yk_srv_hidx<V, 0>(sL, it.pb, it.pe); \
-                      else yk_srv_hidx<V, 1>(sL, it.pb, it.pe); } while (0)
-                switch (sL.vec) {
-                    case 16: YK_SH(16); break;
-                    case 8: YK_SH(8); break;
-                    case 4: YK_SH(4); break;
-                    case 2: YK_SH(2); break;
-                    default: YK_SH(1); break;
-                }
-#undef YK_SH
-                break;
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            if (timed)
-                atomicAdd_system(A.req_busy + it.req % A.qr, yk_globaltimer() - tb);
-            yk_srv_item_done(A, it.req % A.qr);   /* the item's bytes first, then its count */
-        }
-    }
-}
-
-extern "C" int yk_cuda_server_ctas(void)
-{
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, yk_server_kernel, YK_THREADS, 0);
-    if (per_sm < 1)
-        per_sm = 1;
-    return per_sm * yk_cuda_num_sms();
-}
-
-extern "C" int yk_cuda_server_launch(const yk_server_args * a, int ctas, void *stream)
-{
-    yk_server_kernel<<<ctas, YK_THREADS, 0, (cudaStream_t) stream>>>(*a);
-    return (int) cudaGetLastError();
-}
 
 /* ------------------------------------------------------------------------- */
 /* host-side launchers                                                       */
@@ -2555,9 +930,22 @@ static bool yk_owner_lane_cplx(const yk_launch & c, int rshift, cudaStream_t s, 
     return false;
 }
 
-static bool yk_owner_lane_launch(const yk_launch & c, int bt, int rshift, cudaStream_t s, int cap,
-                                 bool d32)
+/* which of yk_owner_lane_kernel / yk_owner_chunk_kernel serves a launch, and how (the
+ * YK_FORM_* fields of yk_desc.h); the server plans its sorted-block items with it too */
+extern "C" int yk_cuda_owner_form(const yk_launch * l, int sorted_blocks)
 {
+    const yk_launch & c = *l;
+    const int bt = c.desc.leaf_type;
+    if ((sorted_blocks & 3) != 2 || c.use64 ||
+        !(bt == YK_BT_I8 || bt == YK_BT_I16 || bt == YK_BT_I32 || bt == YK_BT_I64 ||
+          bt == YK_BT_F32 || bt == YK_BT_F64 || bt == YK_BT_C32 || bt == YK_BT_C64))
+        return 0;
+    const uint64_t R = c.desc.lv[0].cps;
+    int rshift = 0;
+    while (rshift < 31 && (1ull << rshift) < R)
+        rshift++;
+    if ((1ull << rshift) != R)
+        return 0;
     const uint64_t es = (uint64_t) yk_bt_size(bt);
     /* chunks of CW bytes: blocks a multiple of CW bytes, range and packed pointer on CW
      * bytes.  16-byte chunks for 4- and 8-byte elements (within the register budget of
@@ -2573,6 +961,17 @@ static bool yk_owner_lane_launch(const yk_launch & c, int bt, int rshift, cudaSt
                 (uintptr_t) c.packed % cw == 0)
                 chunk = cw;
     }
+    const bool d32 = (sorted_blocks & YK_ORD_D32) != 0 && c.desc.lv[0].has_d32;
+    return rshift | (chunk << 8) | (d32 ? YK_FORM_D32 : 0) | YK_FORM_POW2;
+}
+
+/* the kernel of a form from yk_cuda_owner_form; false when the (type, operator) pair has
+ * no instance */
+static bool yk_owner_lane_launch(const yk_launch & c, int bt, int form, cudaStream_t s, int cap)
+{
+    const uint64_t es = (uint64_t) yk_bt_size(bt);
+    const int rshift = form & 255, chunk = (form >> 8) & 255;
+    const bool d32 = (form & YK_FORM_D32) != 0;
     const uint64_t units = c.nbytes / (chunk ? (uint64_t) chunk : es);
     const unsigned g = yk_grid(units, YK_THREADS, cap > 0 ? cap : 16);
     switch (bt) {
@@ -2661,17 +1060,12 @@ extern "C" int yk_cuda_launch_unpack_ordered(const yk_launch * l, int sorted_blo
         yk_red_count.fetch_add(1, std::memory_order_relaxed);
         return (int) cudaGetLastError();
     }
-    const bool d32 = (sorted_blocks & YK_ORD_D32) != 0 && l->desc.lv[0].has_d32;
+    const int form = yk_cuda_owner_form(l, sorted_blocks);
     sorted_blocks &= 3;
     bool typed_ok = sorted_blocks == 2 && (bt == YK_BT_I8 || bt == YK_BT_I16 || bt == YK_BT_I32 ||
                                            bt == YK_BT_I64 || bt == YK_BT_F32 || bt == YK_BT_F64 ||
                                            bt == YK_BT_C32 || bt == YK_BT_C64);
-    const uint64_t R = c.desc.lv[0].cps;
-    int rshift = 0;
-    while (rshift < 31 && (1ull << rshift) < R)
-        rshift++;
-    if (typed_ok && !c.use64 && (1ull << rshift) == R &&
-        yk_owner_lane_launch(c, bt, rshift, s, ctas_per_sm, d32)) {
+    if (form && yk_owner_lane_launch(c, bt, form, s, ctas_per_sm)) {
         /* launched: power-of-two blocks, operator in the type's table */
     } else if (typed_ok) {
         uint64_t units = c.nbytes / (uint64_t) yk_bt_size(bt);
