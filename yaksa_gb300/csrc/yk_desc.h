@@ -3,7 +3,7 @@
  * interface between the C host library and the CUDA kernels.
  *
  * Plain C (no CUDA types), shared by the host code (yk_*.c) and the kernels
- * (yk_kernels.cu).
+ * (yk_kernels.cu, yk_server.cu, yk_device.cuh).
  *
  * A committed type is flattened into a chain of levels, outermost first, ending in a
  * leaf.  A packed byte position p (relative to the start of the packed form of
