@@ -27,7 +27,7 @@ mirror), an operator 3 (read packed, read target, write target).
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
                     [--no-cpu] [--no-stream] [--no-suite] [--cpu-seconds S]
     python bench.py --suite out.jsonl [--suite-only hindexed,struct,...] [--suite-scale K]
-    python bench.py --stream out.json [--stream-requests R]
+    python bench.py --stream out.json [--stream-requests R] [--stream-families halo,struct,...]
 """
 import argparse
 import ctypes
@@ -577,7 +577,8 @@ def dev_fill(torch, base, nbytes, gen):
     return out
 
 
-def run_stream(nreq=10000, rate=50e3, seed=5, check=True, log=None, floor=True, server_tune=True):
+def run_stream(nreq=10000, rate=50e3, seed=5, check=True, log=None, floor=True, server_tune=True,
+               families=None):
     """10,000 pack/unpack requests with Poisson arrivals at `rate` req/s: families drawn
     uniformly from hvector/halo/hindexed/struct/reduce, packed sizes log-uniform over
     19 power-of-two classes 256 B .. 64 MiB, 20% with the packed buffer in pinned host
@@ -586,7 +587,8 @@ def run_stream(nreq=10000, rate=50e3, seed=5, check=True, log=None, floor=True, 
     buffers and are compared with the oracle after each path: 120 small ones and, for
     every size class, at least one whose typed footprint is at most 256 MiB (the halo
     family's footprint is 256 times its packed size, so its largest classes are checked
-    through the other families).  Returns a dict."""
+    through the other families).  `families` draws from a subset instead (the x-face
+    floor is measured only with halo among them).  Returns a dict."""
     import numpy as np
     import torch
     import yaksa_gb300 as yk
@@ -595,7 +597,7 @@ def run_stream(nreq=10000, rate=50e3, seed=5, check=True, log=None, floor=True, 
     y = yk.Yaksa()
     y.init()
     specs = stream_family_types(yk, np, seed)
-    fams = ["hvector", "halo", "hindexed", "struct", "reduce"]
+    fams = list(families) if families else ["hvector", "halo", "hindexed", "struct", "reduce"]
     rng = np.random.default_rng(seed + 1)
     gen = torch.Generator(device="cuda").manual_seed(seed)
     fam_of = rng.integers(0, len(fams), nreq)
@@ -754,7 +756,7 @@ def run_stream(nreq=10000, rate=50e3, seed=5, check=True, log=None, floor=True, 
     res["server_over_plain"] = {
         "closed_loop_throughput": res["server"]["closed_loop"]["GBps"] / res["plain"]["closed_loop"]["GBps"],
         "open_loop_p99": res["server"]["open_loop"]["p99_us"] / res["plain"]["open_loop"]["p99_us"]}
-    if floor:
+    if floor and "halo" in fams:
         res["xface_floor"] = stream_xface_floor(torch, np, y, yk, keys, dir_of, specs, typed, total,
                                                 res["plain"]["closed_loop"]["GBps"])
     for k in used:
@@ -1182,6 +1184,8 @@ def main():
     ap.add_argument("--stream", default=None,
                     help="run only the mixed request stream (plain vs server) and write its JSON")
     ap.add_argument("--stream-requests", type=int, default=10000)
+    ap.add_argument("--stream-families", default=None,
+                    help="comma-separated subset of hvector,halo,hindexed,struct,reduce for --stream")
     ap.add_argument("--no-stream", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
@@ -1198,7 +1202,8 @@ def main():
     if args.stream:
         import torch
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        r = run_stream(nreq=args.stream_requests, log=sys.stderr)
+        r = run_stream(nreq=args.stream_requests, log=sys.stderr,
+                       families=args.stream_families.split(",") if args.stream_families else None)
         with open(args.stream, "w") as f:
             f.write(json.dumps(r) + "\n")
         print(json.dumps(r))

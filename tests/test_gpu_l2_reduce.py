@@ -90,6 +90,28 @@ def test_red_block_lengths(cuda, prod, oracle, bl, op):
     assert used == 1
 
 
+@pytest.mark.parametrize("op", [yk.OP_SUM, yk.OP_MAX, yk.OP_BXOR])
+@pytest.mark.parametrize("where", ["fits", "offset_over", "table_over", "negative"])
+def test_red_offsets_at_32_bits(cuda, prod, oracle, op, where):
+    """Overlapping int32 blocks of 8 (32 bytes) at byte displacements around 2^31 in
+    random order: every target offset in 32 bits (the form with a shift and 32-bit
+    offsets); a table that fits in 32 bits with one block reaching past 2^31 - 1 (the
+    32-bit table with 64-bit offsets); one displacement of 2^31 (the 64-bit table); and
+    displacements from -2^31 up.  The typed buffer spans only the blocks: its pointer is
+    offset by the lowest displacement."""
+    rng = np.random.default_rng(op * 13 + len(where))
+    start = -(1 << 31) if where == "negative" else (1 << 31) - 64 - 4096
+    offs = (start + rng.integers(0, 1024, 3000) * 4).tolist()
+    if where == "offset_over":
+        offs.append((1 << 31) - 16)     # its last element ends at 2^31 + 15
+    elif where == "table_over":
+        offs.append(1 << 31)
+    rng.shuffle(offs)
+    used = unpack_case(cuda, prod, oracle, "type_create_hindexed_block", (8, offs),
+                       yk.TYPE_INT32_T, 4, op, seed=op)
+    assert used == 1
+
+
 @pytest.mark.parametrize("op", [yk.OP_SUM, yk.OP_MIN, yk.OP_BOR])
 def test_red_segments(cuda, prod, oracle, op):
     """The packed range cut into 9 segments at element (not block) boundaries: each

@@ -568,6 +568,17 @@ static int idx_fits32(const hlev * h)
     return 1;
 }
 
+/* every displacement plus cps - 1 in int32 (idx_fits32 holds) */
+static int idx_offsets_fit32(const hlev * h)
+{
+    if (h->cps == 0 || h->cps > (uint64_t) INT32_MAX)
+        return 0;
+    for (uint64_t j = 0; j < h->count; j++)
+        if (h->disp[j] > (int64_t) INT32_MAX - (int64_t) (h->cps - 1))
+            return 0;
+    return 1;
+}
+
 static int upload(hbuild * b, yk_devdesc * dd, int to_device)
 {
     /* table sizes */
@@ -619,7 +630,7 @@ static int upload(hbuild * b, yk_devdesc * dd, int to_device)
             int32_t *d32 = (int32_t *) (host + pos);
             for (uint64_t j = 0; j < h->count; j++)
                 d32[j] = (int32_t) h->disp[j];
-            l->has_d32 = 1;
+            l->has_d32 = YK_D32_TABLE | (idx_offsets_fit32(h) ? YK_D32_OFFSETS : 0);
             pos += (h->count * sizeof(int32_t) + 7) & ~(size_t) 7;
         }
         if (h->pfx) {

@@ -59,9 +59,11 @@ enum {
 
 typedef struct {
     int32_t kind;
-    int32_t has_d32;            /* IDX: an int32_t copy of disp[] follows it, at
-                                 * (const int32_t *) (disp + count) (every displacement
-                                 * fits in 32 bits) */
+    int32_t has_d32;            /* IDX, bit YK_D32_TABLE: an int32_t copy of disp[]
+                                 * follows it, at (const int32_t *) (disp + count)
+                                 * (every displacement fits in 32 bits); bit
+                                 * YK_D32_OFFSETS: every displacement plus cps - 1 fits
+                                 * too (the offsets inside blocks of cps bytes) */
     uint64_t count;
     int64_t stride;             /* VEC: byte stride; HIDX: child extent */
     uint64_t cps;               /* packed bytes per digit (child packed size) */
@@ -75,6 +77,10 @@ typedef struct {
     uint32_t tshift;
     uint32_t pad2;
 } yk_level;
+
+/* yk_level.has_d32 bits */
+#define YK_D32_TABLE 1
+#define YK_D32_OFFSETS 2
 
 typedef struct {
     int32_t nlev;

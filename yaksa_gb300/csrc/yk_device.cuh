@@ -751,40 +751,60 @@ __device__ __forceinline__ void yk_hidx32_groups(const yk_launch & L, uint64_t p
  * sector request per 32 bytes).  Both sides are aligned to the element size (checked
  * on the host).  K: the level's kind (IDX or VEC); D32: the IDX level's 32-bit copy of
  * its displacements. */
-template <int BT, int OP, int K, bool D32, int U = 4>
+/* yk_red_units' P2X form applies: an IDX level with its 32-bit table, every target
+ * offset in 32 bits and blocks of a power-of-two length */
+__host__ __device__ inline bool yk_red_p2x(const yk_level & lv)
+{
+    return lv.kind == YK_LV_IDX && (lv.has_d32 & YK_D32_TABLE) && (lv.has_d32 & YK_D32_OFFSETS) &&
+        lv.cps && (lv.cps & (lv.cps - 1)) == 0;
+}
+
+template <int BT, int OP, int K, bool D32, int U = 4, bool P2X = false>
 __device__ __forceinline__ void yk_red_units(const yk_launch & L, uint32_t u0, uint32_t nunits,
                                              uint32_t nthr)
 {
     typedef typename yk_elem<BT>::T T;
     constexpr uint32_t es = (uint32_t) sizeof(T);
+    /* P2X (an IDX level read through its 32-bit table): blocks of a power-of-two length
+     * and every target offset in 32 bits (YK_D32_OFFSETS), so a lane keeps a shift
+     * instead of the division and 32-bit offsets.  Fewer live values matter where the
+     * record is not a kernel parameter (the server's items keep every invariant in
+     * thread registers). */
+    typedef typename std::conditional<P2X, int32_t, int64_t>::type OFF;
     const yk_level & lv = L.desc.lv[0];
     const uint32_t p0 = (uint32_t) L.p0;
     const T *packed = (const T *) L.packed;     /* element 0 is packed byte p0 */
     char *typed = L.typed + L.desc.base;
     for (; u0 < nunits; u0 += U * nthr) {
-        int64_t x[U];
+        OFF x[U];
         T in[U];
 #pragma unroll
         for (int k = 0; k < U; k++) {
             const uint32_t u = u0 + k * nthr;
             if (u < nunits) {
                 const uint32_t p = p0 + u * es;
-                const uint32_t b = yk_div(p, lv);
-                int64_t at;
-                if constexpr (K != YK_LV_IDX)
-                    at = (int64_t) b * lv.stride;
-                else if constexpr (D32)
-                    at = __ldg((const int32_t *) (lv.disp + lv.count) + b);
-                else
-                    at = __ldg(lv.disp + b);
-                x[k] = at + (int64_t) (p - b * (uint32_t) lv.cps);
+                if constexpr (P2X) {
+                    const uint32_t b = p >> lv.l;
+                    x[k] = __ldg((const int32_t *) (lv.disp + lv.count) + b) +
+                        (int32_t) (p & ((uint32_t) lv.cps - 1u));
+                } else {
+                    const uint32_t b = yk_div(p, lv);
+                    int64_t at;
+                    if constexpr (K != YK_LV_IDX)
+                        at = (int64_t) b * lv.stride;
+                    else if constexpr (D32)
+                        at = __ldg((const int32_t *) (lv.disp + lv.count) + b);
+                    else
+                        at = __ldg(lv.disp + b);
+                    x[k] = at + (int64_t) (p - b * (uint32_t) lv.cps);
+                }
                 in[k] = __ldg(packed + u);
             }
         }
 #pragma unroll
         for (int k = 0; k < U; k++)
             if (u0 + k * nthr < nunits)
-                yk_red<OP>((T *) (typed + x[k]), in[k]);
+                yk_red<OP>((T *) (typed + (int64_t) x[k]), in[k]);
     }
 }
 

@@ -532,11 +532,11 @@ yk_owner_chunk_kernel(const __grid_constant__ yk_launch L, int rshift)
 
 
 /* yk_red_units over the whole request, grid-stride */
-template <int BT, int OP, int K, bool D32>
+template <int BT, int OP, int K, bool D32, bool P2X>
 __global__ void __launch_bounds__(YK_THREADS)
 yk_red_kernel(const __grid_constant__ yk_launch L)
 {
-    yk_red_units<BT, OP, K, D32>(L, blockIdx.x * YK_THREADS + threadIdx.x,
+    yk_red_units<BT, OP, K, D32, 4, P2X>(L, blockIdx.x * YK_THREADS + threadIdx.x,
                                  (uint32_t) (L.nbytes / sizeof(typename yk_elem<BT>::T)),
                                  gridDim.x * YK_THREADS);
 }
@@ -961,7 +961,7 @@ extern "C" int yk_cuda_owner_form(const yk_launch * l, int sorted_blocks)
                 (uintptr_t) c.packed % cw == 0)
                 chunk = cw;
     }
-    const bool d32 = (sorted_blocks & YK_ORD_D32) != 0 && c.desc.lv[0].has_d32;
+    const bool d32 = (sorted_blocks & YK_ORD_D32) != 0 && (c.desc.lv[0].has_d32 & YK_D32_TABLE);
     return rshift | (chunk << 8) | (d32 ? YK_FORM_D32 : 0) | YK_FORM_POW2;
 }
 
@@ -1010,11 +1010,11 @@ extern "C" int yk_cuda_launch_runs_pack(const yk_launch * l, uint32_t run, void 
 
 /* yk_red_kernel for a 4- or 8-byte integer type and an operator that yk_red_applies()
  * accepts; false when the launch does not fit it */
-template <int BT, int K, bool D32>
+template <int BT, int K, bool D32, bool P2X = false>
 static bool yk_red_launch_bt(const yk_launch & c, cudaStream_t s, unsigned g)
 {
     switch ((int) c.op) {
-#define YK_RD(O) case O: yk_red_kernel<BT, O, K, D32><<<g, YK_THREADS, 0, s>>>(c); return true
+#define YK_RD(O) case O: yk_red_kernel<BT, O, K, D32, P2X><<<g, YK_THREADS, 0, s>>>(c); return true
         YK_RD(OP_MAX); YK_RD(OP_MIN); YK_RD(OP_SUM); YK_RD(OP_BAND); YK_RD(OP_BOR); YK_RD(OP_BXOR);
 #undef YK_RD
     }
@@ -1036,10 +1036,13 @@ static bool yk_red_launch(const yk_launch & c, int bt, cudaStream_t s, int cap)
         return false;
     const uint64_t units = c.nbytes / (uint64_t) yk_bt_size(bt);
     const unsigned g = yk_grid(units, (uint64_t) YK_THREADS * 4, cap > 0 ? cap : 8);
-    /* IDX: the 32-bit copy of the displacements when the level has one */
-    const bool d32 = k == YK_LV_IDX && c.desc.lv[0].has_d32;
+    /* IDX: the 32-bit copy of the displacements when the level has one; for 4-byte
+     * integers also a shift and 32-bit offsets where yk_red_p2x() holds (for 8-byte ones
+     * that form measured slower: int64 MAX 120.8 against 110.6 us) */
+    const bool d32 = k == YK_LV_IDX && (c.desc.lv[0].has_d32 & YK_D32_TABLE);
     if (bt == YK_BT_I32)
         return k != YK_LV_IDX ? yk_red_launch_bt<YK_BT_I32, YK_LV_VEC, false>(c, s, g) :
+            yk_red_p2x(c.desc.lv[0]) ? yk_red_launch_bt<YK_BT_I32, YK_LV_IDX, true, true>(c, s, g) :
             d32 ? yk_red_launch_bt<YK_BT_I32, YK_LV_IDX, true>(c, s, g) :
             yk_red_launch_bt<YK_BT_I32, YK_LV_IDX, false>(c, s, g);
     return k != YK_LV_IDX ? yk_red_launch_bt<YK_BT_I64, YK_LV_VEC, false>(c, s, g) :

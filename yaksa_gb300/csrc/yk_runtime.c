@@ -583,11 +583,13 @@ static int prepare_with(const yk_plan * p, char *typed, char *packed, yk_launch 
             L->desc.lv[0].cps < (1ull << 32) && yk_red_applies(L->desc.leaf_type, L->op)) {
             /* equal blocks, in any order or at a stride under their length, under an
              * order-independent integer operator: L2 reductions, when both sides sit on
-             * the element size */
+             * the element size and the target is device memory (probed at the lowest
+             * byte the request touches: the typed pointer itself may lie outside any
+             * allocation, as with absolute displacements) */
             uint64_t es = (uint64_t) yk_base_type_size(L->desc.leaf_type);
             uint64_t a = (uint64_t) (uintptr_t) (typed + L->desc.base) | (uint64_t) (uintptr_t) packed |
                 b0 | (uint64_t) ddo->elem_align;
-            if (es && (a % es) == 0 && (uint64_t) ddo->elem_align >= es && device_memory(typed))
+            if (es && (a % es) == 0 && (uint64_t) ddo->elem_align >= es && device_memory(typed + p->lo))
                 *sorted |= YK_ORD_RED;
         }
         if (!L->typed_op && !*sorted)

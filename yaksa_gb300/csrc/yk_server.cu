@@ -175,19 +175,29 @@ __device__ __noinline__ void yk_srv_runs(const yk_launch & L, uint64_t ib, uint6
 /* overlapping equal blocks under an order-independent integer operator (the launch
  * form is yk_red_kernel, with 32-bit positions): elements [ub, ue) of the request, one
  * out-of-line function per level form */
-template <int BT, int OP, int K, bool D32>
+template <int BT, int OP, int K, bool D32, bool P2X = false>
 __device__ __noinline__ void yk_srv_red_k(const yk_launch & L, uint64_t ub, uint64_t ue)
 {
-    yk_red_units<BT, OP, K, D32>(L, (uint32_t) ub + threadIdx.x, (uint32_t) ue, YK_THREADS);
+    yk_red_units<BT, OP, K, D32, 4, P2X>(L, (uint32_t) ub + threadIdx.x, (uint32_t) ue, YK_THREADS);
 }
 
 template <int BT, int OP>
 __device__ __forceinline__ void yk_srv_red_t(const yk_launch & L, uint64_t ub, uint64_t ue)
 {
     const yk_level & lv = L.desc.lv[0];
-    if (lv.kind != YK_LV_IDX)
+    if (lv.kind != YK_LV_IDX) {
         yk_srv_red_k<BT, OP, YK_LV_VEC, false>(L, ub, ue);
-    else if (lv.has_d32)
+        return;
+    }
+    /* the launch's choice of form: the shift and 32-bit offsets for 4-byte integers
+     * (server bursts of 16 uint32 BXOR requests of 16 MiB: 572-595 -> 666 GB/s) */
+    if constexpr (BT == YK_BT_I32) {
+        if (yk_red_p2x(lv)) {
+            yk_srv_red_k<BT, OP, YK_LV_IDX, true, true>(L, ub, ue);
+            return;
+        }
+    }
+    if (lv.has_d32 & YK_D32_TABLE)
         yk_srv_red_k<BT, OP, YK_LV_IDX, true>(L, ub, ue);
     else
         yk_srv_red_k<BT, OP, YK_LV_IDX, false>(L, ub, ue);
