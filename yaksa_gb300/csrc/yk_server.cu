@@ -76,7 +76,7 @@ __device__ __noinline__ void yk_srv_owner(const yk_launch & L, uint64_t ub, uint
     }
 }
 
-/* Sorted blocks with both sides aligned to the element size, in the form the host
+/* Sorted blocks with both sides aligned to the element size, from the form the host
  * chose with yk_cuda_owner_form (yk_launch.form): the body of yk_owner_chunk_kernel or
  * yk_owner_lane_kernel over elements [ub, ue) of the request, with 32-bit target
  * offsets, one out-of-line function per form.  The host cuts chunked items on the chunk
@@ -96,18 +96,17 @@ __device__ __noinline__ void yk_srv_owner_lane(const yk_launch & L, uint64_t ub,
                                       YK_THREADS);
 }
 
+/* The chunk form for 8-byte integers only.  In the server every invariant of the item
+ * takes a thread register (the record is in shared memory, not the constant bank), and
+ * there the per-lane form measured faster for the other types (bursts of 16 requests of
+ * 16 MiB, GB/s chunked -> per lane): complex PROD 600 -> 890, float SUM 436 -> 458,
+ * int32 PROD 442 -> 460, int16 SUM 261 -> 272; int64 PROD 696 chunked, 643 per lane. */
 template <int BT, int OP>
 __device__ __forceinline__ void yk_srv_owner_t(const yk_launch & L, uint64_t ub, uint64_t ue)
 {
-    constexpr uint32_t es = (uint32_t) sizeof(typename yk_elem<BT>::T);
-    const int cw = (L.form >> 8) & 255;
-    if constexpr (es == 4 || (es == 8 && BT != YK_BT_F64)) {
-        if (cw == 16)
+    if constexpr (BT == YK_BT_I64) {
+        if (((L.form >> 8) & 255) == 16)
             return yk_srv_owner_chunk<BT, OP, 16>(L, ub, ue);
-    }
-    if constexpr (es < 8) {
-        if (cw == 8)
-            return yk_srv_owner_chunk<BT, OP, 8>(L, ub, ue);
     }
     yk_srv_owner_lane<BT, OP>(L, ub, ue);
 }
@@ -175,10 +174,13 @@ __device__ __noinline__ void yk_srv_runs(const yk_launch & L, uint64_t ib, uint6
 /* overlapping equal blocks under an order-independent integer operator (the launch
  * form is yk_red_kernel, with 32-bit positions): elements [ub, ue) of the request, one
  * out-of-line function per level form */
+/* two elements per lane for 8-byte integers (fewer live registers: int64 MAX bursts
+ * 785-819 -> 873-881 GB/s), four for 4-byte ones */
 template <int BT, int OP, int K, bool D32, bool P2X = false>
 __device__ __noinline__ void yk_srv_red_k(const yk_launch & L, uint64_t ub, uint64_t ue)
 {
-    yk_red_units<BT, OP, K, D32, 4, P2X>(L, (uint32_t) ub + threadIdx.x, (uint32_t) ue, YK_THREADS);
+    yk_red_units<BT, OP, K, D32, (BT == YK_BT_I64 ? 2 : 4), P2X>(L, (uint32_t) ub + threadIdx.x,
+                                                                (uint32_t) ue, YK_THREADS);
 }
 
 template <int BT, int OP>
