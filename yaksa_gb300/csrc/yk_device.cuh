@@ -818,7 +818,7 @@ __device__ __forceinline__ void yk_red_units(const yk_launch & L, uint32_t u0, u
  * each block's target run is read and written by consecutive lanes.  This thread's
  * elements are u0, u0 + nthr, ... below nunits, counted from packed byte p0; ownership
  * is decided against the whole request's range [p0, p0 + nbytes). */
-template <int BT, int OP, bool D32>
+template <int BT, int OP, bool D32, int UO = 0>
 __device__ __forceinline__ void yk_owner_lane_units(const yk_launch & L, int rshift, uint32_t u0,
                                                     uint32_t nunits, uint32_t nthr)
 {
@@ -828,9 +828,9 @@ __device__ __forceinline__ void yk_owner_lane_units(const yk_launch & L, int rsh
     typedef typename std::conditional<D32, int32_t, int64_t>::type OFF;
     constexpr OFF OFF_MAX = D32 ? (OFF) INT32_MAX : (OFF) INT64_MAX;
     constexpr uint32_t es = (uint32_t) sizeof(T);
-    /* elements per lane, loads issued together (complex pairs keep one, within the
-     * register budget of full occupancy) */
-    constexpr int U = (BT == YK_BT_C32 || BT == YK_BT_C64) ? 1 : 2;
+    /* elements per lane, loads issued together: UO when the caller sets it, else two
+     * (complex pairs keep one, within the register budget of full occupancy) */
+    constexpr int U = UO ? UO : (BT == YK_BT_C32 || BT == YK_BT_C64) ? 1 : 2;
     const uint32_t R = 1u << rshift;
     const yk_level & lv = L.desc.lv[0];
     const uint32_t p0 = (uint32_t) L.p0, p1 = (uint32_t) (L.p0 + L.nbytes);

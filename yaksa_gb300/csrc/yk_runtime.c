@@ -1781,12 +1781,8 @@ static int server_plan(yaksa_gb300_pup_t * o, yaksa_info_t info, yk_srv_req * q)
         skind = red ? YK_SRV_RED : (sorted & 3) == 2 ? YK_SRV_OWNER_T : owner ? YK_SRV_OWNER :
             YK_SRV_ORDERED;
         gran = red || owner ? (uint64_t) yk_base_type_size(L.desc.leaf_type) : (uint64_t) L.vec;
-        if (skind == YK_SRV_OWNER_T) {
-            /* the launch kernels' form; chunked forms cut items on the chunk width */
-            L.form = yk_cuda_owner_form(&L, sorted);
-            if ((L.form >> 8) & 255)
-                gran = (uint64_t) ((L.form >> 8) & 255);
-        }
+        if (skind == YK_SRV_OWNER_T)
+            L.form = yk_cuda_owner_form(&L, sorted);   /* block shift, 32-bit offsets */
     }
     q->L = L;
     q->skind = skind;

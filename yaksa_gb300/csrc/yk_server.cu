@@ -76,39 +76,20 @@ __device__ __noinline__ void yk_srv_owner(const yk_launch & L, uint64_t ub, uint
     }
 }
 
-/* Sorted blocks with both sides aligned to the element size, from the form the host
- * chose with yk_cuda_owner_form (yk_launch.form): the body of yk_owner_chunk_kernel or
- * yk_owner_lane_kernel over elements [ub, ue) of the request, with 32-bit target
- * offsets, one out-of-line function per form.  The host cuts chunked items on the chunk
- * width, so an item's first element starts a chunk. */
-template <int BT, int OP, int CW>
-__device__ __noinline__ void yk_srv_owner_chunk(const yk_launch & L, uint64_t ub, uint64_t ue)
-{
-    constexpr uint32_t es = (uint32_t) sizeof(typename yk_elem<BT>::T);
-    yk_owner_chunk_units<BT, OP, CW, true>(L, L.form & 255, (uint32_t) (ub * es / CW) + threadIdx.x,
-                                           (uint32_t) (ue * es / CW), YK_THREADS);
-}
-
+/* Sorted blocks with both sides aligned to the element size, with the block shift and
+ * 32-bit offsets of the form the host chose with yk_cuda_owner_form (yk_launch.form):
+ * the body of yk_owner_lane_kernel over elements [ub, ue) of the request, one element
+ * per lane.  In the server every invariant of an item takes a thread register (the
+ * record is in shared memory, not the constant bank), and there fewer live values win:
+ * bursts of 16 requests of 16 MiB, GB/s with the launch kernels' forms (16-byte chunks,
+ * or two elements per lane) -> this form: double SUM 652 -> 812-841, complex PROD
+ * 600 -> 890-906, float SUM 464 -> 646-661, int32 PROD 456 -> 650-662, int16 SUM
+ * 272 -> 428, int64 PROD 794-797 (chunks) -> 858-866. */
 template <int BT, int OP>
-__device__ __noinline__ void yk_srv_owner_lane(const yk_launch & L, uint64_t ub, uint64_t ue)
+__device__ __noinline__ void yk_srv_owner_t(const yk_launch & L, uint64_t ub, uint64_t ue)
 {
-    yk_owner_lane_units<BT, OP, true>(L, L.form & 255, (uint32_t) ub + threadIdx.x, (uint32_t) ue,
-                                      YK_THREADS);
-}
-
-/* The chunk form for 8-byte integers only.  In the server every invariant of the item
- * takes a thread register (the record is in shared memory, not the constant bank), and
- * there the per-lane form measured faster for the other types (bursts of 16 requests of
- * 16 MiB, GB/s chunked -> per lane): complex PROD 600 -> 890, float SUM 436 -> 458,
- * int32 PROD 442 -> 460, int16 SUM 261 -> 272; int64 PROD 696 chunked, 643 per lane. */
-template <int BT, int OP>
-__device__ __forceinline__ void yk_srv_owner_t(const yk_launch & L, uint64_t ub, uint64_t ue)
-{
-    if constexpr (BT == YK_BT_I64) {
-        if (((L.form >> 8) & 255) == 16)
-            return yk_srv_owner_chunk<BT, OP, 16>(L, ub, ue);
-    }
-    yk_srv_owner_lane<BT, OP>(L, ub, ue);
+    yk_owner_lane_units<BT, OP, true, 1>(L, L.form & 255, (uint32_t) ub + threadIdx.x, (uint32_t) ue,
+                                         YK_THREADS);
 }
 
 /* the compile-time instances of a base type: SUM, PROD, MAX, MIN (not complex) and
@@ -137,8 +118,8 @@ __device__ __forceinline__ bool yk_srv_owner_bt(const yk_launch & L, uint64_t ub
     return false;
 }
 
-/* aligned sorted blocks: the launch kernels' bodies where the request has their form
- * with 32-bit offsets and the operator an instance, else the generic item */
+/* aligned sorted blocks: the per-lane body where the blocks are a power of two long,
+ * the offsets fit in 32 bits and the operator has an instance, else the generic item */
 __device__ __noinline__ void yk_srv_owner_typed(const yk_launch & L, uint64_t ub, uint64_t ue)
 {
     bool done = false;
@@ -174,13 +155,12 @@ __device__ __noinline__ void yk_srv_runs(const yk_launch & L, uint64_t ib, uint6
 /* overlapping equal blocks under an order-independent integer operator (the launch
  * form is yk_red_kernel, with 32-bit positions): elements [ub, ue) of the request, one
  * out-of-line function per level form */
-/* two elements per lane for 8-byte integers (fewer live registers: int64 MAX bursts
- * 785-819 -> 873-881 GB/s), four for 4-byte ones */
+/* two elements per lane, not the launch kernel's four: fewer live registers (bursts of
+ * 16 requests of 16 MiB: int64 MAX 785-819 -> 873-898 GB/s, uint32 BXOR 679 -> 722) */
 template <int BT, int OP, int K, bool D32, bool P2X = false>
 __device__ __noinline__ void yk_srv_red_k(const yk_launch & L, uint64_t ub, uint64_t ue)
 {
-    yk_red_units<BT, OP, K, D32, (BT == YK_BT_I64 ? 2 : 4), P2X>(L, (uint32_t) ub + threadIdx.x,
-                                                                (uint32_t) ue, YK_THREADS);
+    yk_red_units<BT, OP, K, D32, 2, P2X>(L, (uint32_t) ub + threadIdx.x, (uint32_t) ue, YK_THREADS);
 }
 
 template <int BT, int OP>
