@@ -107,7 +107,8 @@ typedef struct {
     int32_t dir;                /* 0 = pack, 1 = unpack */
     int32_t vec;                /* bytes per work unit (REPLACE) or unit granule (ops) */
     int32_t typed_op;           /* 1 = elementwise operator on typed descriptor */
-    int32_t use64;              /* 1 = positions need 64-bit arithmetic */
+    int32_t use64;              /* 1 = positions need 64-bit arithmetic (the packed end
+                                 * is above YK_POS32_END) */
     int32_t regular;            /* 0..YK_REGULAR_MAX: that many VEC levels over a RUN leaf
                                  * with 32-bit positions; -1: any other shape */
     int32_t hidx;               /* 1: one HIDX level of contiguous blocks over its run */
@@ -117,6 +118,12 @@ typedef struct {
 } yk_launch;
 
 #define YK_REGULAR_MAX 3
+
+/* The largest packed end position the 32-bit kernels take.  Their loops step a 32-bit
+ * unit index by a grid's stride (at most 64 CTAs per SM of 256 threads, one unit each:
+ * under 2^24 units); ending 2^24 below 2^32 keeps index + stride from wrapping, which
+ * would restart the loop and never end it. */
+#define YK_POS32_END (0xffffffffull - (1ull << 24))
 
 /* Up to YK_BATCH_MAX REPLACE requests with 32-bit positions in one launch; passed by
  * value as the kernel parameter (about 19 KB, under the 32 KB parameter limit). */

@@ -296,11 +296,12 @@ yk_hidx_unpack_bulk_kernel(const __grid_constant__ yk_launch L)
 }
 
 /* the bulk-staged unpack of a contiguous-block hindexed request: -1 when it does not
- * apply (not an unpack, packed pointer off 16 bytes, 4 GiB or more), else a cudaError_t */
+ * apply (not an unpack, packed pointer off 16 bytes, above YK_POS32_END bytes), else a
+ * cudaError_t */
 extern "C" int yk_cuda_launch_hidx_bulk(const yk_launch * l, void *stream, int ctas_per_sm)
 {
     if (l->typed_op || !l->hidx || l->dir != 1 || ((uintptr_t) l->packed & 15) ||
-        l->nbytes == 0 || l->nbytes > 0xffffffffull)
+        l->nbytes == 0 || l->nbytes > YK_POS32_END)
         return -1;
     yk_tma_count_launch();
     const uint64_t ntiles = (l->nbytes + YK_HB_TILE - 1) / YK_HB_TILE;
@@ -798,7 +799,7 @@ static void yk_launch_hidx32_shape(const yk_launch * l, cudaStream_t s, int unit
 template <int V>
 static void yk_launch_hidx(const yk_launch * l, cudaStream_t s, int units, int ctas_per_sm)
 {
-    if (l->nbytes > 0xffffffffull) {
+    if (l->nbytes > YK_POS32_END) {
         const unsigned g = yk_hidx_grid(l, ctas_per_sm > 0 ? ctas_per_sm : 8);
         if (l->dir == 0)
             yk_hidx_kernel<V, 0><<<g, YK_THREADS, 0, s>>>(*l);

@@ -506,7 +506,7 @@ static int prepare_with(const yk_plan * p, char *typed, char *packed, yk_launch 
     L->nbytes = n;
     L->op = op;
     L->dir = p->dir;
-    L->use64 = (p->b1 > 0xffffffffull);
+    L->use64 = (p->b1 > YK_POS32_END);
     L->ldouble = t->needs_host_ops;
     *sorted = 0;
     if (op == YAKSA_OP__REPLACE && t->is_contig) {
@@ -1760,7 +1760,7 @@ static int server_plan(yaksa_gb300_pup_t * o, yaksa_info_t info, yk_srv_req * q)
         v = YK_MIN(v, pow2_of(p.b0));
         v = YK_MIN(v, pow2_of(p.b1 - p.b0));
         L.vec = v;
-        L.use64 = p.b1 > 0xffffffffull;
+        L.use64 = p.b1 > YK_POS32_END;
         skind = L.use64 ? YK_SRV_BYTES : YK_SRV_REGULAR;
         gran = (uint64_t) v;
     } else if (kind == YK_X_BYTES && runs_pack_ok(&L) && (uintptr_t) L.packed % 16 == 0 &&
