@@ -236,6 +236,49 @@ def test_server_large_requests_split(cuda, prod, oracle):
     srv.destroy()
 
 
+SB_BASES = [("int8", yk.TYPE_INT8_T), ("int16", yk.TYPE_INT16_T), ("int32", yk.TYPE_INT32_T),
+            ("int64", yk.TYPE_INT64_T), ("float", yk.TYPE_FLOAT), ("double", yk.TYPE_DOUBLE),
+            ("c_complex", yk.TYPE_C_COMPLEX), ("c_double_complex", yk.TYPE_C_DOUBLE_COMPLEX)]
+
+
+@pytest.mark.parametrize("base,h", SB_BASES)
+@pytest.mark.parametrize("bl", [8, 3])
+def test_server_sorted_block_items(cuda, prod, oracle, base, h, bl):
+    """Unpacks into overlapping sorted blocks through the server, for every base type of
+    its sorted-block items and each of SUM, PROD, MAX, MIN and REPLACE that the type has:
+    blocks of 8 elements (a power of two in bytes: the per-lane item with 32-bit offsets,
+    or the L2-reduction item for 4- and 8-byte integers) and of 3 (the generic item).
+    About four blocks cover each element; the requests, each cut into many items, run
+    together, and each matches the oracle."""
+    rng = np.random.default_rng(bl * 100 + h)
+    nblk = 1 << 14
+    offs = np.sort(rng.integers(0, nblk * bl // 4, nblk)).astype(np.int64)
+    names = [o for o in ("sum", "prod", "max", "min", "replace") if o in VALID_OPS[base]]
+    tp = prod.type_create_indexed_block_array(nblk, bl, offs.ctypes.data, h)
+    to = oracle.type_create_indexed_block_array(nblk, bl, offs.ctypes.data, h)
+    lo, hi, size = footprint(oracle, to, 1)
+    srv = yk.Server(prod)
+    reqs, ops = [], []
+    for name in names:
+        r = dict(op=yk.OP_NAMES[name], typed=fill(rng, hi - lo + 64, base),
+                 packed=fill(rng, size + 64, base))
+        r["t_g"], r["p_g"] = dev_copy(cuda, r["typed"]), dev_copy(cuda, r["packed"])
+        ops.append(yk.unpack_op(r["p_g"].data_ptr(), size, r["t_g"].data_ptr() + 32 - lo, 1, tp, 0,
+                                op=r["op"]))
+        reqs.append(r)
+    for t in submit_all(srv, ops):
+        srv.wait(t)
+    cuda.cuda.synchronize()
+    for r, o, name in zip(reqs, ops, names):
+        th = r["typed"].copy()
+        a = oracle.unpack(r["packed"].ctypes.data, size, th.ctypes.data + 32 - lo, 1, to, 0, op=r["op"])
+        assert o.actual == a == size
+        assert_same_bytes(host_of(cuda, r["t_g"]), th, f"server sorted blocks {base} {name} bl {bl}")
+    srv.destroy()
+    prod.type_free(tp)
+    oracle.type_free(to)
+
+
 @pytest.mark.parametrize("env", [{"YAKSA_GB300_SERVER_ITEM_KIB": "16", "YAKSA_GB300_SERVER_MIN_ITEMS": "0"},
                                  {"YAKSA_GB300_SERVER_MIN_ITEMS": "1024"}])
 def test_server_item_sizes(cuda, env):
