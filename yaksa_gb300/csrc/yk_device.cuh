@@ -555,7 +555,7 @@ __host__ __device__ __forceinline__ int yk_bt_size(int bt)
     }
 }
 
-/* element types in registers, for the typed ordered-unpack kernel */
+/* element types in registers, for the typed kernels (ordered unpacks, L2 reductions) */
 template <int BT> struct yk_elem;
 template <> struct yk_elem<YK_BT_I8> {
     typedef int8_t T;
@@ -631,12 +631,12 @@ template <int OP> __device__ __forceinline__ void yk_red(int64_t *p, int64_t v)
     else atomicXor(q, (unsigned long long) v);
 }
 
-/* The contiguous-block hindexed walk (yk_hidx_kernel) for ranges under 4 GiB: the groups
- * of 32 blocks that meet the packed range [p0, p1) (a launch's whole request, or one
- * server item), warp `warp` of `nwarps` taking every nwarps-th group.  Positions are
- * relative to each group's first byte: 32-bit search keys (one shuffle per step instead
- * of two) and per-lane state small enough for every warp slot of the SM to stay
- * resident.  Lane k keeps its block's start relative to the group (0 for a block that
+/* The contiguous-block hindexed walk (yk_hidx_kernel) for ranges of up to YK_POS32_END
+ * bytes: the groups of 32 blocks that meet the packed range [p0, p1) (a launch's whole
+ * request, or one server item), warp `warp` of `nwarps` taking every nwarps-th group.
+ * Positions are relative to each group's first byte: 32-bit search keys (one shuffle
+ * per step instead of two) and per-lane state small enough for every warp slot of the SM
+ * to stay resident.  Lane k keeps its block's start relative to the group (0 for a block that
  * starts before the range) and the typed offset of relative position 0 in that block,
  * so a unit's typed offset is one shuffle and one add.
  *
@@ -738,6 +738,14 @@ __device__ __forceinline__ void yk_hidx32_groups(const yk_launch & L, uint64_t p
     }
 }
 
+/* yk_red_units' P2X form applies: an IDX level with its 32-bit table, every target
+ * offset in 32 bits and blocks of a power-of-two length */
+__host__ __device__ inline bool yk_red_p2x(const yk_level & lv)
+{
+    return lv.kind == YK_LV_IDX && (lv.has_d32 & YK_D32_TABLE) && (lv.has_d32 & YK_D32_OFFSETS) &&
+        lv.cps && (lv.cps & (lv.cps - 1)) == 0;
+}
+
 /* Overlapping blocks of R bytes (one IDX level in any block order, or one VEC level
  * whose stride is under its block) under one of those operators:
  * every packed element in the range is folded into its target element by one L2
@@ -751,14 +759,6 @@ __device__ __forceinline__ void yk_hidx32_groups(const yk_launch & L, uint64_t p
  * sector request per 32 bytes).  Both sides are aligned to the element size (checked
  * on the host).  K: the level's kind (IDX or VEC); D32: the IDX level's 32-bit copy of
  * its displacements. */
-/* yk_red_units' P2X form applies: an IDX level with its 32-bit table, every target
- * offset in 32 bits and blocks of a power-of-two length */
-__host__ __device__ inline bool yk_red_p2x(const yk_level & lv)
-{
-    return lv.kind == YK_LV_IDX && (lv.has_d32 & YK_D32_TABLE) && (lv.has_d32 & YK_D32_OFFSETS) &&
-        lv.cps && (lv.cps & (lv.cps - 1)) == 0;
-}
-
 template <int BT, int OP, int K, bool D32, int U = 4, bool P2X = false>
 __device__ __forceinline__ void yk_red_units(const yk_launch & L, uint32_t u0, uint32_t nunits,
                                              uint32_t nthr)
@@ -810,7 +810,7 @@ __device__ __forceinline__ void yk_red_units(const yk_launch & L, uint32_t u0, u
 
 /* Sorted blocks of a power-of-two byte length R, one packed element per lane (32-bit
  * positions), operator fixed at compile time.  The ownership rule of yk_owner_kernel
- * below: element x = disp[b] + j of block b belongs to b unless block b-1 covers x from
+ * (yk_kernels.cu): element x = disp[b] + j of block b belongs to b unless block b-1 covers x from
  * a position inside the range; no earlier block can cover x when b-1 does not, because
  * the displacements ascend.  The owner folds in the blocks b+1, b+2, ... that start at
  * or before x, in block order.  Lanes of one block read the same displacement words
