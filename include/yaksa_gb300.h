@@ -253,6 +253,13 @@ int yaksa_gb300_debug_locate(yaksa_type_t type, uintptr_t count, int typed, uint
 int yaksa_gb300_debug_desc_info(yaksa_type_t type, int typed, int *vec_align, int *unit,
                                 int *may_overlap, int *sorted_blocks, int *nlev);
 
+/* The 32-bit forms of a descriptor (typed = 1: the operator descriptor), computed on the
+ * host: level0_bits receives its first level's bits (1: the displacements fit in 32 bits
+ * and a 32-bit copy of them follows the table; 2: every displacement plus the block
+ * length fits as well), disp32 whether the sorted-block kernels may take every target
+ * offset in 32 bits. */
+int yaksa_gb300_debug_d32(yaksa_type_t type, int typed, int *level0_bits, int *disp32);
+
 #ifdef __cplusplus
 }
 #endif

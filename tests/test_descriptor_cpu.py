@@ -171,3 +171,37 @@ def test_vector_units_and_overlap_flag(prod, oracle, seed):
             for h in reversed(keep):
                 y.type_free(h)
     g.free()
+
+
+def d32_info(prod, h, typed=1):
+    f = prod.lib.yaksa_gb300_debug_d32
+    f.restype = ctypes.c_int
+    bits, d32 = ctypes.c_int(), ctypes.c_int()
+    assert f(ctypes.c_uint64(h), typed, ctypes.byref(bits), ctypes.byref(d32)) == 0
+    return bits.value, d32.value
+
+
+@pytest.mark.parametrize("case,expect", [("small_sorted", (3, 1)), ("small_unsorted", (3, 0)),
+                                         ("offset_over", (1, 0)), ("table_over", (0, 0)),
+                                         ("negative", (3, 1))])
+def test_32bit_forms_at_the_limits(prod, case, expect):
+    """The descriptor's 32-bit forms at the edges of 32 bits, for overlapping blocks of 8
+    int32 (32 bytes): bit 1 (a 32-bit copy of the displacements), bit 2 (every
+    displacement plus the block fits too) and the sorted-block 32-bit-offset flag.  Byte
+    displacements near 0, in ascending or shuffled order; near 2^31 with one block
+    reaching past 2^31 - 1 (the table fits, the offsets do not); one displacement of 2^31
+    (no 32-bit table); and from -2^31 up."""
+    rng = np.random.default_rng(len(case))
+    start = {"small_sorted": 0, "small_unsorted": 0, "offset_over": (1 << 31) - 64 - 4096,
+             "table_over": (1 << 31) - 64 - 4096, "negative": -(1 << 31)}[case]
+    offs = np.sort(start + rng.integers(0, 1024, 300) * 4)
+    if case == "small_unsorted":
+        rng.shuffle(offs)
+    elif case == "offset_over":
+        offs = np.append(offs, (1 << 31) - 16)      # its last element ends at 2^31 + 15
+    elif case == "table_over":
+        offs = np.append(offs, 1 << 31)
+    h = prod.type_create_hindexed_block(8, offs.tolist(), yk.TYPE_INT32_T)
+    assert desc_info(prod, h, 1)["may_overlap"]
+    assert d32_info(prod, h) == expect
+    prod.type_free(h)

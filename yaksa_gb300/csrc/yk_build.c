@@ -892,6 +892,22 @@ int yaksa_gb300_debug_desc_info(yaksa_type_t type, int typed, int *vec_align, in
     return YAKSA_SUCCESS;
 }
 
+int yaksa_gb300_debug_d32(yaksa_type_t type, int typed, int *level0_bits, int *disp32)
+{
+    yk_type *t = yk_type_get(type);
+    if (!t)
+        return YAKSA_ERR__INTERNAL;
+    yk_devdesc dd;
+    memset(&dd, 0, sizeof(dd));
+    int rc = build(t, typed, &dd, 0);
+    free(dd.dev_tables);
+    if (rc)
+        return rc;
+    *level0_bits = dd.d.nlev > 0 ? dd.d.lv[0].has_d32 : 0;
+    *disp32 = dd.disp32;
+    return YAKSA_SUCCESS;
+}
+
 void yk_desc_release(yk_type * t)
 {
     yk_iov_release(t);
